@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 NUFFT engine on the headline workload.
+
+Workload (one "step"): a 3D type-2 then type-1 round trip in complex64 /
+float32 on M = 10,000,000 points -- half iid uniform in [-pi, pi)^3, half
+Gaussian (sigma 0.1) around the origin -- with 256^3 modes, eps = 1e-5:
+    c = nufft2(f, x, y, z, iflag=-1);   g = nufft1((256,)*3, c, x, y, z, iflag=+1)
+Each transform sorts its points (setpts) and executes, as one call of the
+reference's drop-in path does (lib/kernels.cc.cu:57-80).  Inputs are seeded
+synthetic data with the shapes and distributions of the workload.
+
+Metric: NU points/s/transform = 2*M / t_step.  `value` is measured with all
+inputs resident in HBM (plan API: gbn_setpts + gbn_execute); `e2e` goes
+through the reference-facing C-ABI entry points (gbn_nufft3d2f,
+gbn_nufft3d1f) with pinned host buffers, the host->device copies of points
+and modes and the device->host copy of the result inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the algorithm (the oracle
+port: C/OpenMP spreading + scipy pocketfft) on the host cores: the
+reference's own FINUFFT cannot be built here (empty submodule).
+"""
+import argparse
+import ctypes
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "jax-finufft_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+M_POINTS = 10_000_000
+N_MODES = 256
+EPS = 1e-5
+SEED = 20261203
+METRIC = "NU points/s/transform"
+UNIT = "points/s"
+WORKLOAD = ("3D type-2 + type-1 round trip, complex64, M=1e7 points (half U[-pi,pi)^3, half "
+            "N(0,0.1^2)^3), 256^3 modes, eps=1e-5")
+
+
+def make_inputs(M=M_POINTS, N=N_MODES, seed=SEED):
+    rng = np.random.default_rng(seed)
+    h = M // 2
+    pts = np.empty((3, M), dtype=np.float32)
+    for d in range(3):
+        pts[d, :h] = rng.uniform(-np.pi, np.pi, h)
+        pts[d, h:] = rng.normal(0.0, 0.1, M - h)
+    f = np.empty((N, N, N), dtype=np.complex64)
+    f.real = rng.standard_normal((N, N, N), dtype=np.float32)
+    f.imag = rng.standard_normal((N, N, N), dtype=np.float32)
+    return pts, f
+
+
+def algorithmic_bytes(M, nf_total, T=1, d=3, s_r=4, s_c=8):
+    """Spread or interp: read coordinates and strengths, touch the grid once."""
+    return M * d * s_r + T * M * s_c + T * nf_total * s_c
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch from a committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                m = re.match(r"\s*%s\s+dram_bytes_per_launch\s+([0-9.eE+]+)" % kernel, line)
+                if m:
+                    return float(m.group(1))
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# CPU arm (oracle port)
+# ---------------------------------------------------------------------------
+def cpu_round_trip(M):
+    """One round trip of the CPU restatement on M points of the workload."""
+    from oracle import cpu_nufft
+
+    pts, f = make_inputs(M=M)
+    t0 = time.perf_counter()
+    c = cpu_nufft.nufft2(f, *pts, eps=EPS, iflag=-1)
+    cpu_nufft.nufft1((N_MODES,) * 3, c, *pts, eps=EPS, iflag=1)
+    return time.perf_counter() - t0
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import cpu_nufft
+
+    cores = cpu_cores()
+    cpu_nufft.set_threads(cores)
+    budget_steps = args.steps + args.warmup
+    M = M_POINTS if budget_steps <= 13 else max(1_000_000, int(M_POINTS * 13 / budget_steps))
+    for _ in range(args.warmup):
+        cpu_round_trip(M)
+    times = [cpu_round_trip(M) for _ in range(args.steps)]
+    t = sum(times) / len(times)
+    value = 2 * M / t
+    sample = ("oracle port (C/OpenMP spread/interp + scipy pocketfft, FP64) on the full "
+              "workload" if M == M_POINTS else "oracle port on M=%d points of the workload "
+              "(same 256^3 grid)" % M)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "M_sample": M},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "FINUFFT (the reference's CPU library) is an empty submodule and cannot be "
+                "built; the CPU restatement of its algorithm stands in for it",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    from jax_finufft_gb300 import _native
+
+    lib = _native.load()
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    pts_h, f_h = make_inputs()
+    M, N = M_POINTS, N_MODES
+    x = [torch.from_numpy(pts_h[d]).to(dev) for d in range(3)]
+    f = torch.from_numpy(f_h).to(dev)
+    c = torch.empty(M, dtype=torch.complex64, device=dev)
+    g = torch.empty((N, N, N), dtype=torch.complex64, device=dev)
+
+    opts = _native.default_opts()
+    opts.debug = 1  # per-stage CUDA events, no host synchronisation
+    nm = (ctypes.c_int64 * 3)(N, N, N)
+    p2, p1 = ctypes.c_void_p(), ctypes.c_void_p()
+    _native.check(lib.gbnf_makeplan(2, 3, nm, -1, 1, EPS, ctypes.byref(p2), ctypes.byref(opts), sp))
+    _native.check(lib.gbnf_makeplan(1, 3, nm, 1, 1, EPS, ctypes.byref(p1), ctypes.byref(opts), sp))
+    xp = [ctypes.c_void_p(t.data_ptr()) for t in x]
+
+    def step():
+        _native.check(lib.gbnf_setpts(p2, M, xp[0], xp[1], xp[2], 0, None, None, None))
+        _native.check(lib.gbn_execute(p2, ctypes.c_void_p(c.data_ptr()),
+                                      ctypes.c_void_p(f.data_ptr())))
+        _native.check(lib.gbnf_setpts(p1, M, xp[0], xp[1], xp[2], 0, None, None, None))
+        _native.check(lib.gbn_execute(p1, ctypes.c_void_p(c.data_ptr()),
+                                      ctypes.c_void_p(g.data_ptr())))
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(v):
+        if ws == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ms5 = (ctypes.c_float * 5)()
+    nb = ctypes.c_int()
+    lib.gbn_get_timings(p2, ms5, ctypes.byref(nb))  # reset the per-stage sums
+    lib.gbn_get_timings(p1, ms5, ctypes.byref(nb))
+    launches0 = lib.gbn_launch_count()
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    launches = lib.gbn_launch_count() - launches0
+
+    _native.check(lib.gbn_get_timings(p2, ms5, ctypes.byref(nb)))
+    t2 = [ms5[i] / args.steps for i in range(5)]
+    _native.check(lib.gbn_get_timings(p1, ms5, ctypes.byref(nb)))
+    t1 = [ms5[i] / args.steps for i in range(5)]
+    nf3 = (ctypes.c_int64 * 3)()
+    w = ctypes.c_int()
+    lib.gbn_plan_info(p1, ctypes.byref(w), nf3, None, None)
+    nf_total = nf3[0] * nf3[1] * nf3[2]
+
+    ms_step = max_over_ranks(ms_step)
+    value = ws * 2 * M / (ms_step * 1e-3)
+
+    # ---- e2e through the reference-facing C-ABI entry points, host buffers
+    pin_pts = torch.from_numpy(pts_h).pin_memory()
+    pin_f = torch.from_numpy(f_h).pin_memory()
+    pin_out = torch.empty((N, N, N), dtype=torch.complex64).pin_memory()
+    d_pts = torch.empty((3, M), dtype=torch.float32, device=dev)
+    d_f = torch.empty((N, N, N), dtype=torch.complex64, device=dev)
+
+    def e2e_step():
+        d_pts.copy_(pin_pts, non_blocking=True)
+        d_f.copy_(pin_f, non_blocking=True)
+        common = (sp, ctypes.c_float(EPS))
+        px = [ctypes.c_void_p(d_pts[d].data_ptr()) for d in range(3)]
+        _native.check(lib.gbn_nufft3d2f(*common, -1, 1, 1, M, N, N, N, 0, 2.0, 0, 1, 1, 0, 0,
+                                        ctypes.c_void_p(d_f.data_ptr()), *px,
+                                        ctypes.c_void_p(c.data_ptr())))
+        _native.check(lib.gbn_nufft3d1f(*common, 1, 1, 1, M, N, N, N, 0, 2.0, 0, 1, 1, 0, 0,
+                                        ctypes.c_void_p(c.data_ptr()), *px,
+                                        ctypes.c_void_p(g.data_ptr())))
+        pin_out.copy_(g, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    e2e_value = ws * 2 * M / (e2e_ms * 1e-3)
+    h2d = pts_h.nbytes + f_h.nbytes
+    d2h = N * N * N * 8
+
+    # ---- roofline of the dominant point kernel (spread vs interp)
+    peak, peak_kind = measured_peak()
+    alg = algorithmic_bytes(M, nf_total)
+    spread_ms, interp_ms = t1[0], t2[0]
+    dom, dom_ms = ("spread", spread_ms) if spread_ms >= interp_ms else ("interp", interp_ms)
+    achieved = alg / (dom_ms * 1e-3) / 1e9
+    traffic = profile_traffic(dom)
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "M": M, "modes": [N, N, N], "eps": EPS,
+                   "kernel_width": w.value, "fine_grid": [nf3[0], nf3[1], nf3[2]],
+                   "l2": "inputs larger than L2 (fine grid 1.07 GB, points 120 MB)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "path": "gbn_nufft3d2f + gbn_nufft3d1f (C ABI), pinned host buffers"},
+        "gpu_launches": int(launches),
+        "stages_ms": {"type2": {"setpts": t2[4], "deconv": t2[2], "fft": t2[1], "interp": t2[0]},
+                      "type1": {"setpts": t1[4], "spread": t1[0], "fft": t1[1],
+                                "deconv": t1[2]}},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes": alg, "traffic": traffic,
+                     "other": {"spread_GBs": alg / (spread_ms * 1e-3) / 1e9,
+                               "interp_GBs": alg / (interp_ms * 1e-3) / 1e9}},
+    }
+    lib.gbn_destroy(p1)
+    lib.gbn_destroy(p2)
+
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle import cpu_nufft
+
+        cores = cpu_cores()
+        cpu_nufft.set_threads(cores)
+        t_cpu = cpu_round_trip(M_POINTS)
+        result["cpu_baseline"] = {
+            "value": 2 * M_POINTS / t_cpu, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "one full round trip of the workload on the oracle port "
+                      "(C/OpenMP + scipy pocketfft, FP64), %.1f s" % t_cpu}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,218 @@
+/*
+ * gbnufft.h -- C ABI of the GB300 (sm_103a) NUFFT library.
+ *
+ * The library replaces the GPU path jax-finufft reaches through
+ *   lib/jax_finufft_gpu.cc  ->  lib/kernels.cc.cu  ->  lib/cufinufft_wrapper.cc
+ *   ->  vendored cuFINUFFT.
+ * Every entry point takes plain pointers and sizes.  Device pointers are
+ * expected unless a function says otherwise; work is enqueued on the given
+ * CUDA stream and never synchronises the host except where noted
+ * (type-3 setpts reads the point extents back to size its grid).
+ *
+ * Return codes follow the reference's convention (lib/kernels.cc.cu:52-55,
+ * 70-79): 0 success, 1 warning (tolerance not reachable, clamped; results
+ * are still produced), >= 2 error.  gbn_last_error() returns a message for
+ * the calling thread's most recent non-zero code.
+ *
+ * Layouts are the reference backend's (lib/kernels.cc.cu:57-69,
+ * src/jax_finufft/lowering.py:96-105): row-major, dimension 1 ("x") is the
+ * fastest-varying mode axis, transforms stacked as (n_tot, n_transf, ...).
+ */
+#ifndef GBNUFFT_H
+#define GBNUFFT_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GBN_API __attribute__((visibility("default")))
+#else
+#define GBN_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define GBN_OK 0
+#define GBN_WARN_EPS_TOO_SMALL 1
+#define GBN_ERR_ARGS 2
+#define GBN_ERR_CUDA 3
+#define GBN_ERR_CUFFT 4
+#define GBN_ERR_ALLOC 5
+#define GBN_ERR_STATE 6
+
+/*
+ * Options.  The first seven fields are the ones the reference forwards to
+ * cuFINUFFT (src/jax_finufft/options.py:105-119, attrs at
+ * lib/jax_finufft_gpu.cc:28-60); the bin-size and subproblem fields are the
+ * GPU fields Opts carries but never forwards (options.py:69-77); the
+ * precision field selects the compute precision (0 = automatic split).
+ */
+typedef struct gbn_opts {
+  int modeord;            /* 0: modes -N/2..(N-1)/2; 1: FFT order */
+  double upsampfac;       /* sigma: 2.0 (default) or 1.25; 0 picks 2.0 */
+  int gpu_method;         /* 0 auto, 1 global-memory atomics over sorted points, 2 shared-memory subproblems */
+  int gpu_sort;           /* 1 bin-sort points (default); 0 keep input order (forces method 1) */
+  int gpu_kerevalmeth;    /* 1 piecewise Horner polynomials (default); 0 direct exp(sqrt) */
+  int gpu_maxbatchsize;   /* transforms per cuFFT batch; 0 = all (bounded by memory) */
+  int debug;              /* 1: time each stage with CUDA events (gbn_get_timings) */
+  int gpu_binsizex;       /* bin size per axis in fine-grid cells; 0 = default */
+  int gpu_binsizey;
+  int gpu_binsizez;
+  int gpu_maxsubprobsize; /* points per subproblem; 0 = default (1024) */
+  int gpu_precision;      /* compute precision: 0 = the data's (complex64 -> FP32, complex128 ->
+                             FP64, as cuFINUFFT); 1 = FP32; 2 = FP64 (complex128 only);
+                             3 = split rule: FP32 when eps >= 1e-6, FP64 otherwise.  Point
+                             folding and binning are FP64 in every mode. */
+} gbn_opts;
+
+/* Fill *o with the defaults (cuFINUFFT's, per options.py:66-79). */
+GBN_API void gbn_default_opts(gbn_opts* o);
+
+/* Opaque plan. */
+typedef struct gbn_plan_s* gbn_plan;
+
+/*
+ * Plan API.  Replaces cufinufft[f]_makeplan / _setpts / _execute / _destroy
+ * as bound by lib/cufinufft_wrapper.cc:48-99.  The gbn_* functions take
+ * complex128 data with float64 points, the gbnf_* functions complex64 data
+ * with float32 points.  nmodes is in backend order (x first); for type 3 it
+ * is ignored.  stream may be NULL (legacy default stream).
+ */
+GBN_API int gbn_makeplan(int type, int dim, const int64_t* nmodes, int iflag, int ntransf, double eps,
+                 gbn_plan* plan, const gbn_opts* opts, void* stream);
+GBN_API int gbnf_makeplan(int type, int dim, const int64_t* nmodes, int iflag, int ntransf, float eps,
+                  gbn_plan* plan, const gbn_opts* opts, void* stream);
+
+/* Set nonuniform points (device pointers; y/z may be NULL below their dim).
+ * Type 3 also takes N target frequencies s/t/u. */
+GBN_API int gbn_setpts(gbn_plan plan, int64_t M, const double* x, const double* y, const double* z,
+               int64_t N, const double* s, const double* t, const double* u);
+GBN_API int gbnf_setpts(gbn_plan plan, int64_t M, const float* x, const float* y, const float* z,
+                int64_t N, const float* s, const float* t, const float* u);
+
+/* Execute ntransf transforms.  Type 1: c (ntransf, M) -> f (ntransf, N...).
+ * Type 2: f -> c.  Type 3: c (ntransf, M) -> f (ntransf, N). */
+GBN_API int gbn_execute(gbn_plan plan, void* c, void* f);
+
+/* Change the stream later calls enqueue on. */
+GBN_API int gbn_set_stream(gbn_plan plan, void* stream);
+
+/* Release the plan (synchronises its stream first). */
+GBN_API int gbn_destroy(gbn_plan plan);
+
+/* Plan introspection: kernel width, fine-grid sizes (backend order) and the
+ * method actually used (1 or 2).  Any pointer may be NULL. */
+GBN_API int gbn_plan_info(gbn_plan plan, int* w, int64_t* nf3, int* method, int* compute_double);
+
+/* Per-stage device time (ms, CUDA events on the plan's stream) summed over
+ * every execute and setpts since the previous call, when the plan was made
+ * with opts.debug = 1: [0] spread (type 1) or interp (type 2), [1] FFT,
+ * [2] deconvolve, [3] type-3 phasing + spread, [4] setpts.  *nbatch (may be
+ * NULL) receives the number of executed batches summed.  Recording adds no
+ * host synchronisation; this call synchronises the stream and resets the
+ * sums. */
+GBN_API int gbn_get_timings(gbn_plan plan, float* ms5, int* nbatch);
+
+/* Copy the sorted per-point bin ids and the bin counts of the last setpts to
+ * host memory (test hook for bit-exact comparison with the CPU oracle).
+ * bins_out has M entries (bin of each input point, in input order);
+ * counts_out has nbins entries.  Returns the number of bins in *nbins.
+ * Either output may be NULL to query sizes.  Synchronises the stream. */
+GBN_API int gbn_debug_bins(gbn_plan plan, int64_t* bins_out, int64_t* counts_out, int64_t* nbins);
+
+/* Copy per-point grid starts (int64, M x 3, input order) and offsets delta
+ * (double, M x 3, input order) computed by setpts (test hook). */
+GBN_API int gbn_debug_fold(gbn_plan plan, int64_t* i0_out, double* delta_out);
+
+/* Thread-local message describing the last non-zero status. */
+GBN_API const char* gbn_last_error(void);
+
+/* Drop every cached plan held by the one-shot entry points. */
+GBN_API void gbn_clear_cache(void);
+
+/* Number of CUDA kernels this library has launched in this process (its own
+ * kernels only; cuFFT's launches are not counted). */
+GBN_API long long gbn_launch_count(void);
+
+/*
+ * One-shot entry points, one per XLA FFI target name the reference registers
+ * (lib/jax_finufft_gpu.cc:392-420).  Each replaces the matching
+ * nufft{D}d{T}{f}_impl of lib/kernels.h:24-180 (implemented at
+ * lib/kernels.cc.cu:221-467) with the same scalar attributes in the same
+ * order and raw device pointers in place of ffi::AnyBuffer:
+ *   source, points (dim arrays, backend order), [targets,] output.
+ * Semantics follow run_nufft (lib/kernels.cc.cu:25-92): one plan for the
+ * call, a setpts + execute per index of n_tot, offsets index*n_j for points,
+ * index*n_j*n_transf for strengths and index*n_k_total*n_transf for modes.
+ * Unlike the reference, plans are cached across calls (keyed by shape,
+ * options and stream) and the host is not synchronised.
+ */
+#define GBN_ONESHOT_ARGS_F                                                                     \
+  void *stream, float eps, int64_t iflag, int64_t n_tot, int64_t n_transf, int64_t n_j,      \
+      int64_t n_k_1, int64_t n_k_2, int64_t n_k_3, int64_t modeord, double upsampfac,         \
+      int64_t gpu_method, int64_t gpu_sort, int64_t gpu_kerevalmeth, int64_t gpu_maxbatchsize, \
+      int64_t debug
+#define GBN_ONESHOT_ARGS_D                                                                     \
+  void *stream, double eps, int64_t iflag, int64_t n_tot, int64_t n_transf, int64_t n_j,     \
+      int64_t n_k_1, int64_t n_k_2, int64_t n_k_3, int64_t modeord, double upsampfac,         \
+      int64_t gpu_method, int64_t gpu_sort, int64_t gpu_kerevalmeth, int64_t gpu_maxbatchsize, \
+      int64_t debug
+
+/* Type 1 (replaces nufft{1,2,3}d1{f,}_impl, lib/kernels.h:24-70). */
+GBN_API int gbn_nufft1d1f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, void* output);
+GBN_API int gbn_nufft1d1(GBN_ONESHOT_ARGS_D, const void* source, const double* x, void* output);
+GBN_API int gbn_nufft2d1f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  void* output);
+GBN_API int gbn_nufft2d1(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 void* output);
+GBN_API int gbn_nufft3d1f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* z, void* output);
+GBN_API int gbn_nufft3d1(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* z, void* output);
+
+/* Type 2 (replaces nufft{1,2,3}d2{f,}_impl, lib/kernels.h:76-126). */
+GBN_API int gbn_nufft1d2f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, void* output);
+GBN_API int gbn_nufft1d2(GBN_ONESHOT_ARGS_D, const void* source, const double* x, void* output);
+GBN_API int gbn_nufft2d2f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  void* output);
+GBN_API int gbn_nufft2d2(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 void* output);
+GBN_API int gbn_nufft3d2f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* z, void* output);
+GBN_API int gbn_nufft3d2(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* z, void* output);
+
+/* Type 3 (replaces nufft{1,2,3}d3{f,}_impl, lib/kernels.h:132-180); n_k_1 is
+ * the number of targets. */
+GBN_API int gbn_nufft1d3f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* s,
+                  void* output);
+GBN_API int gbn_nufft1d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* s,
+                 void* output);
+GBN_API int gbn_nufft2d3f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* s, const float* t, void* output);
+GBN_API int gbn_nufft2d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* s, const double* t, void* output);
+GBN_API int gbn_nufft3d3f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* z, const float* s, const float* t, const float* u, void* output);
+GBN_API int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* z, const double* s, const double* t, const double* u,
+                 void* output);
+
+/*
+ * Generic one-shot call with full options (bin sizes, precision): the torch
+ * binding uses this.  single = 1 for complex64/float32 data.  pts/tgts hold
+ * dim device pointers each (tgts only for type 3).  n_k in backend order
+ * (type 3: n_k[0] = number of targets).  Same semantics as the named
+ * entry points above.
+ */
+GBN_API int gbn_run(int type, int dim, int single, void* stream, double eps, int iflag, int64_t n_tot,
+            int64_t n_transf, int64_t n_j, const int64_t* n_k, const gbn_opts* opts,
+            const void* source, const void* const* pts, const void* const* tgts, void* output);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBNUFFT_H */

@@ -1,0 +1,168 @@
+// gbn_common.cuh -- types shared by the NUFFT kernels and the host plan code.
+//
+// Data layout in HBM (all row-major, dimension 0 = "x" fastest, the backend
+// order of src/jax_finufft/lowering.py:96-105):
+//   fine grid      (batch, nf2, nf1, nf0) complex in the compute precision TC
+//   sorted points  PtRec<TC, DIM>[M]: per point the offset delta in [0,1) and
+//                  the first grid index i0 of its w-wide support, per axis;
+//                  ordered by bin (counting sort), with perm[] mapping sorted
+//                  position -> input index
+//   bins           bin_count / bin_start over nb0*nb1*nb2 bins of bs0*bs1*bs2
+//                  cells; subproblems (sub_bin, sub_off) split each bin into
+//                  chunks of at most maxsub points
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace gbn {
+
+constexpr int kMaxW = 16;       // widest kernel supported
+constexpr int kThreads = 256;   // threads per block of the point kernels
+
+template <typename T>
+struct Cplx;
+template <>
+struct Cplx<float> {
+  using type = float2;
+};
+template <>
+struct Cplx<double> {
+  using type = double2;
+};
+template <typename T>
+using cplx_t = typename Cplx<T>::type;
+
+// One nonuniform point after folding: offsets and grid starts per axis.
+template <typename T, int DIM>
+struct PtRec {
+  T d[DIM];
+  int i[DIM];
+};
+
+// Spreading-grid and bin geometry.
+struct Geom {
+  int dim;
+  int w;
+  int64_t nf[3];
+  int bs[3];
+  int nb[3];
+  int64_t nbins;
+  int maxsub;
+};
+
+// How points map onto the grid: mode 0 folds periodically (types 1/2),
+// mode 1 rescales (type-3 sources): X = (x - center)*scale + nf/2.
+struct FoldSpec {
+  int mode;
+  double center[3];
+  double scale[3];
+};
+
+// Kernel evaluation: piecewise Horner coefficients coef[piece*(deg+1)+n]
+// (device memory, compute precision) or the direct formula when meth == 0.
+template <typename T>
+struct KerSpec {
+  const T* coef;
+  int deg;
+  int meth;
+  T beta;
+};
+
+// Device-side sort state produced by setpts.
+struct SortState {
+  int* pt_bin;     // [M] bin of each input point
+  int* pt_rank;    // [M] rank inside its bin
+  int* bin_count;  // [nbins]
+  int* bin_start;  // [nbins] exclusive scan of bin_count
+  int* perm;       // [M] sorted position -> input index
+  int* sub_count;  // [nbins] subproblems per bin
+  int* sub_start;  // [nbins] exclusive scan of sub_count
+  int* sub_bin;    // [max_sub] bin of each subproblem
+  int* sub_off;    // [max_sub] first point (within its bin) of each subproblem
+  int* n_sub;      // [1] number of subproblems
+  void* recs;      // [M] PtRec in sorted order
+  void* recs_in;   // [M] PtRec in input order (scratch)
+  int* scan_tmp;   // scan scratch
+  int64_t max_sub; // capacity of sub_bin/sub_off
+};
+
+// Count of kernels this library has launched (process-wide, all threads);
+// every launcher adds the launches it makes.  Read through gbn_launch_count().
+void note_launch(int n = 1);
+
+// ---------------------------------------------------------------------------
+// Launchers (defined in the .cu files, called by the host plan code).
+// TX = coordinate type as given by the caller, TC = compute precision,
+// TD = data precision of strengths / modes.
+// ---------------------------------------------------------------------------
+
+// Fold points, count bins, write per-point records in input order.
+template <typename TX, typename TC>
+cudaError_t launch_fold(const Geom& g, const FoldSpec& fs, int64_t M, const TX* x, const TX* y,
+                        const TX* z, SortState& st, cudaStream_t s);
+
+// Exclusive scan of n ints (in may equal out); tmp needs scan_tmp_ints(n).
+int64_t scan_tmp_ints(int64_t n);
+cudaError_t launch_scan(const int* in, int* out, int64_t n, int* tmp, cudaStream_t s);
+
+// Scatter records into bin order, build the subproblem list.
+template <typename TC>
+cudaError_t launch_sort_finish(const Geom& g, int64_t M, SortState& st, bool sorted,
+                               cudaStream_t s);
+
+// Spread ntr transforms: c (ntr, M) data precision -> fine (ntr, nf) compute precision.
+// method 1 = global atomics per update, 2 = shared-memory subproblems.
+template <typename TC, typename TD>
+cudaError_t launch_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
+                          const SortState& st, const void* c, void* fine, int ntr,
+                          cudaStream_t s);
+
+// Interpolate ntr transforms: fine -> c (ntr, M).
+template <typename TC, typename TD>
+cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
+                          const SortState& st, const void* fine, void* c, int ntr,
+                          cudaStream_t s);
+
+// Type-1 deconvolution + mode reorder: fine (ntr, nf) -> out (ntr, N).
+// phi[d] holds 1/psihat for each output index along axis d.
+template <typename TC, typename TD>
+cudaError_t launch_deconv1(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                           const TC* const* phi, const void* fine, void* out, int ntr,
+                           cudaStream_t s);
+
+// Type-2 pre-correction + zero padding: in (ntr, N) -> fine (ntr, nf), every
+// fine cell written.
+template <typename TC, typename TD>
+cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                           const TC* const* phi, const void* in, void* fine, int ntr,
+                           cudaStream_t s);
+
+// Type 3: min/max of each coordinate array (out: 2 doubles per array).
+template <typename TX>
+cudaError_t launch_minmax(const TX* const* arrs, int narr, int64_t n, double* out,
+                          cudaStream_t s);
+
+// Type 3: tau = (s - center) / scale per axis into double arrays.
+template <typename TX>
+cudaError_t launch_t3_targets(int dim, int64_t N, const TX* const* s, const double* center,
+                              const double* scale, double* const* tau, cudaStream_t s_);
+
+// Type 3: per-point pre-phase exp(iflag*i*sum_d cs_d*(x_d - cx_d)) (compute precision).
+template <typename TX, typename TC>
+cudaError_t launch_t3_prephase_factors(int dim, int64_t M, const TX* const* x, const double* cx,
+                                       const double* cs, int iflag, void* fac, cudaStream_t s);
+
+// Type 3: per-target post factor exp(iflag*i*sum_d cx_d*s_d) / prod_d psihat(tau_d).
+template <typename TX, typename TC>
+cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
+                                   const double* const* tau, int iflag, int w, double beta,
+                                   void* fac, cudaStream_t s);
+
+// out[t, j] = in[t, j] * fac[j] (complex), ntr transforms of length n.
+template <typename TI, typename TO, typename TF>
+cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, void* out,
+                        cudaStream_t s);
+
+}  // namespace gbn

@@ -1,0 +1,313 @@
+// gbn_interp.cu -- type-2 interpolation (fine grid -> nonuniform values).
+//
+// Replaces cuFINUFFT's interp stage.  Same work decomposition as the spread:
+// G lanes per point, lane gl owning x offset gl; each lane gathers its
+// column of w^(d-1) cells weighted by the broadcast y/z kernel values, then
+// the G partial sums are reduced with xor shuffles and one lane writes the
+// result to the point's original position.
+//
+//   method 2 (SM): the block first stages its bin's (bs+w)^d tile from the
+//     fine grid into shared memory (coalesced rows, periodic wrap), so the
+//     gathers never touch HBM.
+//   method 1 (GM): gathers straight from the fine grid through L1/L2.
+#include <cuda_runtime.h>
+
+#include "gbn_common.cuh"
+#include "gbn_device.cuh"
+
+namespace gbn {
+
+namespace {
+
+struct SubArgs {
+  const int* sub_bin;
+  const int* sub_off;
+  const int* n_sub;
+  const int* bin_start;
+  const int* bin_count;
+  const int* perm;
+  int sorted;
+};
+
+__device__ __forceinline__ bool sub_range(const SubArgs& sa, const Geom& g, int64_t M, int sub,
+                                          int& start, int& cnt, int& bin) {
+  if (sa.sorted) {
+    if (sub >= *sa.n_sub) return false;
+    bin = sa.sub_bin[sub];
+    const int off = sa.sub_off[sub];
+    start = sa.bin_start[bin] + off;
+    cnt = min(sa.bin_count[bin] - off, g.maxsub);
+  } else {
+    const int64_t s0 = (int64_t)sub * g.maxsub;
+    if (s0 >= M) return false;
+    bin = 0;
+    start = (int)s0;
+    cnt = (int)min((int64_t)g.maxsub, M - s0);
+  }
+  return cnt > 0;
+}
+
+template <typename TC, int G>
+__device__ __forceinline__ void group_reduce(TC& a, TC& b) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+}
+
+template <typename TC, typename TD, int DIM, int G>
+__global__ void __launch_bounds__(kThreads)
+    interp_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
+                     SubArgs sa, const cplx_t<TC>* __restrict__ fine, cplx_t<TD>* __restrict__ c,
+                     int64_t nftot) {
+  constexpr int NCO = GroupCfg<G>::NCO;
+  constexpr int PPW = 32 / G;
+  constexpr int NWARP = kThreads / 32;
+  int start, cnt, bin;
+  if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
+  const int t = blockIdx.y;
+  const int w = g.w, h = w >> 1;
+  int org[3] = {0, 0, 0}, T[3] = {1, 1, 1};
+  {
+    int rem = bin;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const int b = rem % g.nb[d];
+      rem /= g.nb[d];
+      org[d] = b * g.bs[d] - h;
+      T[d] = g.bs[d] + w;
+    }
+  }
+  const int ncell = T[0] * T[1] * T[2];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
+  const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
+  for (int i = threadIdx.x; i < ncell; i += kThreads) {
+    const int c0 = i % T[0];
+    const int r1 = i / T[0];
+    const int c1 = r1 % T[1];
+    const int c2 = r1 / T[1];
+    const int64_t g0 = wrap_idx(org[0] + c0, g.nf[0]);
+    const int64_t g1 = DIM > 1 ? wrap_idx(org[1] + c1, g.nf[1]) : 0;
+    const int64_t g2 = DIM > 2 ? wrap_idx(org[2] + c2, g.nf[2]) : 0;
+    tile[i] = ft[(g2 * g.nf[1] + g1) * g.nf[0] + g0];
+  }
+  const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
+  TC co[NCO];
+  load_coef<TC, NCO>(co, ks, gl, w);
+  __syncthreads();
+
+  cplx_t<TD>* ct = c + (int64_t)t * M;
+  const bool lane_on = gl < w;
+  for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
+    const int pi = pb + grp;
+    const bool valid = pi < cnt;
+    const int js = start + (valid ? pi : 0);
+    const PtRec<TC, DIM> r = recs[js];
+    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
+    const int l0 = r.i[0] - org[0] + gl;
+    TC ar = TC(0), ai = TC(0);
+    if (DIM == 1) {
+      if (lane_on) {
+        const cplx_t<TC> v = tile[l0];
+        ar = v.x;
+        ai = v.y;
+      }
+    } else if (DIM == 2) {
+      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
+      int idx = (r.i[1] - org[1]) * T[0] + l0;
+      for (int iy = 0; iy < w; ++iy) {
+        const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
+        if (lane_on) {
+          const cplx_t<TC> v = tile[idx];
+          ar = fma(v.x, kyv, ar);
+          ai = fma(v.y, kyv, ai);
+        }
+        idx += T[0];
+      }
+    } else {
+      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
+      const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
+      const int plane = T[0] * T[1];
+      int zbase = ((r.i[2] - org[2]) * T[1] + (r.i[1] - org[1])) * T[0] + l0;
+      for (int iz = 0; iz < w; ++iz) {
+        const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
+        TC yr = TC(0), yi = TC(0);
+        int idx = zbase;
+        for (int iy = 0; iy < w; ++iy) {
+          const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
+          if (lane_on) {
+            const cplx_t<TC> v = tile[idx];
+            yr = fma(v.x, kyv, yr);
+            yi = fma(v.y, kyv, yi);
+          }
+          idx += T[0];
+        }
+        ar = fma(yr, kzv, ar);
+        ai = fma(yi, kzv, ai);
+        zbase += plane;
+      }
+    }
+    ar *= kx;
+    ai *= kx;
+    group_reduce<TC, G>(ar, ai);
+    if (valid && gl == 0) {
+      cplx_t<TD> o;
+      o.x = (TD)ar;
+      o.y = (TD)ai;
+      ct[sa.perm ? sa.perm[js] : js] = o;
+    }
+  }
+}
+
+template <typename TC, typename TD, int DIM, int G>
+__global__ void __launch_bounds__(kThreads)
+    interp_gm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
+                     SubArgs sa, const cplx_t<TC>* __restrict__ fine, cplx_t<TD>* __restrict__ c,
+                     int64_t nftot) {
+  constexpr int NCO = GroupCfg<G>::NCO;
+  constexpr int PPW = 32 / G;
+  constexpr int NWARP = kThreads / 32;
+  int start, cnt, bin;
+  if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
+  const int t = blockIdx.y;
+  const int w = g.w;
+  const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
+  TC co[NCO];
+  load_coef<TC, NCO>(co, ks, gl, w);
+  const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
+  cplx_t<TD>* ct = c + (int64_t)t * M;
+  const bool lane_on = gl < w;
+  for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
+    const int pi = pb + grp;
+    const bool valid = pi < cnt;
+    const int js = start + (valid ? pi : 0);
+    const PtRec<TC, DIM> r = recs[js];
+    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
+    const int64_t gx = wrap_idx((int64_t)r.i[0] + gl, g.nf[0]);
+    TC ar = TC(0), ai = TC(0);
+    if (DIM == 1) {
+      if (lane_on) {
+        const cplx_t<TC> v = ft[gx];
+        ar = v.x;
+        ai = v.y;
+      }
+    } else if (DIM == 2) {
+      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
+      for (int iy = 0; iy < w; ++iy) {
+        const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
+        const int64_t gy = wrap_idx((int64_t)r.i[1] + iy, g.nf[1]);
+        if (lane_on) {
+          const cplx_t<TC> v = ft[gy * g.nf[0] + gx];
+          ar = fma(v.x, kyv, ar);
+          ai = fma(v.y, kyv, ai);
+        }
+      }
+    } else {
+      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
+      const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
+      for (int iz = 0; iz < w; ++iz) {
+        const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
+        const int64_t gz = wrap_idx((int64_t)r.i[2] + iz, g.nf[2]);
+        TC yr = TC(0), yi = TC(0);
+        for (int iy = 0; iy < w; ++iy) {
+          const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
+          const int64_t gy = wrap_idx((int64_t)r.i[1] + iy, g.nf[1]);
+          if (lane_on) {
+            const cplx_t<TC> v = ft[(gz * g.nf[1] + gy) * g.nf[0] + gx];
+            yr = fma(v.x, kyv, yr);
+            yi = fma(v.y, kyv, yi);
+          }
+        }
+        ar = fma(yr, kzv, ar);
+        ai = fma(yi, kzv, ai);
+      }
+    }
+    ar *= kx;
+    ai *= kx;
+    group_reduce<TC, G>(ar, ai);
+    if (valid && gl == 0) {
+      cplx_t<TD> o;
+      o.x = (TD)ar;
+      o.y = (TD)ai;
+      ct[sa.perm ? sa.perm[js] : js] = o;
+    }
+  }
+}
+
+template <typename TC, typename TD, int DIM, int G>
+cudaError_t run_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
+                       const SortState& st, const void* fine, void* c, int ntr,
+                       cudaStream_t s) {
+  SubArgs sa;
+  sa.sub_bin = st.sub_bin;
+  sa.sub_off = st.sub_off;
+  sa.n_sub = st.n_sub;
+  sa.bin_start = st.bin_start;
+  sa.bin_count = st.bin_count;
+  sa.perm = st.perm;
+  sa.sorted = st.perm != nullptr;
+  const int64_t nblk = sa.sorted ? st.max_sub : (M + g.maxsub - 1) / g.maxsub;
+  if (nblk == 0 || ntr == 0) return cudaSuccess;
+  int64_t nftot = 1;
+  for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
+  const PtRec<TC, DIM>* recs = (const PtRec<TC, DIM>*)(sa.sorted ? st.recs : st.recs_in);
+  for (int t0 = 0; t0 < ntr; t0 += 65535) {
+    const int nt = ntr - t0 < 65535 ? ntr - t0 : 65535;
+    dim3 grid((unsigned)nblk, (unsigned)nt);
+    const cplx_t<TC>* ft = (const cplx_t<TC>*)fine + (int64_t)t0 * nftot;
+    cplx_t<TD>* ct = (cplx_t<TD>*)c + (int64_t)t0 * M;
+    if (method == 2 && sa.sorted) {
+      int64_t ncell = 1;
+      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w;
+      const size_t smem = (size_t)ncell * sizeof(cplx_t<TC>);
+      auto kern = interp_sm_kernel<TC, TD, DIM, G>;
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return e;
+      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ft, ct, nftot);
+      note_launch();
+    } else {
+      interp_gm_kernel<TC, TD, DIM, G><<<grid, kThreads, 0, s>>>(g, ks, M, recs, sa, ft, ct,
+                                                                  nftot);
+      note_launch();
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+template <typename TC, typename TD>
+cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
+                          const SortState& st, const void* fine, void* c, int ntr,
+                          cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  const bool wide = g.w > 8;
+  switch (g.dim) {
+    case 1:
+      return wide ? run_interp<TC, TD, 1, 16>(g, ks, method, M, st, fine, c, ntr, s)
+                  : run_interp<TC, TD, 1, 8>(g, ks, method, M, st, fine, c, ntr, s);
+    case 2:
+      return wide ? run_interp<TC, TD, 2, 16>(g, ks, method, M, st, fine, c, ntr, s)
+                  : run_interp<TC, TD, 2, 8>(g, ks, method, M, st, fine, c, ntr, s);
+    default:
+      return wide ? run_interp<TC, TD, 3, 16>(g, ks, method, M, st, fine, c, ntr, s)
+                  : run_interp<TC, TD, 3, 8>(g, ks, method, M, st, fine, c, ntr, s);
+  }
+}
+
+template cudaError_t launch_interp<float, float>(const Geom&, const KerSpec<float>&, int,
+                                                 int64_t, const SortState&, const void*, void*,
+                                                 int, cudaStream_t);
+template cudaError_t launch_interp<float, double>(const Geom&, const KerSpec<float>&, int,
+                                                  int64_t, const SortState&, const void*, void*,
+                                                  int, cudaStream_t);
+template cudaError_t launch_interp<double, double>(const Geom&, const KerSpec<double>&, int,
+                                                   int64_t, const SortState&, const void*,
+                                                   void*, int, cudaStream_t);
+
+}  // namespace gbn

@@ -1,0 +1,1312 @@
+// gbn_plan.cu -- host side of the library: plans, setpts/execute
+// orchestration, cuFFT, the plan cache and the C ABI (include/gbnufft.h).
+//
+// Replaces lib/kernels.cc.cu (run_nufft and the nufft{d}d{t}{f}_impl
+// functions) and lib/cufinufft_wrapper.cc (makeplan/setpts/execute/destroy).
+// Differences from the reference driver, all deliberate:
+//   * plans (kernel coefficients, deconvolution factors, cuFFT plan, grids
+//     and sort buffers) are cached across one-shot calls instead of being
+//     rebuilt per call (kernels.cc.cu:51);
+//   * the host is never blocked at the end of a call (kernels.cc.cu:83); all
+//     work is stream-ordered and scratch memory is stream-ordered
+//     (cudaMallocAsync/cudaFreeAsync);
+//   * double-precision 3D does not force global-memory spreading
+//     (cufinufft_wrapper.cc:33-35): the shared-memory method is used while
+//     its tile fits.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/gbnufft.h"
+#include "gbn_common.cuh"
+
+using namespace gbn;
+
+namespace gbn {
+static std::atomic<long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace gbn
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define GBN_CUDA(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(GBN_ERR_CUDA, std::string(#expr) + " failed: " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define GBN_TRY(expr)      \
+  do {                     \
+    int r_ = (expr);       \
+    if (r_ >= 2) return r_; \
+  } while (0)
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// ---------------------------------------------------------------------------
+// plan-time arithmetic (same rules as the CPU restatement in oracle/)
+// ---------------------------------------------------------------------------
+int64_t next235even(int64_t n0) {
+  if (n0 <= 2) return 2;
+  int64_t n = (n0 % 2) ? n0 + 1 : n0;
+  for (;; n += 2) {
+    int64_t m = n;
+    while (m % 2 == 0) m /= 2;
+    while (m % 3 == 0) m /= 3;
+    while (m % 5 == 0) m /= 5;
+    if (m == 1) return n;
+  }
+}
+
+// Width w and shape beta of the ES kernel for tolerance eps; returns 1 when
+// the width is clamped at kMaxW.
+int kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
+  int warn = 0;
+  double wd = (sigma == 2.0) ? std::ceil(-std::log10(eps / 10.0))
+                             : std::ceil(-std::log(eps) / (kPi * std::sqrt(1.0 - 1.0 / sigma)));
+  if (!(wd >= 2.0)) wd = 2.0;
+  if (wd > kMaxW) {
+    wd = kMaxW;
+    warn = 1;
+  }
+  const int w = (int)wd;
+  double ratio;
+  if (sigma == 2.0) {
+    ratio = 2.30;
+    if (w == 2) ratio = 2.20;
+    if (w == 3) ratio = 2.26;
+    if (w == 4) ratio = 2.38;
+  } else {
+    ratio = 0.97 * kPi * (1.0 - 1.0 / (2.0 * sigma));
+  }
+  *w_out = w;
+  *beta_out = ratio * (double)w;
+  return warn;
+}
+
+int64_t fine_size(int64_t n, double sigma, int w) {
+  int64_t m = (int64_t)std::ceil(sigma * (double)n);
+  if (m < 2 * (int64_t)w) m = 2 * (int64_t)w;
+  return next235even(m);
+}
+
+double es_kernel(double t, int w, double beta) {
+  const double z = 2.0 * t / (double)w;
+  const double s = 1.0 - z * z;
+  return s < 0.0 ? 0.0 : std::exp(beta * (std::sqrt(s) - 1.0));
+}
+
+// Chebyshev interpolation of each unit piece at degree deg, as monomials in
+// u = 2*delta - 1.
+void horner_fit(int w, double beta, int deg, std::vector<double>& coef) {
+  const int n1 = deg + 1;
+  std::vector<double> node(n1), val(n1), cheb(n1);
+  std::vector<std::vector<double>> tk(n1, std::vector<double>(n1, 0.0));
+  for (int i = 0; i < n1; ++i) node[i] = std::cos(kPi * (i + 0.5) / n1);
+  tk[0][0] = 1.0;
+  if (n1 > 1) tk[1][1] = 1.0;
+  for (int k = 2; k < n1; ++k)
+    for (int n = 0; n < n1; ++n) tk[k][n] = (n ? 2.0 * tk[k - 1][n - 1] : 0.0) - tk[k - 2][n];
+  coef.assign((size_t)w * n1, 0.0);
+  for (int j = 0; j < w; ++j) {
+    for (int i = 0; i < n1; ++i) val[i] = es_kernel(j - 0.5 * w + 0.5 * (node[i] + 1.0), w, beta);
+    for (int k = 0; k < n1; ++k) {
+      double s = 0.0;
+      for (int i = 0; i < n1; ++i) s += val[i] * std::cos(kPi * k * (i + 0.5) / n1);
+      cheb[k] = s * (k == 0 ? 1.0 : 2.0) / n1;
+    }
+    for (int n = 0; n < n1; ++n) {
+      double s = 0.0;
+      for (int k = 0; k < n1; ++k) s += cheb[k] * tk[k][n];
+      coef[(size_t)j * n1 + n] = s;
+    }
+  }
+}
+
+void gauss_legendre(int q, double* x, double* wt) {
+  for (int i = 0; i < (q + 1) / 2; ++i) {
+    double z = std::cos(kPi * (i + 0.75) / (q + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= q; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = q * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= q; ++k) {
+      double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = q * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = -z;
+    x[q - 1 - i] = z;
+    wt[i] = wt[q - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// psihat(omega) = int psi(t) cos(omega t) dt, t = (w/2) sin(theta) substitution.
+void kernel_ft(int w, double beta, const std::vector<double>& omega, std::vector<double>& out) {
+  const int q = 2 * w + 10;
+  double xg[64], wg[64], tq[64], fq[64];
+  gauss_legendre(q, xg, wg);
+  for (int i = 0; i < q; ++i) {
+    const double th = (xg[i] + 1.0) * kPi / 4.0;
+    const double wt = wg[i] * kPi / 4.0;
+    tq[i] = 0.5 * w * std::sin(th);
+    fq[i] = 2.0 * wt * std::exp(beta * (std::cos(th) - 1.0)) * 0.5 * w * std::cos(th);
+  }
+  out.resize(omega.size());
+  for (size_t k = 0; k < omega.size(); ++k) {
+    double s = 0.0;
+    for (int i = 0; i < q; ++i) s += fq[i] * std::cos(omega[k] * tq[i]);
+    out[k] = s;
+  }
+}
+
+int64_t type3_params(double xmin, double xmax, double smin, double smax, double sigma, int w,
+                     double* cx, double* cs, double* scale) {
+  *cx = 0.5 * (xmax + xmin);
+  const double hx = 0.5 * (xmax - xmin);
+  *cs = 0.5 * (smax + smin);
+  const double hs = 0.5 * (smax - smin);
+  double X = hx, S = hs;
+  if (X == 0.0) {
+    if (S == 0.0) {
+      X = 1.0;
+      S = 1.0;
+    } else if (X < 1.0 / S) {
+      X = 1.0 / S;
+    }
+  } else if (S < 1.0 / X) {
+    S = 1.0 / X;
+  }
+  double nfd = 2.0 * sigma * S * X / kPi + (double)(w + 1);
+  if (!std::isfinite(nfd)) nfd = 0.0;
+  int64_t nf = (int64_t)nfd;
+  if (nf < 2 * (int64_t)w) nf = 2 * (int64_t)w;
+  nf = next235even(nf);
+  *scale = sigma * S / kPi;
+  return nf;
+}
+
+int64_t mode_freq(int64_t i, int64_t N, int modeord) {
+  if (modeord == 0) return i - N / 2;
+  return i < (N + 1) / 2 ? i : i - N;
+}
+
+// ---------------------------------------------------------------------------
+// stream-ordered device buffer
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes, cudaStream_t s) {
+    if (bytes <= n && p) return cudaSuccess;
+    release(s);
+    if (bytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMallocAsync(&p, bytes, s);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      n = 0;
+      return e;
+    }
+    n = bytes;
+    return cudaSuccess;
+  }
+  void release(cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+size_t rec_size(int dim, bool single) {
+  if (single) {
+    switch (dim) {
+      case 1:
+        return sizeof(PtRec<float, 1>);
+      case 2:
+        return sizeof(PtRec<float, 2>);
+      default:
+        return sizeof(PtRec<float, 3>);
+    }
+  }
+  switch (dim) {
+    case 1:
+      return sizeof(PtRec<double, 1>);
+    case 2:
+      return sizeof(PtRec<double, 2>);
+    default:
+      return sizeof(PtRec<double, 3>);
+  }
+}
+
+}  // namespace
+
+// =============================================================================
+// plan
+// =============================================================================
+struct gbn_plan_s {
+  int type = 1, dim = 1, iflag = 1, ntransf = 1;
+  bool data_single = true, comp_single = true;
+  double eps = 1e-6, sigma = 2.0, beta = 0.0;
+  int w = 2, deg = 4, warn = 0;
+  int64_t N[3] = {1, 1, 1};
+  int64_t nf[3] = {1, 1, 1};
+  int64_t nftot = 1, Ntot = 1;
+  gbn_opts opts{};
+  int method = 2;
+  bool sorted = true;
+  int batch = 1;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  Geom geom{};
+
+  DevBuf coef, phi[3], fine;
+  DevBuf pt_bin, pt_rank, bin_count, bin_start, perm, sub_count, sub_start, sub_bin, sub_off,
+      n_sub, recs, recs_in, scan_tmp;
+  SortState st{};
+  int64_t M = 0;
+  bool pts_set = false;
+
+  cufftHandle fft = 0, fft_rem = 0;
+  int fft_batch = 0, fft_rem_batch = 0;
+
+  // type 3
+  std::unique_ptr<gbn_plan_s> inner;
+  double t3_cx[3] = {0, 0, 0}, t3_cs[3] = {0, 0, 0}, t3_scale[3] = {1, 1, 1};
+  int64_t Nt = 0;
+  DevBuf t3_tau[3], t3_pre, t3_post, t3_cbuf, t3_obuf, t3_minmax;
+
+  // debug timings: 4 events per executed batch (stage boundaries) and 2 per
+  // setpts, recorded without host synchronisation and summed by
+  // gbn_get_timings, which then resets the pool.
+  bool ev_ok = false;
+  std::vector<cudaEvent_t> ev_exec, ev_setpts;
+  size_t ev_exec_used = 0, ev_setpts_used = 0;
+
+  ~gbn_plan_s() {
+    cudaStreamSynchronize(stream);
+    DevBuf* bufs[] = {&coef,   &phi[0],    &phi[1],    &phi[2],   &fine,     &pt_bin,
+                      &pt_rank, &bin_count, &bin_start, &perm,     &sub_count, &sub_start,
+                      &sub_bin, &sub_off,   &n_sub,     &recs,     &recs_in,  &scan_tmp,
+                      &t3_tau[0], &t3_tau[1], &t3_tau[2], &t3_pre,  &t3_post,  &t3_cbuf,
+                      &t3_obuf, &t3_minmax};
+    for (DevBuf* b : bufs) b->release(stream);
+    if (fft) cufftDestroy(fft);
+    if (fft_rem) cufftDestroy(fft_rem);
+    for (auto& e : ev_exec) cudaEventDestroy(e);
+    for (auto& e : ev_setpts) cudaEventDestroy(e);
+    cudaStreamSynchronize(stream);
+  }
+};
+
+namespace {
+
+size_t cplx_size(bool single) { return single ? 8 : 16; }
+
+// Default bin sizes (cells per axis) for the shared-memory method.
+void default_bins(int dim, bool single, int* bs) {
+  bs[0] = bs[1] = bs[2] = 1;
+  if (dim == 1) {
+    bs[0] = 1024;
+  } else if (dim == 2) {
+    bs[0] = 32;
+    bs[1] = 32;
+  } else if (single) {
+    bs[0] = 16;
+    bs[1] = 16;
+    bs[2] = 8;
+  } else {
+    bs[0] = 8;
+    bs[1] = 8;
+    bs[2] = 8;
+  }
+}
+
+size_t tile_bytes(int dim, const int* bs, int w, bool single) {
+  size_t n = 1;
+  for (int d = 0; d < dim; ++d) n *= (size_t)(bs[d] + w);
+  return n * 2 * (single ? 4 : 8);
+}
+
+// Fill geometry (bins, nb) for the current nf and options; choose method.
+void setup_geom(gbn_plan_s* p) {
+  Geom& g = p->geom;
+  g.dim = p->dim;
+  g.w = p->w;
+  int bs[3];
+  default_bins(p->dim, p->comp_single, bs);
+  const int user[3] = {p->opts.gpu_binsizex, p->opts.gpu_binsizey, p->opts.gpu_binsizez};
+  for (int d = 0; d < 3; ++d) {
+    if (d < p->dim && user[d] > 0) bs[d] = user[d];
+    if (d >= p->dim) bs[d] = 1;
+    if (d < p->dim && bs[d] > p->nf[d]) bs[d] = (int)p->nf[d];
+    if (bs[d] < 1) bs[d] = 1;
+  }
+  // method: 1 = global atomics, 2 = shared-memory tiles
+  int method = p->opts.gpu_method;
+  const size_t smem_limit = 200 * 1024;
+  if (!p->sorted) method = 1;
+  if (method == 0) {
+    method = 2;
+    if (!p->comp_single && p->dim == 3 && tile_bytes(3, bs, p->w, false) > 96 * 1024) method = 1;
+  }
+  if (method == 2) {
+    // shrink the largest bin axis until the tile fits
+    while (tile_bytes(p->dim, bs, p->w, p->comp_single) > smem_limit) {
+      int dmax = 0;
+      for (int d = 1; d < p->dim; ++d)
+        if (bs[d] > bs[dmax]) dmax = d;
+      if (bs[dmax] <= 1) {
+        method = 1;
+        break;
+      }
+      bs[dmax] = (bs[dmax] + 1) / 2;
+    }
+  }
+  p->method = method;
+  g.nbins = 1;
+  for (int d = 0; d < 3; ++d) {
+    g.nf[d] = d < p->dim ? p->nf[d] : 1;
+    g.bs[d] = bs[d];
+    g.nb[d] = d < p->dim ? (int)((p->nf[d] + bs[d] - 1) / bs[d]) : 1;
+    g.nbins *= g.nb[d];
+  }
+  g.maxsub = p->opts.gpu_maxsubprobsize > 0 ? p->opts.gpu_maxsubprobsize : 1024;
+}
+
+int upload_doubles_as(const std::vector<double>& v, bool single, DevBuf& buf, cudaStream_t s) {
+  const size_t bytes = v.size() * (single ? 4 : 8);
+  GBN_CUDA(buf.ensure(bytes, s));
+  if (v.empty()) return GBN_OK;
+  if (single) {
+    std::vector<float> f(v.begin(), v.end());
+    GBN_CUDA(cudaMemcpyAsync(buf.p, f.data(), bytes, cudaMemcpyHostToDevice, s));
+    // keep host staging alive until the copy ran: pageable copies are staged
+    // synchronously by the driver before the call returns
+  } else {
+    GBN_CUDA(cudaMemcpyAsync(buf.p, v.data(), bytes, cudaMemcpyHostToDevice, s));
+  }
+  return GBN_OK;
+}
+
+// Deconvolution factors 1/psihat(2 pi k / nf) per output index, per axis.
+int setup_phi(gbn_plan_s* p) {
+  for (int d = 0; d < p->dim; ++d) {
+    std::vector<double> om((size_t)p->N[d]);
+    for (int64_t i = 0; i < p->N[d]; ++i)
+      om[(size_t)i] = 2.0 * kPi * (double)mode_freq(i, p->N[d], p->opts.modeord) / (double)p->nf[d];
+    std::vector<double> ph;
+    kernel_ft(p->w, p->beta, om, ph);
+    for (auto& v : ph) v = 1.0 / v;
+    GBN_TRY(upload_doubles_as(ph, p->comp_single, p->phi[d], p->stream));
+  }
+  return GBN_OK;
+}
+
+int setup_kernel_coef(gbn_plan_s* p) {
+  std::vector<double> coef;
+  horner_fit(p->w, p->beta, p->deg, coef);
+  return upload_doubles_as(coef, p->comp_single, p->coef, p->stream);
+}
+
+int make_fft(gbn_plan_s* p, int nbatch, cufftHandle* h) {
+  int n[3];
+  for (int d = 0; d < p->dim; ++d) n[d] = (int)p->nf[p->dim - 1 - d];
+  cufftResult r = cufftPlanMany(h, p->dim, n, nullptr, 1, (int)p->nftot, nullptr, 1,
+                                (int)p->nftot, p->comp_single ? CUFFT_C2C : CUFFT_Z2Z, nbatch);
+  if (r != CUFFT_SUCCESS) {
+    *h = 0;
+    return fail(GBN_ERR_CUFFT, "cufftPlanMany failed with code " + std::to_string((int)r));
+  }
+  return GBN_OK;
+}
+
+int exec_fft(gbn_plan_s* p, int nb) {
+  cufftHandle* h;
+  if (nb == p->batch) {
+    if (!p->fft) {
+      GBN_TRY(make_fft(p, p->batch, &p->fft));
+      p->fft_batch = p->batch;
+    }
+    h = &p->fft;
+  } else {
+    if (!p->fft_rem || p->fft_rem_batch != nb) {
+      if (p->fft_rem) cufftDestroy(p->fft_rem);
+      p->fft_rem = 0;
+      GBN_TRY(make_fft(p, nb, &p->fft_rem));
+      p->fft_rem_batch = nb;
+    }
+    h = &p->fft_rem;
+  }
+  cufftSetStream(*h, p->stream);
+  const int dir = p->iflag >= 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
+  cufftResult r;
+  if (p->comp_single)
+    r = cufftExecC2C(*h, (cufftComplex*)p->fine.p, (cufftComplex*)p->fine.p, dir);
+  else
+    r = cufftExecZ2Z(*h, (cufftDoubleComplex*)p->fine.p, (cufftDoubleComplex*)p->fine.p, dir);
+  if (r != CUFFT_SUCCESS) return fail(GBN_ERR_CUFFT, "cufftExec failed with code " + std::to_string((int)r));
+  return GBN_OK;
+}
+
+// Resolve compute precision; returns an error for unsupported combinations.
+int resolve_precision(gbn_plan_s* p) {
+  switch (p->opts.gpu_precision) {
+    case 0:
+      p->comp_single = p->data_single;
+      break;
+    case 1:
+      p->comp_single = true;
+      break;
+    case 2:
+      if (p->data_single)
+        return fail(GBN_ERR_ARGS, "gpu_precision=2 (FP64 compute) needs complex128 data");
+      p->comp_single = false;
+      break;
+    case 3:
+      p->comp_single = p->data_single || p->eps >= 1e-6;
+      break;
+    default:
+      return fail(GBN_ERR_ARGS, "gpu_precision must be 0..3");
+  }
+  return GBN_OK;
+}
+
+int plan_create(int type, int dim, const int64_t* nmodes, int iflag, int ntransf, double eps,
+                bool data_single, const gbn_opts* opts_in, void* stream, gbn_plan_s** out) {
+  *out = nullptr;
+  if (type < 1 || type > 3) return fail(GBN_ERR_ARGS, "type must be 1, 2 or 3");
+  if (dim < 1 || dim > 3) return fail(GBN_ERR_ARGS, "dim must be 1, 2 or 3");
+  if (ntransf < 1) return fail(GBN_ERR_ARGS, "ntransf must be >= 1");
+  if (!(eps > 0.0) || !std::isfinite(eps)) return fail(GBN_ERR_ARGS, "eps must be positive");
+  std::unique_ptr<gbn_plan_s> p(new gbn_plan_s());
+  if (opts_in)
+    p->opts = *opts_in;
+  else
+    gbn_default_opts(&p->opts);
+  p->type = type;
+  p->dim = dim;
+  p->iflag = iflag >= 0 ? 1 : -1;
+  p->ntransf = ntransf;
+  p->data_single = data_single;
+  p->eps = eps;
+  p->stream = (cudaStream_t)stream;
+  GBN_CUDA(cudaGetDevice(&p->device));
+  GBN_TRY(resolve_precision(p.get()));
+  p->sigma = p->opts.upsampfac > 0.0 ? p->opts.upsampfac : 2.0;
+  if (!(p->sigma > 1.0)) return fail(GBN_ERR_ARGS, "upsampfac must be > 1");
+  if (p->opts.modeord != 0 && p->opts.modeord != 1)
+    return fail(GBN_ERR_ARGS, "modeord must be 0 or 1");
+  p->sorted = p->opts.gpu_sort != 0;
+  int warn = 0;
+  double e = eps;
+  if (p->comp_single && e < 1e-7) {
+    e = 1e-7;
+    warn = 1;
+  }
+  warn |= kernel_params(e, p->sigma, &p->w, &p->beta);
+  p->warn = warn;
+  p->deg = p->w + 2;
+  if (type != 3) {
+    for (int d = 0; d < 3; ++d) {
+      p->N[d] = d < dim ? nmodes[d] : 1;
+      if (p->N[d] < 1) return fail(GBN_ERR_ARGS, "number of modes must be >= 1");
+      p->nf[d] = d < dim ? fine_size(p->N[d], p->sigma, p->w) : 1;
+    }
+    p->nftot = p->nf[0] * p->nf[1] * p->nf[2];
+    p->Ntot = p->N[0] * p->N[1] * p->N[2];
+    if (p->nftot > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "fine grid too large (> 2^31 cells)");
+    setup_geom(p.get());
+    GBN_TRY(setup_phi(p.get()));
+  }
+  GBN_TRY(setup_kernel_coef(p.get()));
+  // transforms per batch: bounded so the fine grids stay within 8 GiB
+  int b = p->opts.gpu_maxbatchsize > 0 ? p->opts.gpu_maxbatchsize : ntransf;
+  if (b > ntransf) b = ntransf;
+  if (type != 3 && p->opts.gpu_maxbatchsize <= 0) {
+    const double grid_bytes = (double)p->nftot * cplx_size(p->comp_single);
+    const int cap = (int)std::max(1.0, std::floor(8.0 * (1 << 30) / grid_bytes));
+    if (b > cap) b = cap;
+  }
+  p->batch = b;
+  p->ev_ok = p->opts.debug != 0;
+  *out = p.release();
+  return warn ? GBN_WARN_EPS_TOO_SMALL : GBN_OK;
+}
+
+// Next n events of a pool (created on demand); null once the pool is full.
+cudaEvent_t* take_events(std::vector<cudaEvent_t>& pool, size_t& used, size_t n) {
+  constexpr size_t kMaxEvents = 1 << 14;
+  if (used + n > kMaxEvents) return nullptr;
+  while (pool.size() < used + n) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    pool.push_back(e);
+  }
+  cudaEvent_t* r = pool.data() + used;
+  used += n;
+  return r;
+}
+
+void fill_sort_state(gbn_plan_s* p) {
+  SortState& st = p->st;
+  st.pt_bin = p->pt_bin.as<int>();
+  st.pt_rank = p->pt_rank.as<int>();
+  st.bin_count = p->sorted ? p->bin_count.as<int>() : nullptr;
+  st.bin_start = p->bin_start.as<int>();
+  st.perm = p->sorted ? p->perm.as<int>() : nullptr;
+  st.sub_count = p->sub_count.as<int>();
+  st.sub_start = p->sub_start.as<int>();
+  st.sub_bin = p->sub_bin.as<int>();
+  st.sub_off = p->sub_off.as<int>();
+  st.n_sub = p->n_sub.as<int>();
+  st.recs = p->recs.p;
+  st.recs_in = p->recs_in.p;
+  st.scan_tmp = p->scan_tmp.as<int>();
+}
+
+// Fold + sort M points (coordinate type TX) onto the plan's geometry.
+template <typename TX>
+int sort_points(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
+                const FoldSpec& fs) {
+  if (M < 0) return fail(GBN_ERR_ARGS, "number of points must be >= 0");
+  if (M > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "too many points (> 2^31)");
+  if (M > 0 && (!x || (p->dim > 1 && !y) || (p->dim > 2 && !z)))
+    return fail(GBN_ERR_ARGS, "missing coordinate array");
+  cudaStream_t s = p->stream;
+  const Geom& g = p->geom;
+  const size_t rs = rec_size(p->dim, p->comp_single);
+  const size_t m = (size_t)std::max<int64_t>(M, 1);
+  GBN_CUDA(p->recs_in.ensure(m * rs, s));
+  GBN_CUDA(p->pt_bin.ensure(m * 4, s));
+  GBN_CUDA(p->pt_rank.ensure(m * 4, s));
+  if (p->sorted) {
+    const int64_t nb = g.nbins;
+    p->st.max_sub = nb + (M + g.maxsub - 1) / g.maxsub;
+    GBN_CUDA(p->recs.ensure(m * rs, s));
+    GBN_CUDA(p->perm.ensure(m * 4, s));
+    GBN_CUDA(p->bin_count.ensure((size_t)nb * 4, s));
+    GBN_CUDA(p->bin_start.ensure((size_t)nb * 4, s));
+    GBN_CUDA(p->sub_count.ensure((size_t)nb * 4, s));
+    GBN_CUDA(p->sub_start.ensure((size_t)nb * 4, s));
+    GBN_CUDA(p->sub_bin.ensure((size_t)p->st.max_sub * 4, s));
+    GBN_CUDA(p->sub_off.ensure((size_t)p->st.max_sub * 4, s));
+    GBN_CUDA(p->n_sub.ensure(4, s));
+    GBN_CUDA(p->scan_tmp.ensure((size_t)scan_tmp_ints(nb) * 4, s));
+  }
+  fill_sort_state(p);
+  if (p->sorted) GBN_CUDA(cudaMemsetAsync(p->bin_count.p, 0, (size_t)g.nbins * 4, s));
+  if (p->comp_single) {
+    GBN_CUDA((launch_fold<TX, float>(g, fs, M, x, y, z, p->st, s)));
+    GBN_CUDA(launch_sort_finish<float>(g, M, p->st, p->sorted, s));
+  } else {
+    if (std::is_same<TX, float>::value)
+      return fail(GBN_ERR_ARGS, "FP64 compute with float32 points is not supported");
+    GBN_CUDA((launch_fold<double, double>(g, fs, M, (const double*)x, (const double*)y,
+                                          (const double*)z, p->st, s)));
+    GBN_CUDA(launch_sort_finish<double>(g, M, p->st, p->sorted, s));
+  }
+  p->M = M;
+  p->pts_set = true;
+  return GBN_OK;
+}
+
+int execute_ntr(gbn_plan_s* p, void* c, void* f, int ntr);
+
+template <typename TX>
+int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z, int64_t N,
+                const TX* s, const TX* t, const TX* u) {
+  cudaStream_t st = p->stream;
+  cudaEvent_t* sev = p->ev_ok ? take_events(p->ev_setpts, p->ev_setpts_used, 2) : nullptr;
+  if (sev) GBN_CUDA(cudaEventRecord(sev[0], st));
+  if (p->type != 3) {
+    FoldSpec fs{};
+    fs.mode = 0;
+    GBN_TRY(sort_points<TX>(p, M, x, y, z, fs));
+  } else {
+    if (N < 0) return fail(GBN_ERR_ARGS, "number of targets must be >= 0");
+    if (N > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "too many targets (> 2^31)");
+    const TX* xs[3] = {x, y, z};
+    const TX* ss[3] = {s, t, u};
+    for (int d = 0; d < p->dim; ++d)
+      if ((M > 0 && !xs[d]) || (N > 0 && !ss[d])) return fail(GBN_ERR_ARGS, "missing coordinate array");
+    // extents of sources and targets (one host round trip)
+    GBN_CUDA(p->t3_minmax.ensure(sizeof(double) * 12, st));
+    const TX* arrs[6];
+    for (int d = 0; d < p->dim; ++d) {
+      arrs[d] = xs[d];
+      arrs[p->dim + d] = ss[d];
+    }
+    double* mm = p->t3_minmax.as<double>();
+    GBN_CUDA(launch_minmax<TX>(arrs, p->dim, M, mm, st));
+    GBN_CUDA(launch_minmax<TX>(arrs + p->dim, p->dim, N, mm + 2 * p->dim, st));
+    double h[12];
+    GBN_CUDA(cudaMemcpyAsync(h, mm, sizeof(double) * 4 * p->dim, cudaMemcpyDeviceToHost, st));
+    GBN_CUDA(cudaStreamSynchronize(st));
+    int64_t nmodes_inner[3] = {1, 1, 1};
+    for (int d = 0; d < p->dim; ++d) {
+      const double xmin = M > 0 ? h[2 * d] : 0.0, xmax = M > 0 ? h[2 * d + 1] : 0.0;
+      const double smin = N > 0 ? h[2 * (p->dim + d)] : 0.0;
+      const double smax = N > 0 ? h[2 * (p->dim + d) + 1] : 0.0;
+      p->nf[d] = type3_params(xmin, xmax, smin, smax, p->sigma, p->w, &p->t3_cx[d],
+                              &p->t3_cs[d], &p->t3_scale[d]);
+      nmodes_inner[d] = p->nf[d];
+    }
+    for (int d = p->dim; d < 3; ++d) p->nf[d] = 1;
+    p->nftot = p->nf[0] * p->nf[1] * p->nf[2];
+    if (p->nftot > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "type-3 grid too large (> 2^31 cells)");
+    p->Nt = N;
+    setup_geom(p);
+    // inner type-2 plan on the spreading grid, in the compute precision
+    bool remake = !p->inner;
+    if (p->inner)
+      for (int d = 0; d < p->dim; ++d)
+        if (p->inner->N[d] != nmodes_inner[d]) remake = true;
+    if (remake) {
+      p->inner.reset();
+      gbn_opts io = p->opts;
+      io.modeord = 0;
+      io.gpu_precision = 0;
+      io.debug = 0;
+      io.gpu_maxbatchsize = p->batch;
+      gbn_plan_s* ip = nullptr;
+      int r = plan_create(2, p->dim, nmodes_inner, p->iflag, p->batch, p->eps, p->comp_single,
+                          &io, (void*)st, &ip);
+      if (r >= 2) return r;
+      p->inner.reset(ip);
+    }
+    // targets -> inner type-2 points (FP64)
+    double* taus[3] = {nullptr, nullptr, nullptr};
+    for (int d = 0; d < p->dim; ++d) {
+      GBN_CUDA(p->t3_tau[d].ensure((size_t)std::max<int64_t>(N, 1) * 8, st));
+      taus[d] = p->t3_tau[d].as<double>();
+    }
+    GBN_CUDA(launch_t3_targets<TX>(p->dim, N, ss, p->t3_cs, p->t3_scale, taus, st));
+    {
+      FoldSpec fs{};
+      fs.mode = 0;
+      GBN_TRY(sort_points<double>(p->inner.get(), N, taus[0], taus[1], taus[2], fs));
+    }
+    // sources -> spreading grid
+    {
+      FoldSpec fs{};
+      fs.mode = 1;
+      for (int d = 0; d < 3; ++d) {
+        fs.center[d] = p->t3_cx[d];
+        fs.scale[d] = p->t3_scale[d];
+      }
+      GBN_TRY(sort_points<TX>(p, M, x, y, z, fs));
+    }
+    const size_t cs = cplx_size(p->comp_single);
+    GBN_CUDA(p->t3_pre.ensure((size_t)std::max<int64_t>(M, 1) * cs, st));
+    GBN_CUDA(p->t3_post.ensure((size_t)std::max<int64_t>(N, 1) * cs, st));
+    const double* ctaus[3] = {taus[0], taus[1], taus[2]};
+    if (p->comp_single) {
+      GBN_CUDA((launch_t3_prephase_factors<TX, float>(p->dim, M, xs, p->t3_cx, p->t3_cs,
+                                                       p->iflag, p->t3_pre.p, st)));
+      GBN_CUDA((launch_t3_post_factors<TX, float>(p->dim, N, ss, p->t3_cx, ctaus, p->iflag,
+                                                   p->w, p->beta, p->t3_post.p, st)));
+    } else {
+      GBN_CUDA((launch_t3_prephase_factors<double, double>(p->dim, M, (const double* const*)xs,
+                                                           p->t3_cx, p->t3_cs, p->iflag,
+                                                           p->t3_pre.p, st)));
+      GBN_CUDA((launch_t3_post_factors<double, double>(p->dim, N, (const double* const*)ss,
+                                                       p->t3_cx, ctaus, p->iflag, p->w,
+                                                       p->beta, p->t3_post.p, st)));
+    }
+  }
+  if (sev) GBN_CUDA(cudaEventRecord(sev[1], st));
+  return GBN_OK;
+}
+
+template <typename TC>
+KerSpec<TC> ker_spec(gbn_plan_s* p) {
+  KerSpec<TC> ks;
+  ks.coef = p->coef.as<TC>();
+  ks.deg = p->deg;
+  ks.meth = p->opts.gpu_kerevalmeth != 0 ? 1 : 0;
+  ks.beta = (TC)p->beta;
+  return ks;
+}
+
+int do_spread(gbn_plan_s* p, const void* c, int nb, bool c_is_compute) {
+  const Geom& g = p->geom;
+  cudaError_t e;
+  if (p->comp_single) {
+    if (p->data_single || c_is_compute)
+      e = launch_spread<float, float>(g, ker_spec<float>(p), p->method, p->M, p->st, c,
+                                      p->fine.p, nb, p->stream);
+    else
+      e = launch_spread<float, double>(g, ker_spec<float>(p), p->method, p->M, p->st, c,
+                                       p->fine.p, nb, p->stream);
+  } else {
+    e = launch_spread<double, double>(g, ker_spec<double>(p), p->method, p->M, p->st, c,
+                                      p->fine.p, nb, p->stream);
+  }
+  GBN_CUDA(e);
+  return GBN_OK;
+}
+
+int do_interp(gbn_plan_s* p, void* c, int nb) {
+  const Geom& g = p->geom;
+  cudaError_t e;
+  if (p->comp_single) {
+    if (p->data_single)
+      e = launch_interp<float, float>(g, ker_spec<float>(p), p->method, p->M, p->st, p->fine.p,
+                                      c, nb, p->stream);
+    else
+      e = launch_interp<float, double>(g, ker_spec<float>(p), p->method, p->M, p->st,
+                                       p->fine.p, c, nb, p->stream);
+  } else {
+    e = launch_interp<double, double>(g, ker_spec<double>(p), p->method, p->M, p->st, p->fine.p,
+                                      c, nb, p->stream);
+  }
+  GBN_CUDA(e);
+  return GBN_OK;
+}
+
+int do_deconv(gbn_plan_s* p, void* modes, int nb, bool to_modes) {
+  cudaError_t e;
+  if (p->comp_single) {
+    const float* phi[3] = {p->phi[0].as<float>(), p->phi[1].as<float>(), p->phi[2].as<float>()};
+    if (p->data_single)
+      e = to_modes ? launch_deconv1<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi,
+                                                  p->fine.p, modes, nb, p->stream)
+                   : launch_deconv2<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi,
+                                                  modes, p->fine.p, nb, p->stream);
+    else
+      e = to_modes ? launch_deconv1<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
+                                                   p->fine.p, modes, nb, p->stream)
+                   : launch_deconv2<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
+                                                   modes, p->fine.p, nb, p->stream);
+  } else {
+    const double* phi[3] = {p->phi[0].as<double>(), p->phi[1].as<double>(),
+                            p->phi[2].as<double>()};
+    e = to_modes ? launch_deconv1<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
+                                                  p->fine.p, modes, nb, p->stream)
+                 : launch_deconv2<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
+                                                  modes, p->fine.p, nb, p->stream);
+  }
+  GBN_CUDA(e);
+  return GBN_OK;
+}
+
+void ev_record(cudaEvent_t* ev, int i, cudaStream_t s) {
+  if (ev) cudaEventRecord(ev[i], s);
+}
+
+// Execute ntr (<= batch for inner type-2 plans, any for others) transforms.
+int execute_ntr(gbn_plan_s* p, void* c, void* f, int ntr) {
+  if (!p->pts_set) return fail(GBN_ERR_STATE, "execute called before setpts");
+  cudaStream_t s = p->stream;
+  const size_t dsz = cplx_size(p->data_single);
+  const size_t csz = cplx_size(p->comp_single);
+  GBN_CUDA(p->fine.ensure((size_t)p->batch * p->nftot * csz, s));
+  for (int t0 = 0; t0 < ntr; t0 += p->batch) {
+    const int nb = std::min(p->batch, ntr - t0);
+    cudaEvent_t* ev = p->ev_ok ? take_events(p->ev_exec, p->ev_exec_used, 4) : nullptr;
+    if (p->type == 1) {
+      const char* cb = (const char*)c + (size_t)t0 * p->M * dsz;
+      char* fb = (char*)f + (size_t)t0 * p->Ntot * dsz;
+      ev_record(ev, 0, s);
+      GBN_CUDA(cudaMemsetAsync(p->fine.p, 0, (size_t)nb * p->nftot * csz, s));
+      GBN_TRY(do_spread(p, cb, nb, false));
+      ev_record(ev, 1, s);
+      GBN_TRY(exec_fft(p, nb));
+      ev_record(ev, 2, s);
+      GBN_TRY(do_deconv(p, fb, nb, true));
+      ev_record(ev, 3, s);
+    } else if (p->type == 2) {
+      char* cb = (char*)c + (size_t)t0 * p->M * dsz;
+      const char* fb = (const char*)f + (size_t)t0 * p->Ntot * dsz;
+      ev_record(ev, 0, s);
+      GBN_TRY(do_deconv(p, (void*)fb, nb, false));
+      ev_record(ev, 1, s);
+      GBN_TRY(exec_fft(p, nb));
+      ev_record(ev, 2, s);
+      GBN_TRY(do_interp(p, cb, nb));
+      ev_record(ev, 3, s);
+    } else {
+      const char* cb = (const char*)c + (size_t)t0 * p->M * dsz;
+      char* fb = (char*)f + (size_t)t0 * p->Nt * dsz;
+      GBN_CUDA(p->t3_cbuf.ensure((size_t)p->batch * std::max<int64_t>(p->M, 1) * csz, s));
+      GBN_CUDA(p->t3_obuf.ensure((size_t)p->batch * std::max<int64_t>(p->Nt, 1) * csz, s));
+      ev_record(ev, 0, s);
+      cudaError_t e;
+      if (p->comp_single)
+        e = p->data_single ? launch_cmul<float, float, float>(p->M, nb, cb, p->t3_pre.p,
+                                                              p->t3_cbuf.p, s)
+                           : launch_cmul<double, float, float>(p->M, nb, cb, p->t3_pre.p,
+                                                               p->t3_cbuf.p, s);
+      else
+        e = launch_cmul<double, double, double>(p->M, nb, cb, p->t3_pre.p, p->t3_cbuf.p, s);
+      GBN_CUDA(e);
+      GBN_CUDA(cudaMemsetAsync(p->fine.p, 0, (size_t)nb * p->nftot * csz, s));
+      GBN_TRY(do_spread(p, p->t3_cbuf.p, nb, true));
+      ev_record(ev, 1, s);
+      // inner type 2: modes = spread grid (CMCL order), points = rescaled targets
+      GBN_TRY(execute_ntr(p->inner.get(), p->t3_obuf.p, p->fine.p, nb));
+      ev_record(ev, 2, s);
+      if (p->comp_single)
+        e = p->data_single ? launch_cmul<float, float, float>(p->Nt, nb, p->t3_obuf.p,
+                                                              p->t3_post.p, fb, s)
+                           : launch_cmul<float, double, float>(p->Nt, nb, p->t3_obuf.p,
+                                                               p->t3_post.p, fb, s);
+      else
+        e = launch_cmul<double, double, double>(p->Nt, nb, p->t3_obuf.p, p->t3_post.p, fb, s);
+      GBN_CUDA(e);
+      ev_record(ev, 3, s);
+    }
+  }
+  GBN_CUDA(cudaGetLastError());
+  return GBN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plan cache for the one-shot entry points
+// ---------------------------------------------------------------------------
+struct CacheKey {
+  int type, dim, single, iflag, ntransf, device;
+  int64_t nk[3];
+  double eps;
+  gbn_opts opts;
+  void* stream;
+  bool operator==(const CacheKey& o) const {
+    return type == o.type && dim == o.dim && single == o.single && iflag == o.iflag &&
+           ntransf == o.ntransf && device == o.device && nk[0] == o.nk[0] && nk[1] == o.nk[1] &&
+           nk[2] == o.nk[2] && eps == o.eps && stream == o.stream && opts_equal(opts, o.opts);
+  }
+  static bool opts_equal(const gbn_opts& a, const gbn_opts& b) {
+    return a.modeord == b.modeord && a.upsampfac == b.upsampfac && a.gpu_method == b.gpu_method &&
+           a.gpu_sort == b.gpu_sort && a.gpu_kerevalmeth == b.gpu_kerevalmeth &&
+           a.gpu_maxbatchsize == b.gpu_maxbatchsize && a.debug == b.debug &&
+           a.gpu_binsizex == b.gpu_binsizex && a.gpu_binsizey == b.gpu_binsizey &&
+           a.gpu_binsizez == b.gpu_binsizez && a.gpu_maxsubprobsize == b.gpu_maxsubprobsize &&
+           a.gpu_precision == b.gpu_precision;
+  }
+};
+
+struct PlanCache {
+  std::mutex mu;
+  std::list<std::pair<CacheKey, gbn_plan_s*>> idle;  // most recent first
+  size_t capacity = 8;
+
+  gbn_plan_s* take(const CacheKey& k) {
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto it = idle.begin(); it != idle.end(); ++it)
+      if (it->first == k) {
+        gbn_plan_s* p = it->second;
+        idle.erase(it);
+        return p;
+      }
+    return nullptr;
+  }
+  void give(const CacheKey& k, gbn_plan_s* p) {
+    std::vector<gbn_plan_s*> evict;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      idle.emplace_front(k, p);
+      while (idle.size() > capacity) {
+        evict.push_back(idle.back().second);
+        idle.pop_back();
+      }
+    }
+    for (auto* q : evict) delete q;
+  }
+  void clear() {
+    std::list<std::pair<CacheKey, gbn_plan_s*>> all;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      all.swap(idle);
+    }
+    for (auto& kv : all) delete kv.second;
+  }
+};
+
+PlanCache& cache() {
+  static PlanCache* c = new PlanCache();  // never destroyed: no CUDA calls at exit
+  return *c;
+}
+
+template <typename TX>
+int run_oneshot(int type, int dim, bool single, void* stream, double eps, int iflag,
+                int64_t n_tot, int64_t n_transf, int64_t n_j, const int64_t* n_k,
+                const gbn_opts* opts, const void* source, const TX* const* pts,
+                const TX* const* tgts, void* output) {
+  if (n_tot < 0 || n_transf < 0 || n_j < 0) return fail(GBN_ERR_ARGS, "negative size");
+  if (n_transf > INT32_MAX) return fail(GBN_ERR_ARGS, "n_transf too large");
+  if (n_tot == 0 || n_transf == 0) return GBN_OK;
+  int64_t nk[3] = {1, 1, 1};
+  int64_t n_k_total = 1;
+  if (type != 3) {
+    for (int d = 0; d < dim; ++d) {
+      nk[d] = n_k[d];
+      n_k_total *= n_k[d];
+    }
+  } else {
+    n_k_total = n_k[0];
+  }
+  CacheKey key;
+  std::memset(&key, 0, sizeof(key));
+  key.type = type;
+  key.dim = dim;
+  key.single = single;
+  key.iflag = iflag >= 0 ? 1 : -1;
+  key.ntransf = (int)n_transf;
+  GBN_CUDA(cudaGetDevice(&key.device));
+  for (int d = 0; d < 3; ++d) key.nk[d] = nk[d];
+  key.eps = eps;
+  if (opts)
+    key.opts = *opts;
+  else
+    gbn_default_opts(&key.opts);
+  key.stream = stream;
+  gbn_plan_s* p = cache().take(key);
+  int warn = 0;
+  if (!p) {
+    int r = plan_create(type, dim, nk, iflag, (int)n_transf, eps, single, &key.opts, stream, &p);
+    if (r >= 2) return r;
+    warn = r;
+  } else {
+    warn = p->warn;
+  }
+  const size_t dsz = cplx_size(single);
+  int ret = GBN_OK;
+  for (int64_t idx = 0; idx < n_tot && ret < 2; ++idx) {
+    const int64_t i = idx * n_j;
+    const int64_t j = idx * n_j * n_transf;
+    const int64_t k = idx * n_k_total * n_transf;
+    const TX* xs[3] = {nullptr, nullptr, nullptr};
+    const TX* ss[3] = {nullptr, nullptr, nullptr};
+    for (int d = 0; d < dim; ++d) {
+      xs[d] = pts[d] ? pts[d] + i : nullptr;
+      if (type == 3) ss[d] = tgts[d] ? tgts[d] + idx * n_k_total : nullptr;
+    }
+    ret = plan_setpts<TX>(p, n_j, xs[0], xs[1], xs[2], type == 3 ? n_k_total : 0, ss[0], ss[1],
+                          ss[2]);
+    if (ret >= 2) break;
+    const char* src = (const char*)source;
+    char* out = (char*)output;
+    if (type == 2)
+      ret = execute_ntr(p, out + (size_t)j * dsz, (void*)(src + (size_t)k * dsz), p->ntransf);
+    else
+      ret = execute_ntr(p, (void*)(src + (size_t)j * dsz), out + (size_t)k * dsz, p->ntransf);
+  }
+  if (ret >= 2) {
+    delete p;  // state unknown after a failure: do not cache
+    return ret;
+  }
+  cache().give(key, p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(GBN_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e));
+  return warn ? GBN_WARN_EPS_TOO_SMALL : GBN_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+void gbn_default_opts(gbn_opts* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->modeord = 0;
+  o->upsampfac = 2.0;
+  o->gpu_method = 0;
+  o->gpu_sort = 1;
+  o->gpu_kerevalmeth = 1;
+  o->gpu_maxbatchsize = 0;
+  o->debug = 0;
+  o->gpu_maxsubprobsize = 1024;
+  o->gpu_precision = 0;
+}
+
+const char* gbn_last_error(void) { return g_err.c_str(); }
+
+int gbn_makeplan(int type, int dim, const int64_t* nmodes, int iflag, int ntransf, double eps,
+                 gbn_plan* plan, const gbn_opts* opts, void* stream) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan pointer is NULL");
+  if (type != 3 && !nmodes) return fail(GBN_ERR_ARGS, "nmodes is NULL");
+  return plan_create(type, dim, nmodes, iflag, ntransf, eps, false, opts, stream, plan);
+}
+
+int gbnf_makeplan(int type, int dim, const int64_t* nmodes, int iflag, int ntransf, float eps,
+                  gbn_plan* plan, const gbn_opts* opts, void* stream) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan pointer is NULL");
+  if (type != 3 && !nmodes) return fail(GBN_ERR_ARGS, "nmodes is NULL");
+  return plan_create(type, dim, nmodes, iflag, ntransf, (double)eps, true, opts, stream, plan);
+}
+
+int gbn_setpts(gbn_plan plan, int64_t M, const double* x, const double* y, const double* z,
+               int64_t N, const double* s, const double* t, const double* u) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  if (plan->data_single) return fail(GBN_ERR_ARGS, "complex64 plan: use gbnf_setpts");
+  return plan_setpts<double>(plan, M, x, y, z, N, s, t, u);
+}
+
+int gbnf_setpts(gbn_plan plan, int64_t M, const float* x, const float* y, const float* z,
+                int64_t N, const float* s, const float* t, const float* u) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  if (!plan->data_single) return fail(GBN_ERR_ARGS, "complex128 plan: use gbn_setpts");
+  if (!plan->comp_single) return fail(GBN_ERR_ARGS, "FP64 compute needs float64 points");
+  return plan_setpts<float>(plan, M, x, y, z, N, s, t, u);
+}
+
+int gbn_execute(gbn_plan plan, void* c, void* f) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  return execute_ntr(plan, c, f, plan->ntransf);
+}
+
+int gbn_set_stream(gbn_plan plan, void* stream) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  plan->stream = (cudaStream_t)stream;
+  if (plan->inner) plan->inner->stream = (cudaStream_t)stream;
+  return GBN_OK;
+}
+
+int gbn_destroy(gbn_plan plan) {
+  delete plan;
+  return GBN_OK;
+}
+
+int gbn_plan_info(gbn_plan plan, int* w, int64_t* nf3, int* method, int* compute_double) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  if (w) *w = plan->w;
+  if (nf3)
+    for (int d = 0; d < 3; ++d) nf3[d] = plan->nf[d];
+  if (method) *method = plan->method;
+  if (compute_double) *compute_double = plan->comp_single ? 0 : 1;
+  return GBN_OK;
+}
+
+int gbn_get_timings(gbn_plan plan, float* ms5, int* nbatch) {
+  if (!plan || !ms5) return fail(GBN_ERR_ARGS, "NULL argument");
+  if (!plan->ev_ok) return fail(GBN_ERR_STATE, "plan was made without opts.debug");
+  GBN_CUDA(cudaStreamSynchronize(plan->stream));
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (size_t i = 0; i + 4 <= plan->ev_exec_used; i += 4) {
+    float a = 0, b = 0, c = 0;
+    cudaEvent_t* e = plan->ev_exec.data() + i;
+    GBN_CUDA(cudaEventElapsedTime(&a, e[0], e[1]));
+    GBN_CUDA(cudaEventElapsedTime(&b, e[1], e[2]));
+    GBN_CUDA(cudaEventElapsedTime(&c, e[2], e[3]));
+    if (plan->type == 3) {
+      acc[3] += a + c;
+      acc[1] += b;
+    } else {
+      acc[0] += plan->type == 1 ? a : c;
+      acc[1] += b;
+      acc[2] += plan->type == 1 ? c : a;
+    }
+  }
+  for (size_t i = 0; i + 2 <= plan->ev_setpts_used; i += 2) {
+    float a = 0;
+    GBN_CUDA(cudaEventElapsedTime(&a, plan->ev_setpts[i], plan->ev_setpts[i + 1]));
+    acc[4] += a;
+  }
+  for (int i = 0; i < 5; ++i) ms5[i] = (float)acc[i];
+  if (nbatch) *nbatch = (int)(plan->ev_exec_used / 4);
+  plan->ev_exec_used = 0;
+  plan->ev_setpts_used = 0;
+  return GBN_OK;
+}
+
+int gbn_debug_bins(gbn_plan plan, int64_t* bins_out, int64_t* counts_out, int64_t* nbins) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  if (nbins) *nbins = plan->geom.nbins;
+  if (!plan->pts_set || !plan->sorted) return fail(GBN_ERR_STATE, "no sorted points");
+  GBN_CUDA(cudaStreamSynchronize(plan->stream));
+  if (bins_out && plan->M > 0) {
+    std::vector<int> b((size_t)plan->M);
+    GBN_CUDA(cudaMemcpy(b.data(), plan->pt_bin.p, b.size() * 4, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < b.size(); ++i) bins_out[i] = b[i];
+  }
+  if (counts_out) {
+    std::vector<int> b((size_t)plan->geom.nbins);
+    GBN_CUDA(cudaMemcpy(b.data(), plan->bin_count.p, b.size() * 4, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < b.size(); ++i) counts_out[i] = b[i];
+  }
+  return GBN_OK;
+}
+
+int gbn_debug_fold(gbn_plan plan, int64_t* i0_out, double* delta_out) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  if (!plan->pts_set) return fail(GBN_ERR_STATE, "no points");
+  GBN_CUDA(cudaStreamSynchronize(plan->stream));
+  const int dim = plan->dim;
+  const size_t rs = rec_size(dim, plan->comp_single);
+  std::vector<unsigned char> raw((size_t)plan->M * rs);
+  if (plan->M > 0)
+    GBN_CUDA(cudaMemcpy(raw.data(), plan->recs_in.p, raw.size(), cudaMemcpyDeviceToHost));
+  for (int64_t j = 0; j < plan->M; ++j) {
+    const unsigned char* r = raw.data() + (size_t)j * rs;
+    for (int d = 0; d < 3; ++d) {
+      int64_t iv = 0;
+      double dv = 0.0;
+      if (d < dim) {
+        if (plan->comp_single) {
+          float f;
+          int ii;
+          std::memcpy(&f, r + d * 4, 4);
+          std::memcpy(&ii, r + dim * 4 + d * 4, 4);
+          dv = f;
+          iv = ii;
+        } else {
+          double f;
+          int ii;
+          std::memcpy(&f, r + d * 8, 8);
+          std::memcpy(&ii, r + dim * 8 + d * 4, 4);
+          dv = f;
+          iv = ii;
+        }
+      }
+      if (i0_out) i0_out[j * 3 + d] = iv;
+      if (delta_out) delta_out[j * 3 + d] = dv;
+    }
+  }
+  return GBN_OK;
+}
+
+void gbn_clear_cache(void) { cache().clear(); }
+
+long long gbn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int gbn_run(int type, int dim, int single, void* stream, double eps, int iflag, int64_t n_tot,
+            int64_t n_transf, int64_t n_j, const int64_t* n_k, const gbn_opts* opts,
+            const void* source, const void* const* pts, const void* const* tgts, void* output) {
+  if (type < 1 || type > 3 || dim < 1 || dim > 3) return fail(GBN_ERR_ARGS, "bad type or dim");
+  if (!n_k || !pts) return fail(GBN_ERR_ARGS, "NULL n_k or points");
+  if (type == 3 && !tgts) return fail(GBN_ERR_ARGS, "NULL targets");
+  if (single) {
+    const float* p[3] = {(const float*)pts[0], dim > 1 ? (const float*)pts[1] : nullptr,
+                         dim > 2 ? (const float*)pts[2] : nullptr};
+    const float* t[3] = {nullptr, nullptr, nullptr};
+    if (type == 3)
+      for (int d = 0; d < dim; ++d) t[d] = (const float*)tgts[d];
+    return run_oneshot<float>(type, dim, true, stream, eps, iflag, n_tot, n_transf, n_j, n_k,
+                              opts, source, p, t, output);
+  }
+  const double* p[3] = {(const double*)pts[0], dim > 1 ? (const double*)pts[1] : nullptr,
+                        dim > 2 ? (const double*)pts[2] : nullptr};
+  const double* t[3] = {nullptr, nullptr, nullptr};
+  if (type == 3)
+    for (int d = 0; d < dim; ++d) t[d] = (const double*)tgts[d];
+  return run_oneshot<double>(type, dim, false, stream, eps, iflag, n_tot, n_transf, n_j, n_k,
+                             opts, source, p, t, output);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// the 18 named one-shot entry points (reference FFI target names)
+// ---------------------------------------------------------------------------
+namespace {
+gbn_opts opts_from_attrs(int64_t modeord, double upsampfac, int64_t gpu_method, int64_t gpu_sort,
+                         int64_t gpu_kerevalmeth, int64_t gpu_maxbatchsize, int64_t debug) {
+  gbn_opts o;
+  gbn_default_opts(&o);
+  o.modeord = (int)modeord;
+  o.upsampfac = upsampfac;
+  o.gpu_method = (int)gpu_method;
+  o.gpu_sort = (int)gpu_sort;
+  o.gpu_kerevalmeth = (int)gpu_kerevalmeth;
+  o.gpu_maxbatchsize = (int)gpu_maxbatchsize;
+  o.debug = (int)debug;
+  return o;
+}
+}  // namespace
+
+#define GBN_ONESHOT_BODY(TYPE, DIM, SINGLE, TX, ...)                                             \
+  {                                                                                              \
+    gbn_opts o = opts_from_attrs(modeord, upsampfac, gpu_method, gpu_sort, gpu_kerevalmeth,      \
+                                 gpu_maxbatchsize, debug);                                       \
+    const int64_t nk[3] = {n_k_1, n_k_2, n_k_3};                                                 \
+    const void* P[6] = {__VA_ARGS__};                                                            \
+    const void* pts[3] = {P[0], DIM > 1 ? P[1] : nullptr, DIM > 2 ? P[2] : nullptr};             \
+    const void* tg[3] = {TYPE == 3 ? P[DIM] : nullptr, (TYPE == 3 && DIM > 1) ? P[DIM + 1] : nullptr, \
+                         (TYPE == 3 && DIM > 2) ? P[DIM + 2] : nullptr};                         \
+    return gbn_run(TYPE, DIM, SINGLE, stream, (double)eps, (int)iflag, n_tot, n_transf, n_j, nk, \
+                   &o, source, pts, tg, output);                                                 \
+  }
+
+extern "C" {
+int gbn_nufft1d1f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, void* output)
+    GBN_ONESHOT_BODY(1, 1, 1, float, x, nullptr, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft1d1(GBN_ONESHOT_ARGS_D, const void* source, const double* x, void* output)
+    GBN_ONESHOT_BODY(1, 1, 0, double, x, nullptr, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft2d1f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y, void* output)
+    GBN_ONESHOT_BODY(1, 2, 1, float, x, y, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft2d1(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y, void* output)
+    GBN_ONESHOT_BODY(1, 2, 0, double, x, y, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft3d1f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* z, void* output)
+    GBN_ONESHOT_BODY(1, 3, 1, float, x, y, z, nullptr, nullptr, nullptr)
+int gbn_nufft3d1(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* z, void* output)
+    GBN_ONESHOT_BODY(1, 3, 0, double, x, y, z, nullptr, nullptr, nullptr)
+int gbn_nufft1d2f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, void* output)
+    GBN_ONESHOT_BODY(2, 1, 1, float, x, nullptr, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft1d2(GBN_ONESHOT_ARGS_D, const void* source, const double* x, void* output)
+    GBN_ONESHOT_BODY(2, 1, 0, double, x, nullptr, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft2d2f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y, void* output)
+    GBN_ONESHOT_BODY(2, 2, 1, float, x, y, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft2d2(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y, void* output)
+    GBN_ONESHOT_BODY(2, 2, 0, double, x, y, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft3d2f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* z, void* output)
+    GBN_ONESHOT_BODY(2, 3, 1, float, x, y, z, nullptr, nullptr, nullptr)
+int gbn_nufft3d2(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* z, void* output)
+    GBN_ONESHOT_BODY(2, 3, 0, double, x, y, z, nullptr, nullptr, nullptr)
+int gbn_nufft1d3f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* s, void* output)
+    GBN_ONESHOT_BODY(3, 1, 1, float, x, s, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft1d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* s, void* output)
+    GBN_ONESHOT_BODY(3, 1, 0, double, x, s, nullptr, nullptr, nullptr, nullptr)
+int gbn_nufft2d3f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* s, const float* t, void* output)
+    GBN_ONESHOT_BODY(3, 2, 1, float, x, y, s, t, nullptr, nullptr)
+int gbn_nufft2d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* s, const double* t, void* output)
+    GBN_ONESHOT_BODY(3, 2, 0, double, x, y, s, t, nullptr, nullptr)
+int gbn_nufft3d3f(GBN_ONESHOT_ARGS_F, const void* source, const float* x, const float* y,
+                  const float* z, const float* s, const float* t, const float* u, void* output)
+    GBN_ONESHOT_BODY(3, 3, 1, float, x, y, z, s, t, u)
+int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const double* y,
+                 const double* z, const double* s, const double* t, const double* u,
+                 void* output)
+    GBN_ONESHOT_BODY(3, 3, 0, double, x, y, z, s, t, u)
+}  // extern "C"

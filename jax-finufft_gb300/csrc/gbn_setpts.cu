@@ -1,0 +1,753 @@
+// gbn_setpts.cu -- point folding and bin sort (setpts), deconvolution and
+// mode reordering, and the type-3 phase kernels.
+//
+// These kernels replace the setpts stage and the deconvolve stage of the
+// vendored cuFINUFFT that lib/cufinufft_wrapper.cc:63-89 calls (per
+// lib/kernels.cc.cu:57-80).  All HBM-bound; each reads and writes its arrays
+// once with coalesced accesses.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gbn_common.cuh"
+
+namespace gbn {
+
+namespace {
+
+constexpr double kInv2Pi = 0.159154943091895335768883763372514362;
+
+// Periodic fold onto [0, nf) with one rounding per operation (bit-identical
+// to the CPU restatement, which is compiled with -ffp-contract=off).
+__device__ __forceinline__ double fold_rn(double x, int64_t nf) {
+  if (!isfinite(x)) return 0.0;
+  double t = __dmul_rn(x, kInv2Pi);
+  double f = __dsub_rn(t, floor(t));
+  double X = __dmul_rn(f, (double)nf);
+  if (X >= (double)nf) X = __dsub_rn(X, (double)nf);
+  return X;
+}
+
+// Type-3 rescale: X = (x - center)*scale + nf/2, wrapped once into [0, nf).
+__device__ __forceinline__ double rescale_rn(double x, double center, double scale, int64_t nf) {
+  if (!isfinite(x)) return 0.0;
+  double d = __dsub_rn(x, center);
+  double X = __dmul_rn(d, scale);
+  X = __dadd_rn(X, 0.5 * (double)nf);
+  if (X < 0.0) X = __dadd_rn(X, (double)nf);
+  if (X >= (double)nf) X = __dsub_rn(X, (double)nf);
+  return X;
+}
+
+template <typename TX, typename TC, int DIM>
+__global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict__ x,
+                            const TX* __restrict__ y, const TX* __restrict__ z,
+                            int* __restrict__ pt_bin, int* __restrict__ pt_rank,
+                            int* __restrict__ bin_count, PtRec<TC, DIM>* __restrict__ recs_in,
+                            int count_bins) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = j < M;
+  int bin = 0;
+  if (valid) {
+    const TX* c[3] = {x, y, z};
+    PtRec<TC, DIM> r;
+    int stride = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const double xv = (double)c[d][j];
+      const double X = fs.mode == 0 ? fold_rn(xv, g.nf[d])
+                                    : rescale_rn(xv, fs.center[d], fs.scale[d], g.nf[d]);
+      const double s = __dsub_rn(X, 0.5 * (double)g.w);
+      const double cl = ceil(s);
+      r.i[d] = (int)cl;
+      r.d[d] = (TC)__dsub_rn(cl, s);
+      const int fl = (int)floor(X);
+      bin += (fl / g.bs[d]) * stride;
+      stride *= g.nb[d];
+    }
+    recs_in[j] = r;
+  }
+  if (!count_bins) return;
+  // Warp-aggregated bin counting: lanes that share a bin make one atomic.
+  const unsigned active = __ballot_sync(0xffffffffu, valid);
+  if (valid) {
+    const unsigned peers = __match_any_sync(active, bin);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&bin_count[bin], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    pt_bin[j] = bin;
+    pt_rank[j] = base + __popc(peers & ((1u << lane) - 1u));
+  }
+}
+
+// --- exclusive scan of int32 ------------------------------------------------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
+  __shared__ int warp_sums[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int n = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += n;
+  }
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int ws = warp_sums[lane];
+    int wi = ws;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int n = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += n;
+    }
+    warp_sums[lane] = wi - ws;
+    if (lane == 31) *total = wi;
+  }
+  __syncthreads();
+  int r = incl - v + warp_sums[warp];
+  __syncthreads();
+  return r;
+}
+
+__global__ void scan_local_kernel(const int* in, int* out, int64_t n, int* block_sums) {
+  __shared__ int total;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n) ? in[base + i] : 0;
+    s += v[i];
+  }
+  int ex = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) out[base + i] = ex;
+    ex += v[i];
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void scan_sums_kernel(int* sums, int64_t nb) {
+  __shared__ int total;
+  int carry = 0;
+  for (int64_t b0 = 0; b0 < nb; b0 += kScanThreads) {
+    const int64_t i = b0 + threadIdx.x;
+    int v = i < nb ? sums[i] : 0;
+    int ex = block_exclusive_scan(v, &total);
+    if (i < nb) sums[i] = ex + carry;
+    carry += total;
+    __syncthreads();
+  }
+}
+
+__global__ void scan_add_kernel(int* out, int64_t n, const int* sums) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += sums[i / kScanTile];
+}
+
+// --- bin-order scatter and subproblems ---------------------------------------
+template <typename REC>
+__global__ void scatter_kernel(int64_t M, const int* __restrict__ pt_bin,
+                               const int* __restrict__ pt_rank, const int* __restrict__ bin_start,
+                               const REC* __restrict__ recs_in, REC* __restrict__ recs,
+                               int* __restrict__ perm) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  const int pos = bin_start[pt_bin[j]] + pt_rank[j];
+  perm[pos] = (int)j;
+  recs[pos] = recs_in[j];
+}
+
+__global__ void subcount_kernel(int64_t nbins, const int* __restrict__ bin_count, int maxsub,
+                                int* __restrict__ sub_count) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nbins) sub_count[b] = (bin_count[b] + maxsub - 1) / maxsub;
+}
+
+__global__ void subfill_kernel(int64_t nbins, const int* __restrict__ sub_count,
+                               const int* __restrict__ sub_start, int maxsub,
+                               int* __restrict__ sub_bin, int* __restrict__ sub_off,
+                               int* __restrict__ n_sub) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  const int n = sub_count[b], s0 = sub_start[b];
+  for (int s = 0; s < n; ++s) {
+    sub_bin[s0 + s] = (int)b;
+    sub_off[s0 + s] = s * maxsub;
+  }
+  if (b == nbins - 1) *n_sub = s0 + n;
+}
+
+// --- deconvolution -------------------------------------------------------------
+__device__ __forceinline__ int64_t mode_freq(int64_t i, int64_t N, int modeord) {
+  if (modeord == 0) return i - N / 2;
+  return i < (N + 1) / 2 ? i : i - N;
+}
+
+// Fine index g -> output index along one axis, or -1 when g holds no mode.
+__device__ __forceinline__ int64_t fine_to_mode(int64_t g, int64_t N, int64_t nf, int modeord) {
+  int64_t k;
+  if (g <= (N - 1) / 2)
+    k = g;
+  else if (g >= nf - N / 2)
+    k = g - nf;
+  else
+    return -1;
+  if (modeord == 0) return k + N / 2;
+  return k >= 0 ? k : k + N;
+}
+
+template <typename TC, typename TD, int DIM>
+__global__ void deconv1_kernel(int64_t N0, int64_t N1, int64_t N2, int64_t nf0, int64_t nf1,
+                               int64_t nf2, int modeord, const TC* __restrict__ p0,
+                               const TC* __restrict__ p1, const TC* __restrict__ p2,
+                               const cplx_t<TC>* __restrict__ fine, cplx_t<TD>* __restrict__ out,
+                               int ntr) {
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i0 >= N0) return;
+  int64_t k0 = mode_freq(i0, N0, modeord);
+  const int64_t g0 = k0 < 0 ? k0 + nf0 : k0;
+  for (int64_t i1 = blockIdx.y; i1 < N1; i1 += gridDim.y) {
+  int64_t g1 = 0;
+  TC f = p0[i0];
+  if (DIM > 1) {
+    int64_t k1 = mode_freq(i1, N1, modeord);
+    g1 = k1 < 0 ? k1 + nf1 : k1;
+    f *= p1[i1];
+  }
+  for (int64_t zz = blockIdx.z; zz < (int64_t)N2 * ntr; zz += gridDim.z) {
+    const int64_t t = zz / N2, i2 = zz - t * N2;
+    int64_t g2 = 0;
+    TC ff = f;
+    if (DIM > 2) {
+      int64_t k2 = mode_freq(i2, N2, modeord);
+      g2 = k2 < 0 ? k2 + nf2 : k2;
+      ff *= p2[i2];
+    }
+    const cplx_t<TC> v = fine[((t * nf2 + g2) * nf1 + g1) * nf0 + g0];
+    cplx_t<TD> o;
+    o.x = (TD)(v.x * ff);
+    o.y = (TD)(v.y * ff);
+    out[((t * N2 + i2) * N1 + i1) * N0 + i0] = o;
+  }
+  }
+}
+
+template <typename TC, typename TD, int DIM>
+__global__ void deconv2_kernel(int64_t N0, int64_t N1, int64_t N2, int64_t nf0, int64_t nf1,
+                               int64_t nf2, int modeord, const TC* __restrict__ p0,
+                               const TC* __restrict__ p1, const TC* __restrict__ p2,
+                               const cplx_t<TD>* __restrict__ in, cplx_t<TC>* __restrict__ fine,
+                               int ntr) {
+  const int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g0 >= nf0) return;
+  const int64_t i0 = fine_to_mode(g0, N0, nf0, modeord);
+  for (int64_t g1 = blockIdx.y; g1 < nf1; g1 += gridDim.y) {
+  const int64_t i1 = DIM > 1 ? fine_to_mode(g1, N1, nf1, modeord) : 0;
+  TC f = 0;
+  if (i0 >= 0 && i1 >= 0) f = p0[i0] * (DIM > 1 ? p1[i1] : TC(1));
+  for (int64_t zz = blockIdx.z; zz < (int64_t)nf2 * ntr; zz += gridDim.z) {
+    const int64_t t = zz / nf2, g2 = zz - t * nf2;
+    const int64_t i2 = DIM > 2 ? fine_to_mode(g2, N2, nf2, modeord) : 0;
+    cplx_t<TC> o;
+    o.x = 0;
+    o.y = 0;
+    if (i0 >= 0 && i1 >= 0 && i2 >= 0) {
+      const TC ff = DIM > 2 ? f * p2[i2] : f;
+      const cplx_t<TD> v = in[((t * N2 + i2) * N1 + i1) * N0 + i0];
+      o.x = (TC)v.x * ff;
+      o.y = (TC)v.y * ff;
+    }
+    fine[((t * nf2 + g2) * nf1 + g1) * nf0 + g0] = o;
+  }
+  }
+}
+
+// --- type 3 -----------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long dkey(double v) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+template <typename TX>
+__global__ void minmax_kernel(const TX* __restrict__ a, int64_t n, unsigned long long* out) {
+  unsigned long long lo = ~0ull, hi = 0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = (double)a[i];
+    if (!isfinite(v)) continue;
+    unsigned long long k = dkey(v);
+    lo = k < lo ? k : lo;
+    hi = k > hi ? k : hi;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    lo = l2 < lo ? l2 : lo;
+    hi = h2 > hi ? h2 : hi;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[0], lo);
+    atomicMax(&out[1], hi);
+  }
+}
+
+__global__ void minmax_init_kernel(unsigned long long* k, int narr) {
+  int i = threadIdx.x;
+  if (i < narr) {
+    k[2 * i] = ~0ull;
+    k[2 * i + 1] = 0ull;
+  }
+}
+
+__global__ void minmax_decode_kernel(const unsigned long long* k, double* out, int narr) {
+  int i = threadIdx.x;
+  if (i < 2 * narr) {
+    unsigned long long b = k[i];
+    if (i % 2 == 0 && b == ~0ull) {
+      out[i] = 0.0;  // no finite values
+      return;
+    }
+    if (i % 2 == 1 && b == 0ull) {
+      out[i] = 0.0;
+      return;
+    }
+    b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
+    out[i] = __longlong_as_double((long long)b);
+  }
+}
+
+struct Ptrs3 {
+  const void* p[3];
+};
+struct DPtrs3 {
+  double* p[3];
+};
+struct CDPtrs3 {
+  const double* p[3];
+};
+
+template <typename TX>
+__global__ void t3_targets_kernel(int dim, int64_t N, Ptrs3 s, double c0, double c1, double c2,
+                                  double sc0, double sc1, double sc2, DPtrs3 tau) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double c[3] = {c0, c1, c2}, sc[3] = {sc0, sc1, sc2};
+  for (int d = 0; d < dim; ++d) {
+    double v = (double)((const TX*)s.p[d])[k];
+    tau.p[d][k] = isfinite(v) ? (v - c[d]) / sc[d] : 0.0;
+  }
+}
+
+template <typename TX, typename TC>
+__global__ void t3_pre_kernel(int dim, int64_t M, Ptrs3 x, double cx0, double cx1, double cx2,
+                              double cs0, double cs1, double cs2, int iflag,
+                              cplx_t<TC>* __restrict__ fac) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  const double cx[3] = {cx0, cx1, cx2}, cs[3] = {cs0, cs1, cs2};
+  double ph = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    double v = (double)((const TX*)x.p[d])[j];
+    if (!isfinite(v)) v = cx[d];
+    ph += cs[d] * (v - cx[d]);
+  }
+  double sn, cn;
+  sincos((double)iflag * ph, &sn, &cn);
+  cplx_t<TC> o;
+  o.x = (TC)cn;
+  o.y = (TC)sn;
+  fac[j] = o;
+}
+
+constexpr int kMaxQuad = 64;
+struct Quad {
+  int q;
+  double t[kMaxQuad];
+  double f[kMaxQuad];
+};
+
+template <typename TX, typename TC>
+__global__ void t3_post_kernel(int dim, int64_t N, Ptrs3 s, double cx0, double cx1, double cx2,
+                               CDPtrs3 tau, int iflag, Quad qd, cplx_t<TC>* __restrict__ fac) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double cx[3] = {cx0, cx1, cx2};
+  double ph = 0.0, den = 1.0;
+  for (int d = 0; d < dim; ++d) {
+    double v = (double)((const TX*)s.p[d])[k];
+    if (!isfinite(v)) v = 0.0;
+    ph += cx[d] * v;
+    const double tv = tau.p[d][k];
+    double acc = 0.0;
+    for (int i = 0; i < qd.q; ++i) acc += qd.f[i] * cos(tv * qd.t[i]);
+    den *= acc;
+  }
+  double sn, cn;
+  sincos((double)iflag * ph, &sn, &cn);
+  cplx_t<TC> o;
+  o.x = (TC)(cn / den);
+  o.y = (TC)(sn / den);
+  fac[k] = o;
+}
+
+template <typename TI, typename TO, typename TF>
+__global__ void cmul_kernel(int64_t n, int ntr, const cplx_t<TI>* __restrict__ in,
+                            const cplx_t<TF>* __restrict__ fac, cplx_t<TO>* __restrict__ out) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const cplx_t<TF> f = fac[j];
+  for (int t = 0; t < ntr; ++t) {
+    const cplx_t<TI> v = in[(int64_t)t * n + j];
+    const TF vr = (TF)v.x, vi = (TF)v.y;
+    cplx_t<TO> o;
+    o.x = (TO)(vr * f.x - vi * f.y);
+    o.y = (TO)(vr * f.y + vi * f.x);
+    out[(int64_t)t * n + j] = o;
+  }
+}
+
+inline unsigned grid1(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+// =============================================================================
+// launchers
+// =============================================================================
+
+template <typename TX, typename TC>
+cudaError_t launch_fold(const Geom& g, const FoldSpec& fs, int64_t M, const TX* x, const TX* y,
+                        const TX* z, SortState& st, cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  const unsigned nb = grid1(M, kThreads);
+  const int count = st.bin_count != nullptr;
+  switch (g.dim) {
+    case 1:
+      fold_kernel<TX, TC, 1><<<nb, kThreads, 0, s>>>(g, fs, M, x, y, z, st.pt_bin, st.pt_rank,
+                                                     st.bin_count,
+                                                     (PtRec<TC, 1>*)st.recs_in, count);
+      note_launch();
+      break;
+    case 2:
+      fold_kernel<TX, TC, 2><<<nb, kThreads, 0, s>>>(g, fs, M, x, y, z, st.pt_bin, st.pt_rank,
+                                                     st.bin_count,
+                                                     (PtRec<TC, 2>*)st.recs_in, count);
+      note_launch();
+      break;
+    default:
+      fold_kernel<TX, TC, 3><<<nb, kThreads, 0, s>>>(g, fs, M, x, y, z, st.pt_bin, st.pt_rank,
+                                                     st.bin_count,
+                                                     (PtRec<TC, 3>*)st.recs_in, count);
+      note_launch();
+      break;
+  }
+  return cudaGetLastError();
+}
+
+int64_t scan_tmp_ints(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+cudaError_t launch_scan(const int* in, int* out, int64_t n, int* tmp, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int64_t nblk = (n + kScanTile - 1) / kScanTile;
+  scan_local_kernel<<<(unsigned)nblk, kScanThreads, 0, s>>>(in, out, n, tmp);
+  note_launch();
+  if (nblk > 1) {
+    scan_sums_kernel<<<1, kScanThreads, 0, s>>>(tmp, nblk);
+    note_launch();
+    scan_add_kernel<<<grid1(n, 256), 256, 0, s>>>(out, n, tmp);
+    note_launch();
+  }
+  return cudaGetLastError();
+}
+
+template <typename TC>
+cudaError_t launch_sort_finish(const Geom& g, int64_t M, SortState& st, bool sorted,
+                               cudaStream_t s) {
+  if (!sorted) return cudaSuccess;
+  cudaError_t e = launch_scan(st.bin_count, st.bin_start, g.nbins, st.scan_tmp, s);
+  if (e != cudaSuccess) return e;
+  if (M > 0) {
+    const unsigned nb = grid1(M, kThreads);
+    switch (g.dim) {
+      case 1:
+        scatter_kernel<PtRec<TC, 1>><<<nb, kThreads, 0, s>>>(
+            M, st.pt_bin, st.pt_rank, st.bin_start, (const PtRec<TC, 1>*)st.recs_in,
+            (PtRec<TC, 1>*)st.recs, st.perm);
+        note_launch();
+        break;
+      case 2:
+        scatter_kernel<PtRec<TC, 2>><<<nb, kThreads, 0, s>>>(
+            M, st.pt_bin, st.pt_rank, st.bin_start, (const PtRec<TC, 2>*)st.recs_in,
+            (PtRec<TC, 2>*)st.recs, st.perm);
+        note_launch();
+        break;
+      default:
+        scatter_kernel<PtRec<TC, 3>><<<nb, kThreads, 0, s>>>(
+            M, st.pt_bin, st.pt_rank, st.bin_start, (const PtRec<TC, 3>*)st.recs_in,
+            (PtRec<TC, 3>*)st.recs, st.perm);
+        note_launch();
+        break;
+    }
+  }
+  const unsigned nbb = grid1(g.nbins, 256);
+  subcount_kernel<<<nbb, 256, 0, s>>>(g.nbins, st.bin_count, g.maxsub, st.sub_count);
+  note_launch();
+  e = launch_scan(st.sub_count, st.sub_start, g.nbins, st.scan_tmp, s);
+  if (e != cudaSuccess) return e;
+  subfill_kernel<<<nbb, 256, 0, s>>>(g.nbins, st.sub_count, st.sub_start, g.maxsub, st.sub_bin,
+                                     st.sub_off, st.n_sub);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <typename TC, typename TD>
+cudaError_t launch_deconv1(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                           const TC* const* phi, const void* fine, void* out, int ntr,
+                           cudaStream_t s) {
+  dim3 grid(grid1(N[0], 128), (unsigned)(N[1] < 65535 ? N[1] : 65535),
+            (unsigned)(N[2] * ntr < 65535 ? N[2] * ntr : 65535));
+  const TC* p1 = dim > 1 ? phi[1] : nullptr;
+  const TC* p2 = dim > 2 ? phi[2] : nullptr;
+  switch (dim) {
+    case 1:
+      deconv1_kernel<TC, TD, 1><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
+                                                     modeord, phi[0], p1, p2,
+                                                     (const cplx_t<TC>*)fine, (cplx_t<TD>*)out,
+                                                     ntr);
+      note_launch();
+      break;
+    case 2:
+      deconv1_kernel<TC, TD, 2><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
+                                                     modeord, phi[0], p1, p2,
+                                                     (const cplx_t<TC>*)fine, (cplx_t<TD>*)out,
+                                                     ntr);
+      note_launch();
+      break;
+    default:
+      deconv1_kernel<TC, TD, 3><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
+                                                     modeord, phi[0], p1, p2,
+                                                     (const cplx_t<TC>*)fine, (cplx_t<TD>*)out,
+                                                     ntr);
+      note_launch();
+      break;
+  }
+  return cudaGetLastError();
+}
+
+template <typename TC, typename TD>
+cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                           const TC* const* phi, const void* in, void* fine, int ntr,
+                           cudaStream_t s) {
+  dim3 grid(grid1(nf[0], 128), (unsigned)(nf[1] < 65535 ? nf[1] : 65535),
+            (unsigned)(nf[2] * ntr < 65535 ? nf[2] * ntr : 65535));
+  const TC* p1 = dim > 1 ? phi[1] : nullptr;
+  const TC* p2 = dim > 2 ? phi[2] : nullptr;
+  switch (dim) {
+    case 1:
+      deconv2_kernel<TC, TD, 1><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
+                                                     modeord, phi[0], p1, p2,
+                                                     (const cplx_t<TD>*)in, (cplx_t<TC>*)fine,
+                                                     ntr);
+      note_launch();
+      break;
+    case 2:
+      deconv2_kernel<TC, TD, 2><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
+                                                     modeord, phi[0], p1, p2,
+                                                     (const cplx_t<TD>*)in, (cplx_t<TC>*)fine,
+                                                     ntr);
+      note_launch();
+      break;
+    default:
+      deconv2_kernel<TC, TD, 3><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
+                                                     modeord, phi[0], p1, p2,
+                                                     (const cplx_t<TD>*)in, (cplx_t<TC>*)fine,
+                                                     ntr);
+      note_launch();
+      break;
+  }
+  return cudaGetLastError();
+}
+
+template <typename TX>
+cudaError_t launch_minmax(const TX* const* arrs, int narr, int64_t n, double* out,
+                          cudaStream_t s) {
+  // out doubles as key scratch: 2*narr unsigned long long then decoded in place
+  unsigned long long* keys = (unsigned long long*)out;
+  minmax_init_kernel<<<1, 32, 0, s>>>(keys, narr);
+  note_launch();
+  unsigned nb = grid1(n, 256);
+  if (nb > 4096) nb = 4096;
+  if (nb == 0) nb = 1;
+  for (int a = 0; a < narr; ++a)
+    if (n > 0) minmax_kernel<TX><<<nb, 256, 0, s>>>(arrs[a], n, keys + 2 * a);
+    note_launch();
+  minmax_decode_kernel<<<1, 64, 0, s>>>(keys, out, narr);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <typename TX>
+cudaError_t launch_t3_targets(int dim, int64_t N, const TX* const* s, const double* center,
+                              const double* scale, double* const* tau, cudaStream_t st) {
+  if (N == 0) return cudaSuccess;
+  Ptrs3 sp{};
+  DPtrs3 tp{};
+  double c[3] = {0, 0, 0}, sc[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) {
+    sp.p[d] = s[d];
+    tp.p[d] = tau[d];
+    c[d] = center[d];
+    sc[d] = scale[d];
+  }
+  t3_targets_kernel<TX><<<grid1(N, 256), 256, 0, st>>>(dim, N, sp, c[0], c[1], c[2], sc[0],
+                                                       sc[1], sc[2], tp);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <typename TX, typename TC>
+cudaError_t launch_t3_prephase_factors(int dim, int64_t M, const TX* const* x, const double* cx,
+                                       const double* cs, int iflag, void* fac, cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  Ptrs3 xp{};
+  double c[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d) {
+    xp.p[d] = x[d];
+    c[d] = cx[d];
+    t[d] = cs[d];
+  }
+  t3_pre_kernel<TX, TC><<<grid1(M, 256), 256, 0, s>>>(dim, M, xp, c[0], c[1], c[2], t[0], t[1],
+                                                      t[2], iflag, (cplx_t<TC>*)fac);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// Gauss-Legendre nodes on [-1, 1] (Newton iteration on P_q); host side.
+static void gauss_legendre(int q, double* x, double* wt) {
+  const double pi = 3.141592653589793238462643383279502884;
+  for (int i = 0; i < (q + 1) / 2; ++i) {
+    double z = cos(pi * (i + 0.75) / (q + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= q; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = q * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= q; ++k) {
+      double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = q * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = -z;
+    x[q - 1 - i] = z;
+    wt[i] = wt[q - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+template <typename TX, typename TC>
+cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
+                                   const double* const* tau, int iflag, int w, double beta,
+                                   void* fac, cudaStream_t s) {
+  if (N == 0) return cudaSuccess;
+  const double pi = 3.141592653589793238462643383279502884;
+  Quad qd;
+  qd.q = 2 * w + 10;
+  double xg[kMaxQuad], wg[kMaxQuad];
+  gauss_legendre(qd.q, xg, wg);
+  for (int i = 0; i < qd.q; ++i) {
+    const double th = (xg[i] + 1.0) * pi / 4.0;
+    const double wt = wg[i] * pi / 4.0;
+    qd.t[i] = 0.5 * w * sin(th);
+    qd.f[i] = 2.0 * wt * exp(beta * (cos(th) - 1.0)) * 0.5 * w * cos(th);
+  }
+  Ptrs3 sp{};
+  CDPtrs3 tp{};
+  double c[3] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d) {
+    sp.p[d] = sx[d];
+    tp.p[d] = tau[d];
+    c[d] = cx[d];
+  }
+  t3_post_kernel<TX, TC><<<grid1(N, 128), 128, 0, s>>>(dim, N, sp, c[0], c[1], c[2], tp, iflag,
+                                                       qd, (cplx_t<TC>*)fac);
+  note_launch();
+  return cudaGetLastError();
+}
+
+template <typename TI, typename TO, typename TF>
+cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, void* out,
+                        cudaStream_t s) {
+  if (n == 0 || ntr == 0) return cudaSuccess;
+  cmul_kernel<TI, TO, TF><<<grid1(n, 256), 256, 0, s>>>(n, ntr, (const cplx_t<TI>*)in,
+                                                        (const cplx_t<TF>*)fac,
+                                                        (cplx_t<TO>*)out);
+  note_launch();
+  return cudaGetLastError();
+}
+
+// explicit instantiations
+#define GBN_INST_FOLD(TX, TC)                                                                 \
+  template cudaError_t launch_fold<TX, TC>(const Geom&, const FoldSpec&, int64_t, const TX*, \
+                                           const TX*, const TX*, SortState&, cudaStream_t);
+GBN_INST_FOLD(float, float)
+GBN_INST_FOLD(double, float)
+GBN_INST_FOLD(double, double)
+template cudaError_t launch_sort_finish<float>(const Geom&, int64_t, SortState&, bool,
+                                               cudaStream_t);
+template cudaError_t launch_sort_finish<double>(const Geom&, int64_t, SortState&, bool,
+                                                cudaStream_t);
+#define GBN_INST_DECONV(TC, TD)                                                               \
+  template cudaError_t launch_deconv1<TC, TD>(int, const int64_t*, const int64_t*, int,       \
+                                              const TC* const*, const void*, void*, int,      \
+                                              cudaStream_t);                                  \
+  template cudaError_t launch_deconv2<TC, TD>(int, const int64_t*, const int64_t*, int,       \
+                                              const TC* const*, const void*, void*, int,      \
+                                              cudaStream_t);
+GBN_INST_DECONV(float, float)
+GBN_INST_DECONV(float, double)
+GBN_INST_DECONV(double, double)
+template cudaError_t launch_minmax<float>(const float* const*, int, int64_t, double*,
+                                          cudaStream_t);
+template cudaError_t launch_minmax<double>(const double* const*, int, int64_t, double*,
+                                           cudaStream_t);
+template cudaError_t launch_t3_targets<float>(int, int64_t, const float* const*, const double*,
+                                              const double*, double* const*, cudaStream_t);
+template cudaError_t launch_t3_targets<double>(int, int64_t, const double* const*,
+                                               const double*, const double*, double* const*,
+                                               cudaStream_t);
+#define GBN_INST_T3(TX, TC)                                                                    \
+  template cudaError_t launch_t3_prephase_factors<TX, TC>(int, int64_t, const TX* const*,      \
+                                                          const double*, const double*, int,   \
+                                                          void*, cudaStream_t);                \
+  template cudaError_t launch_t3_post_factors<TX, TC>(int, int64_t, const TX* const*,          \
+                                                      const double*, const double* const*,     \
+                                                      int, int, double, void*, cudaStream_t);
+GBN_INST_T3(float, float)
+GBN_INST_T3(double, float)
+GBN_INST_T3(double, double)
+#define GBN_INST_CMUL(TI, TO, TF)                                                             \
+  template cudaError_t launch_cmul<TI, TO, TF>(int64_t, int, const void*, const void*, void*, \
+                                               cudaStream_t);
+GBN_INST_CMUL(float, float, float)
+GBN_INST_CMUL(double, float, float)
+GBN_INST_CMUL(float, double, float)
+GBN_INST_CMUL(double, double, double)
+
+}  // namespace gbn

@@ -1,0 +1,439 @@
+/*
+ * nufft_oracle.c -- CPU restatement of the NUFFT algorithm that jax-finufft
+ * reaches through cuFINUFFT / FINUFFT 2.4.1.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library in
+ * jax-finufft_gb300/csrc: only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it.  The product path never calls into it.
+ *
+ * The reference repository vendors FINUFFT as an empty git submodule
+ * (.gitmodules:1-3, CMakeLists.txt:61), so the arithmetic below restates the
+ * published method instead of copying code:
+ *   - Barnett, Magland, af Klinteberg, "A parallel non-uniform fast Fourier
+ *     transform library based on an exponential of semicircle kernel",
+ *     SIAM J. Sci. Comput. 41 (2019): ES kernel, the width/beta rule, the
+ *     upsampled-grid size rule, deconvolution by the kernel's Fourier
+ *     transform, and the type-3 rescaling.
+ *   - Shih et al., "cuFINUFFT: a load-balanced GPU library for general-purpose
+ *     nonuniform FFTs", IPDPSW 2021: bin sorting of folded points.
+ * The call sites that pin the semantics are lib/kernels.cc.cu:25-92
+ * (run_nufft), src/jax_finufft/ops.py:159-170 (transform definitions) and
+ * src/jax_finufft/ops.py:114-123 (mode ordering).
+ *
+ * Everything is double precision.  The fold, bin, grid-start and offset
+ * arithmetic uses one rounding per operation in a fixed order (built with
+ * -ffp-contract=off) so that the CUDA kernels, which use __dmul_rn/__dadd_rn
+ * in the same order, produce bit-identical bin indices and offsets.
+ *
+ * Conventions (shared with the CUDA library):
+ *   - dimension 0 ("x") is the fastest-varying grid axis, as in the backend
+ *     order that lowering.py:96-105 produces by reversing the user's axes;
+ *   - fine grid index l corresponds to coordinate l * 2*pi / nf;
+ *   - kernel psi(t) = exp(beta*(sqrt(1-(2t/w)^2)-1)) for |t| <= w/2 in grid
+ *     units, zero outside;
+ *   - a point at grid coordinate X touches grid indices i0..i0+w-1 with
+ *     i0 = ceil(X - w/2); delta = i0 - (X - w/2) lies in [0, 1).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_MAX_W 16
+#define ORC_PI 3.141592653589793238462643383279502884
+#define ORC_INV2PI 0.159154943091895335768883763372514362
+
+/* ----------------------------------------------------------------------- */
+/* Plan-time parameters                                                     */
+/* ----------------------------------------------------------------------- */
+
+/* Smallest even n >= n0 with prime factors in {2, 3, 5}. */
+int64_t orc_next235even(int64_t n0) {
+  if (n0 <= 2) return 2;
+  int64_t n = (n0 % 2) ? n0 + 1 : n0;
+  for (;; n += 2) {
+    int64_t m = n;
+    while (m % 2 == 0) m /= 2;
+    while (m % 3 == 0) m /= 3;
+    while (m % 5 == 0) m /= 5;
+    if (m == 1) return n;
+  }
+}
+
+/* Kernel width and shape parameter for a requested tolerance.
+ * Width rule (published): sigma == 2 gives w = ceil(log10(10/eps)); other
+ * sigma gives w = ceil(-ln(eps) / (pi*sqrt(1-1/sigma))).  Shape: beta =
+ * 2.30*w at sigma == 2 (2.20, 2.26, 2.38 for w = 2, 3, 4), else
+ * beta = 0.97*pi*(1-1/(2*sigma))*w.
+ * Returns 1 when the width had to be clamped at ORC_MAX_W (tolerance not
+ * reachable, the reference's FINUFFT_WARN_EPS_TOO_SMALL), else 0. */
+int orc_kernel_params(double eps, double sigma, int *w_out, double *beta_out) {
+  int warn = 0;
+  double wd;
+  if (sigma == 2.0)
+    wd = ceil(-log10(eps / 10.0));
+  else
+    wd = ceil(-log(eps) / (ORC_PI * sqrt(1.0 - 1.0 / sigma)));
+  if (!(wd >= 2.0)) wd = 2.0;
+  if (wd > ORC_MAX_W) {
+    wd = ORC_MAX_W;
+    warn = 1;
+  }
+  int w = (int)wd;
+  double ratio;
+  if (sigma == 2.0) {
+    ratio = 2.30;
+    if (w == 2) ratio = 2.20;
+    if (w == 3) ratio = 2.26;
+    if (w == 4) ratio = 2.38;
+  } else {
+    ratio = 0.97 * ORC_PI * (1.0 - 1.0 / (2.0 * sigma));
+  }
+  *w_out = w;
+  *beta_out = ratio * (double)w;
+  return warn;
+}
+
+/* Fine-grid size for n modes: next235even(max(ceil(sigma*n), 2w)). */
+int64_t orc_fine_size(int64_t nmodes, double sigma, int w) {
+  double a = ceil(sigma * (double)nmodes);
+  int64_t n = (int64_t)a;
+  if (n < 2 * (int64_t)w) n = 2 * (int64_t)w;
+  return orc_next235even(n);
+}
+
+/* The ES kernel at offset t (grid units). */
+double orc_kernel(double t, int w, double beta) {
+  double z = 2.0 * t / (double)w;
+  double s = 1.0 - z * z;
+  if (s < 0.0) return 0.0;
+  return exp(beta * (sqrt(s) - 1.0));
+}
+
+/* Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_q. */
+static void orc_gauss_legendre(int q, double *x, double *wt) {
+  for (int i = 0; i < (q + 1) / 2; ++i) {
+    double z = cos(ORC_PI * (i + 0.75) / (q + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= q; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (q == 1) {
+        p1 = z;
+        p0 = 1.0;
+      }
+      dp = q * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    /* recompute derivative at the converged node */
+    {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= q; ++k) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = q * (z * p1 - p0) / (z * z - 1.0);
+    }
+    x[i] = -z;
+    x[q - 1 - i] = z;
+    wt[i] = wt[q - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+/* Fourier transform of the kernel, psihat(omega) = int psi(t) cos(omega t) dt,
+ * by Gauss-Legendre quadrature after the substitution t = (w/2) sin(theta),
+ * which removes the square-root endpoint singularity (q = 2w + 10 nodes on
+ * [0, pi/2]). */
+void orc_kernel_ft(int w, double beta, int64_t n, const double *omega, double *out) {
+  int q = 2 * w + 10;
+  double xg[64], wg[64], tq[64], fq[64];
+  orc_gauss_legendre(q, xg, wg);
+  for (int i = 0; i < q; ++i) {
+    double th = (xg[i] + 1.0) * ORC_PI / 4.0;
+    double wt = wg[i] * ORC_PI / 4.0;
+    tq[i] = 0.5 * w * sin(th);
+    fq[i] = 2.0 * wt * exp(beta * (cos(th) - 1.0)) * 0.5 * w * cos(th);
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < n; ++k) {
+    double s = 0.0;
+    for (int i = 0; i < q; ++i) s += fq[i] * cos(omega[k] * tq[i]);
+    out[k] = s;
+  }
+}
+
+/* ----------------------------------------------------------------------- */
+/* Fold, grid start, bins                                                   */
+/* ----------------------------------------------------------------------- */
+
+/* Periodic fold of x (radians) onto grid coordinate X in [0, nf).
+ * Non-finite inputs map to 0. */
+double orc_fold(double x, int64_t nf) {
+  if (!isfinite(x)) return 0.0;
+  double t = x * ORC_INV2PI;
+  double f = t - floor(t);
+  double X = f * (double)nf;
+  if (X >= (double)nf) X = X - (double)nf;
+  return X;
+}
+
+/* Type-3 rescale onto a non-periodic grid: X = (x - center) * inv + nf/2,
+ * kept inside [0, nf) by one wrap in either direction. */
+double orc_rescale(double x, double center, double inv, int64_t nf) {
+  if (!isfinite(x)) return 0.0;
+  double d = x - center;
+  double X = d * inv;
+  X = X + 0.5 * (double)nf;
+  if (X < 0.0) X = X + (double)nf;
+  if (X >= (double)nf) X = X - (double)nf;
+  return X;
+}
+
+/* Grid start i0 = ceil(X - w/2) and offset delta = i0 - (X - w/2). */
+static inline void orc_start(double X, int w, int64_t *i0, double *delta) {
+  double s = X - 0.5 * (double)w;
+  double c = ceil(s);
+  *i0 = (int64_t)c;
+  *delta = c - s;
+}
+
+/* Fold points (mode 0) or rescale them (mode 1, type 3) onto grid
+ * coordinates, and report per point the grid start, the offset and the bin
+ * index bin = floor(X_0)/B_0 + nb_0*(floor(X_1)/B_1 + nb_1*floor(X_2)/B_2).
+ * coords[d] may be NULL for d >= dim.  center/inv are read for mode 1 only. */
+void orc_fold_points(int dim, int mode, int w, const int64_t *nf, const int *binsize, int64_t M,
+                     const double *cx, const double *cy, const double *cz,
+                     const double *center, const double *inv, double *X, int64_t *i0,
+                     double *delta, int64_t *bin) {
+  const double *c[3] = {cx, cy, cz};
+  int64_t nb[3];
+  for (int d = 0; d < 3; ++d) nb[d] = (d < dim) ? (nf[d] + binsize[d] - 1) / binsize[d] : 1;
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < M; ++j) {
+    int64_t b = 0, stride = 1;
+    for (int d = 0; d < dim; ++d) {
+      double Xd = mode == 0 ? orc_fold(c[d][j], nf[d]) : orc_rescale(c[d][j], center[d], inv[d], nf[d]);
+      int64_t s;
+      double del;
+      orc_start(Xd, w, &s, &del);
+      X[j * 3 + d] = Xd;
+      i0[j * 3 + d] = s;
+      delta[j * 3 + d] = del;
+      int64_t fl = (int64_t)floor(Xd);
+      b += (fl / binsize[d]) * stride;
+      stride *= nb[d];
+    }
+    for (int d = dim; d < 3; ++d) {
+      X[j * 3 + d] = 0.0;
+      i0[j * 3 + d] = 0;
+      delta[j * 3 + d] = 0.0;
+    }
+    bin[j] = b;
+  }
+}
+
+/* ----------------------------------------------------------------------- */
+/* Spread (type 1) and interpolate (type 2)                                 */
+/* ----------------------------------------------------------------------- */
+
+static inline int64_t wrapi(int64_t i, int64_t n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+static void kernel_values(double delta, int w, double beta, double *k) {
+  for (int j = 0; j < w; ++j) k[j] = orc_kernel((double)j - 0.5 * w + delta, w, beta);
+}
+
+/* grid (complex interleaved, nf[0]*nf[1]*nf[2] cells, x fastest) +=
+ *   sum_j c_j psi(l - X_j) over the w^dim cells each point touches.
+ * Parallel over slabs of the slowest used axis; each thread owns a slab and
+ * clips every point's support to it, so the result is deterministic.
+ * X/i0/delta are the per-point outputs of orc_fold_points. */
+void orc_spread(int dim, const int64_t *nf, int w, double beta, int64_t M, const int64_t *i0,
+                const double *delta, const double *c, double *grid) {
+  int slow = dim - 1;
+  int64_t nslow = nf[slow];
+  int64_t plane = 1;
+  for (int d = 0; d < slow; ++d) plane *= nf[d];
+  int nthr = 1;
+#ifdef _OPENMP
+  nthr = omp_get_max_threads();
+#endif
+  int64_t nslab = nthr * 4;
+  if (nslab > nslow) nslab = nslow;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t sl = 0; sl < nslab; ++sl) {
+    int64_t lo = sl * nslow / nslab, hi = (sl + 1) * nslow / nslab;
+    double kv[3][ORC_MAX_W];
+    for (int64_t j = 0; j < M; ++j) {
+      int64_t s0 = i0[j * 3 + slow];
+      /* does [s0, s0+w) mod nslow meet [lo, hi)? */
+      int hit = 0;
+      for (int q = 0; q < w; ++q) {
+        int64_t g = wrapi(s0 + q, nslow);
+        if (g >= lo && g < hi) {
+          hit = 1;
+          break;
+        }
+      }
+      if (!hit) continue;
+      for (int d = 0; d < dim; ++d) kernel_values(delta[j * 3 + d], w, beta, kv[d]);
+      double cr = c[2 * j], ci = c[2 * j + 1];
+      for (int qs = 0; qs < w; ++qs) {
+        int64_t gs = wrapi(s0 + qs, nslow);
+        if (gs < lo || gs >= hi) continue;
+        double ks = kv[slow][qs];
+        if (dim == 1) {
+          grid[2 * gs] += cr * ks;
+          grid[2 * gs + 1] += ci * ks;
+        } else if (dim == 2) {
+          int64_t base = gs * plane;
+          for (int qx = 0; qx < w; ++qx) {
+            int64_t gx = wrapi(i0[j * 3 + 0] + qx, nf[0]);
+            double kk = ks * kv[0][qx];
+            grid[2 * (base + gx)] += cr * kk;
+            grid[2 * (base + gx) + 1] += ci * kk;
+          }
+        } else {
+          int64_t base = gs * plane;
+          for (int qy = 0; qy < w; ++qy) {
+            int64_t gy = wrapi(i0[j * 3 + 1] + qy, nf[1]);
+            double kyz = ks * kv[1][qy];
+            for (int qx = 0; qx < w; ++qx) {
+              int64_t gx = wrapi(i0[j * 3 + 0] + qx, nf[0]);
+              double kk = kyz * kv[0][qx];
+              int64_t idx = base + gy * nf[0] + gx;
+              grid[2 * idx] += cr * kk;
+              grid[2 * idx + 1] += ci * kk;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+/* c_j = sum over the w^dim touched cells of grid(l) psi(l - X_j). */
+void orc_interp(int dim, const int64_t *nf, int w, double beta, int64_t M, const int64_t *i0,
+                const double *delta, const double *grid, double *c) {
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < M; ++j) {
+    double kv[3][ORC_MAX_W];
+    for (int d = 0; d < 3; ++d)
+      for (int q = 0; q < ORC_MAX_W; ++q) kv[d][q] = (d == 0 || q == 0) ? 1.0 : 0.0;
+    for (int d = 0; d < dim; ++d) kernel_values(delta[j * 3 + d], w, beta, kv[d]);
+    int wy = dim >= 2 ? w : 1, wz = dim >= 3 ? w : 1;
+    double sr = 0.0, si = 0.0;
+    for (int qz = 0; qz < wz; ++qz) {
+      int64_t gz = dim >= 3 ? wrapi(i0[j * 3 + 2] + qz, nf[2]) : 0;
+      for (int qy = 0; qy < wy; ++qy) {
+        int64_t gy = dim >= 2 ? wrapi(i0[j * 3 + 1] + qy, nf[1]) : 0;
+        double kyz = (dim >= 3 ? kv[2][qz] : 1.0) * (dim >= 2 ? kv[1][qy] : 1.0);
+        int64_t base = (gz * nf[1] + gy) * nf[0];
+        double rr = 0.0, ri = 0.0;
+        for (int qx = 0; qx < w; ++qx) {
+          int64_t gx = wrapi(i0[j * 3 + 0] + qx, nf[0]);
+          rr += grid[2 * (base + gx)] * kv[0][qx];
+          ri += grid[2 * (base + gx) + 1] * kv[0][qx];
+        }
+        sr += rr * kyz;
+        si += ri * kyz;
+      }
+    }
+    c[2 * j] = sr;
+    c[2 * j + 1] = si;
+  }
+}
+
+/* Piecewise-polynomial fit of the kernel, the same scheme the CUDA library
+ * uses at plan time (Chebyshev interpolation of each unit piece at degree
+ * `deg`, converted to monomials in u = 2*delta - 1).  coef[j*(deg+1)+n] is
+ * the coefficient of u^n on piece j.  Exposed so the tests can check the fit
+ * error against the exact kernel. */
+void orc_horner_fit(int w, double beta, int deg, double *coef) {
+  int n1 = deg + 1;
+  double node[32], val[32], cheb[32], mono[32], tk[32][32];
+  for (int i = 0; i < n1; ++i) node[i] = cos(ORC_PI * (i + 0.5) / n1);
+  /* monomial coefficients of Chebyshev T_k: T_0 = 1, T_1 = u, T_k = 2u T_{k-1} - T_{k-2} */
+  memset(tk, 0, sizeof(tk));
+  tk[0][0] = 1.0;
+  if (n1 > 1) tk[1][1] = 1.0;
+  for (int k = 2; k < n1; ++k)
+    for (int n = 0; n < n1; ++n) tk[k][n] = (n ? 2.0 * tk[k - 1][n - 1] : 0.0) - tk[k - 2][n];
+  for (int j = 0; j < w; ++j) {
+    for (int i = 0; i < n1; ++i)
+      val[i] = orc_kernel((double)j - 0.5 * w + 0.5 * (node[i] + 1.0), w, beta);
+    for (int k = 0; k < n1; ++k) {
+      double s = 0.0;
+      for (int i = 0; i < n1; ++i) s += val[i] * cos(ORC_PI * k * (i + 0.5) / n1);
+      cheb[k] = s * (k == 0 ? 1.0 : 2.0) / n1;
+    }
+    for (int n = 0; n < n1; ++n) {
+      double s = 0.0;
+      for (int k = 0; k < n1; ++k) s += cheb[k] * tk[k][n];
+      mono[n] = s;
+    }
+    for (int n = 0; n < n1; ++n) coef[j * n1 + n] = mono[n];
+  }
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+/* Type-3 grid parameters for one dimension (published rescaling).
+ * Sources lie in [xmin, xmax], targets in [smin, smax].  With half-widths
+ * X = (xmax-xmin)/2, S = (smax-smin)/2 (each kept >= 1/other so X*S >= 1),
+ * the spreading grid has nf = next235even(max(floor(2*sigma*S*X/pi + w + 1),
+ * 2w)) cells; a source maps to grid coordinate (x - cx)*scale + nf/2 with
+ * scale = sigma*S/pi, and a target maps to the inner type-2 point
+ * (s - cs)/scale (radians, inside [-pi/sigma, pi/sigma]).
+ * out[0] = cx, out[1] = cs, out[2] = scale; returns nf. */
+int64_t orc_type3_params(double xmin, double xmax, double smin, double smax, double sigma, int w,
+                         double *out) {
+  double cx = 0.5 * (xmax + xmin), hx = 0.5 * (xmax - xmin);
+  double cs = 0.5 * (smax + smin), hs = 0.5 * (smax - smin);
+  double X = hx, S = hs;
+  if (X == 0.0) {
+    if (S == 0.0) {
+      X = 1.0;
+      S = 1.0;
+    } else if (X < 1.0 / S) {
+      X = 1.0 / S;
+    }
+  } else if (S < 1.0 / X) {
+    S = 1.0 / X;
+  }
+  double nfd = 2.0 * sigma * S * X / ORC_PI + (double)(w + 1);
+  if (!isfinite(nfd)) nfd = 0.0;
+  int64_t nf = (int64_t)nfd;
+  if (nf < 2 * (int64_t)w) nf = 2 * (int64_t)w;
+  nf = orc_next235even(nf);
+  out[0] = cx;
+  out[1] = cs;
+  out[2] = sigma * S / ORC_PI;
+  return nf;
+}

@@ -1,0 +1,196 @@
+"""Host-side logic on CPU: shape flattening, options, and the C ABI surface."""
+import ctypes
+import os
+import re
+
+import pytest
+import torch
+
+from jax_finufft_gb300 import options, shapes
+
+
+# --- shapes (port of the reference's tests/shapes_test.py) ------------------
+def test_broadcast_inputs():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        1, (10,), torch.empty((50, 5, 1, 7, 12, 5)), torch.empty((50, 1, 6, 1, 12, 5)))
+    assert source.shape == (50 * 6 * 12, 5 * 7, 5)
+    assert len(points) == 1
+    assert points[0].shape == (50 * 6 * 12, 5)
+    assert index.broadcast_from == (1, 3)
+    assert index.broadcast_to == (3, 4)
+    assert index.expected_output_shape == (50, 6, 12, 5, 7, 10)
+
+
+def test_broadcast_inputs_type2():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        2, None, torch.empty((50, 5, 1, 7, 12, 11)), torch.empty((50, 1, 6, 1, 12, 5)))
+    assert source.shape == (50 * 6 * 12, 5 * 7, 11)
+    assert points[0].shape == (50 * 6 * 12, 5)
+    assert index.broadcast_from == (1, 3)
+    assert index.broadcast_to == (3, 4)
+    assert index.expected_output_shape == (50, 6, 12, 5, 7, 5)
+
+
+def test_vector_inputs():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        2, None, torch.empty((5, 6)), torch.empty((10,)), torch.empty((10,)))
+    assert source.shape == (1, 1, 5, 6)
+    assert [p.shape for p in points] == [(1, 10), (1, 10)]
+    assert index.expected_output_shape == (10,)
+    assert index.broadcast_from == () and index.broadcast_to == ()
+
+
+def test_unpadded_points_type2():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        2, None, torch.empty((3, 8, 5, 6)), torch.empty((3, 10)), torch.empty((3, 10)))
+    assert source.shape == (3, 8, 5, 6)
+    assert [p.shape for p in points] == [(3, 10), (3, 10)]
+    assert index.expected_output_shape == (3, 8, 10)
+    assert index.broadcast_from == (1,) and index.broadcast_to == (1,)
+
+
+def test_unpadded_points_type1():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        1, (17, 13), torch.empty((3, 5, 6)), torch.empty((1, 6)), torch.empty((1, 6)))
+    assert source.shape == (1, 3 * 5, 6)
+    assert [p.shape for p in points] == [(1, 6), (1, 6)]
+    assert index.expected_output_shape == (3, 5, 17, 13)
+    assert index.broadcast_from == (0, 1) and index.broadcast_to == (0, 1)
+
+
+def test_unpadded_points_type3():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        3, None, torch.empty((3, 5, 6)), torch.empty((3, 6)), torch.empty((3, 6)),
+        torch.empty((3, 11)), torch.empty((3, 11)))
+    assert source.shape == (3, 5, 6)
+    assert [p.shape for p in points] == [(3, 6), (3, 6), (3, 11), (3, 11)]
+    assert index.expected_output_shape == (3, 5, 11)
+    assert index.broadcast_from == (1,) and index.broadcast_to == (1,)
+
+
+def test_type3():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        3, None, torch.empty((13, 3, 5, 7, 11)), torch.empty((13, 1, 5, 1, 11)),
+        torch.empty((1, 5, 1, 23)))
+    assert source.shape == (13 * 5, 3 * 7, 11)
+    assert [p.shape for p in points] == [(13 * 5, 11), (13 * 5, 23)]
+    assert index.expected_output_shape == (13, 5, 3, 7, 23)
+    assert index.broadcast_from == (1, 3) and index.broadcast_to == (2, 3)
+
+
+def test_type3_2d():
+    index, source, *points = shapes.broadcast_and_flatten_inputs(
+        3, None, torch.empty((13, 3, 5, 7, 11)), torch.empty((13, 1, 5, 1, 11)),
+        torch.empty((1, 5, 1, 11)), torch.empty((5, 1, 23)), torch.empty((1, 23)))
+    assert source.shape == (13 * 5, 3 * 7, 11)
+    assert [p.shape for p in points] == [(65, 11), (65, 11), (65, 23), (65, 23)]
+    assert index.expected_output_shape == (13, 5, 3, 7, 23)
+    assert index.broadcast_from == (1, 3) and index.broadcast_to == (2, 3)
+
+
+def test_unflatten_roundtrip():
+    idx, source, *pts = shapes.broadcast_and_flatten_inputs(
+        1, (4,), torch.arange(2 * 3 * 5, dtype=torch.float64).reshape(2, 3, 5),
+        torch.zeros(2, 1, 5))
+    res = torch.arange(source.shape[0] * source.shape[1] * 4, dtype=torch.float64).reshape(
+        source.shape[0], source.shape[1], 4)
+    out = idx.unflatten(res)
+    assert tuple(out.shape) == (2, 3, 4)
+
+
+# --- options (port of the reference's tests/options_test.py) ------------------
+@pytest.mark.parametrize("opts", [None, options.Opts()])
+def test_default_options(opts):
+    for t in (1, 2):
+        for fwd in (True, False):
+            assert options.unpack_opts(opts, t, fwd) == opts
+
+
+def test_nested_by_type():
+    opts = options.NestedOpts(type1=options.Opts(spread_debug=True),
+                              type2=options.Opts(debug=True))
+    assert options.unpack_opts(opts, 1, True) == options.Opts(spread_debug=True)
+    assert options.unpack_opts(opts, 2, True) == options.Opts(debug=True)
+
+
+def test_nested_by_direction():
+    opts = options.NestedOpts(forward=options.Opts(spread_debug=True),
+                              backward=options.Opts(debug=True))
+    assert options.unpack_opts(opts, 1, True) == options.Opts(spread_debug=True)
+    assert options.unpack_opts(opts, 1, False) == options.Opts(debug=True)
+
+
+def test_nested_multi():
+    opts = options.NestedOpts(
+        forward=options.Opts(spread_debug=True),
+        backward=options.NestedOpts(type1=options.Opts(spread_debug=True, debug=True),
+                                    type2=options.Opts(debug=True)))
+    assert options.unpack_opts(opts, 1, True) == options.Opts(spread_debug=True)
+    assert options.unpack_opts(opts, 1, False) == options.NestedOpts(
+        type1=options.Opts(spread_debug=True, debug=True), type2=options.Opts(debug=True))
+    assert options.unpack_opts(options.unpack_opts(opts, 1, False), 1, True) == options.Opts(
+        spread_debug=True, debug=True)
+    assert options.unpack_opts(options.unpack_opts(opts, 1, False), 2, True) == options.Opts(
+        debug=True)
+
+
+def test_opts_validation_and_native():
+    with pytest.raises(ValueError):
+        options.Opts(gpu_upsampfac=1.0)
+    with pytest.raises(ValueError):
+        options.Opts(gpu_precision=7)
+    n = options.to_native(options.Opts(modeord=True, gpu_method=2, gpu_binsizex=16,
+                                       gpu_upsampfac=1.25))
+    assert (n.modeord, n.gpu_method, n.gpu_binsizex, n.upsampfac) == (1, 2, 16, 1.25)
+    o = options.Opts().to_cufinufft_opts()
+    assert (o.upsampfac, o.gpu_method, o.gpu_sort, o.gpu_kerevalmeth) == (2.0, 0, 1, 1)
+    assert hash(options.Opts()) == hash(options.Opts())
+
+
+# --- the C ABI surface ----------------------------------------------------------
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "gbnufft.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"GBN_API\s+[\w\s\*]*?\b(gbnf?_\w+)\s*\(", text)))
+
+
+def test_header_declares_full_abi():
+    names = declared_symbols()
+    for t in (1, 2, 3):
+        for d in (1, 2, 3):
+            assert "gbn_nufft%dd%df" % (d, t) in names
+            assert "gbn_nufft%dd%d" % (d, t) in names
+    for n in ("gbn_makeplan", "gbnf_makeplan", "gbn_setpts", "gbnf_setpts", "gbn_execute",
+              "gbn_destroy", "gbn_run", "gbn_last_error", "gbn_default_opts"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(native):
+    from jax_finufft_gb300 import _native
+
+    for name in declared_symbols():
+        assert hasattr(native, name), name
+        assert name in _native.SIGNATURES, name
+
+
+def test_default_opts_and_struct_layout(native):
+    from jax_finufft_gb300 import _native
+
+    o = _native.default_opts()
+    assert (o.modeord, o.upsampfac, o.gpu_method, o.gpu_sort, o.gpu_kerevalmeth) == (
+        0, 2.0, 0, 1, 1)
+    assert o.gpu_maxsubprobsize == 1024 and o.gpu_precision == 0
+    assert ctypes.sizeof(_native.GbnOpts) == 56
+
+
+def test_cpu_tensors_are_rejected():
+    """No CPU fallback: the product path refuses host tensors."""
+    import jax_finufft_gb300 as jf
+
+    x = torch.zeros(10, dtype=torch.float64)
+    c = torch.zeros(10, dtype=torch.complex128)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        jf.nufft1(8, c, x)

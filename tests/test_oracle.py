@@ -1,0 +1,152 @@
+"""The CPU oracle pinned against the reference tests' known answers.
+
+The reference's tests (tests/ops_test.py) check every transform against a
+direct NUDFT sum; tests/golden holds those sums for the same seeds, sizes and
+parameter grids.  The oracle (CPU restatement of the fast algorithm) must meet
+the reference's own tolerances on them before it is trusted as the checker
+for the GPU path.
+"""
+from itertools import product
+
+import numpy as np
+import pytest
+
+from helpers import check_close, golden, rel_l2
+
+
+@pytest.fixture(scope="module")
+def cn(oracle_lib):
+    from oracle import cpu_nufft
+
+    return cpu_nufft
+
+
+FWD = list(product([1, 2, 3], [False, True], [-1, 1]))
+
+
+def _key(ndim, x64, iflag):
+    return "d%d_%s_i%+d" % (ndim, "x64" if x64 else "x32", iflag)
+
+
+@pytest.mark.parametrize("ndim, x64, iflag", FWD)
+def test_oracle_nufft1_golden(cn, ndim, x64, iflag):
+    g = golden("forward.npz")
+    k = "t1_" + _key(ndim, x64, iflag)
+    x, c, f = g[k + "_x"], g[k + "_c"], g[k + "_f"]
+    eps = 1e-10 if x64 else 1e-7
+    out = cn.nufft1(f.shape, c.astype(np.complex128), *x.astype(np.float64), eps=eps, iflag=iflag)
+    check_close(out.astype(c.dtype), f.astype(c.dtype))
+
+
+@pytest.mark.parametrize("ndim, x64, iflag", FWD)
+def test_oracle_nufft2_golden(cn, ndim, x64, iflag):
+    g = golden("forward.npz")
+    k = "t2_" + _key(ndim, x64, iflag)
+    x, f, c = g[k + "_x"], g[k + "_f"], g[k + "_c"]
+    eps = 1e-10 if x64 else 1e-7
+    out = cn.nufft2(f.astype(np.complex128), *x.astype(np.float64), eps=eps, iflag=iflag)
+    check_close(out.astype(f.dtype), c.astype(f.dtype))
+
+
+@pytest.mark.parametrize("ndim, x64, iflag", FWD)
+def test_oracle_nufft3_golden(cn, ndim, x64, iflag):
+    g = golden("forward.npz")
+    k = "t3_" + _key(ndim, x64, iflag)
+    x, s, c, f = g[k + "_x"], g[k + "_s"], g[k + "_c"], g[k + "_f"]
+    eps = 1e-10 if x64 else 1e-7
+    out = cn.nufft3(c.astype(np.complex128), *x.astype(np.float64), *s.astype(np.float64),
+                    eps=eps, iflag=iflag)
+    check_close(out.astype(c.dtype), f.astype(c.dtype),
+                rtol={"complex128": 1e-7, "complex64": 1e-3})
+
+
+@pytest.mark.parametrize("mo, nf, ndim, ty", list(product([0, 1], [16, 17], [1, 2, 3], [1, 2])))
+def test_oracle_modeord_golden(cn, mo, nf, ndim, ty):
+    g = golden("modeord.npz")
+    k = "mo%d_n%d_d%d_t%d" % (mo, nf, ndim, ty)
+    x = g[k + "_x"]
+    if ty == 1:
+        c, f = g[k + "_c"], g[k + "_f"]
+        out = cn.nufft1(f.shape, c, *x, eps=1e-10, iflag=1, modeord=mo)
+        check_close(out, f)
+    else:
+        f, c = g[k + "_f"], g[k + "_c"]
+        out = cn.nufft2(f, *x, eps=1e-10, iflag=1, modeord=mo)
+        check_close(out, c)
+
+
+def test_oracle_multi_golden(cn):
+    g = golden("multi.npz")
+    n_k = int(g["n_k"])
+    for i in range(g["x"].shape[0]):
+        check_close(cn.nufft1((n_k,), g["c"][i], g["x"][i], eps=1e-6, iflag=1), g["t1"][i],
+                    rtol=1e-4)
+        check_close(cn.nufft2(g["f"][i], g["x"][i], eps=1e-6, iflag=-1), g["t2"][i], rtol=1e-4)
+        check_close(cn.nufft3(g["c"][i], g["x"][i], g["xt"][i], eps=1e-6, iflag=-1), g["t3"][i],
+                    rtol=1e-4)
+
+
+@pytest.mark.parametrize("eps", [1e-3, 1e-6, 1e-9, 1e-12])
+@pytest.mark.parametrize("sigma", [2.0, 1.25])
+def test_oracle_error_tracks_eps(cn, eps, sigma):
+    """Relative l2 error vs the direct sum stays within a small multiple of eps."""
+    from oracle import direct
+
+    if cn.kernel_params(eps, sigma)[2]:
+        pytest.skip("tolerance below what width 16 reaches at this sigma (warning case)")
+    rng = np.random.default_rng(1)
+    x = [rng.uniform(-np.pi, np.pi, 400) for _ in range(2)]
+    c = rng.normal(size=400) + 1j * rng.normal(size=400)
+    out = cn.nufft1((24, 31), c, *x, eps=eps, iflag=1, sigma=sigma)
+    assert rel_l2(out, direct.type1(c, x, (24, 31), 1)) < 10 * eps
+
+
+def test_oracle_points_outside_period(cn):
+    """Points far outside [-pi, pi) fold periodically (ops_test.py:464 uses N(0,1))."""
+    from oracle import direct
+
+    rng = np.random.default_rng(2)
+    x = rng.normal(size=300) * 50.0
+    c = rng.normal(size=300) + 1j * rng.normal(size=300)
+    out = cn.nufft1((40,), c, x, eps=1e-9, iflag=-1)
+    assert rel_l2(out, direct.type1(c, [x], (40,), -1)) < 1e-8
+
+
+def test_horner_fit_accuracy(cn):
+    """The piecewise-polynomial fit (degree w+2) matches the kernel to ~e^-beta."""
+    for sigma in (2.0, 1.25):
+        for w in range(2, 17):
+            if sigma == 2.0:
+                beta = {2: 2.20, 3: 2.26, 4: 2.38}.get(w, 2.30) * w
+            else:
+                beta = 0.97 * np.pi * (1 - 1 / (2 * sigma)) * w
+            coef = cn.horner_fit(w, beta, w + 2)
+            d = np.linspace(0, 1, 257)[:-1]
+            u = 2 * d - 1
+            worst = 0.0
+            for j in range(w):
+                fit = np.polynomial.polynomial.polyval(u, coef[j])
+                exact = cn.kernel(j - w / 2 + d, w, beta)
+                worst = max(worst, np.max(np.abs(fit - exact)))
+            assert worst < max(np.exp(-beta), 1e-14) * 2.0, (sigma, w, worst)
+
+
+def test_kernel_params_rule(cn):
+    assert cn.kernel_params(1e-6, 2.0)[0] == 7
+    assert cn.kernel_params(1e-5, 2.0)[0] == 6
+    assert cn.kernel_params(1e-12, 2.0)[0] == 13
+    assert cn.kernel_params(1e-20, 2.0) [0] == 16 and cn.kernel_params(1e-20, 2.0)[2] == 1
+    assert cn.fine_size(256, 2.0, 7) == 512
+    assert cn.fine_size(75, 2.0, 8) == 150
+    assert cn.next235even(1001) == 1024 and cn.next235even(7) == 8 and cn.next235even(2) == 2
+
+
+def test_fold_edges(cn):
+    nf = 512
+    assert cn.lib().orc_fold(0.0, nf) == 0.0
+    assert cn.lib().orc_fold(np.pi, nf) == 256.0
+    assert 0.0 <= cn.lib().orc_fold(-np.pi, nf) < nf
+    assert cn.lib().orc_fold(float("nan"), nf) == 0.0
+    assert cn.lib().orc_fold(float("inf"), nf) == 0.0
+    assert 0.0 <= cn.lib().orc_fold(1e300, nf) < nf
+    assert 0.0 <= cn.lib().orc_fold(-1e-300, nf) < nf
