@@ -228,8 +228,8 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
 
-    pts_h, f_h = make_inputs()
-    M, N = M_POINTS, N_MODES
+    M, N = args.points, args.modes
+    pts_h, f_h = make_inputs(M=M, N=N)
     x = [torch.from_numpy(pts_h[d]).to(dev) for d in range(3)]
     f = torch.from_numpy(f_h).to(dev)
     c = torch.empty(M, dtype=torch.complex64, device=dev)
@@ -300,6 +300,56 @@ def run_ours(args):
     value = ws * 2 * M / (ms_step * 1e-3)
 
     # ---- e2e through the reference-facing C-ABI entry points, host buffers
+    e2e_value = e2e_ms = None
+    h2d = pts_h.nbytes + f_h.nbytes
+    d2h = N * N * N * 8
+    if not args.no_e2e:
+        e2e_value, e2e_ms = run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws,
+                                    barrier, max_over_ranks)
+    peak, peak_kind = measured_peak()
+    alg = algorithmic_bytes(M, nf_total)
+    spread_ms, interp_ms = t1[0], t2[0]
+    dom, dom_ms = ("spread", spread_ms) if spread_ms >= interp_ms else ("interp", interp_ms)
+    achieved = alg / (dom_ms * 1e-3) / 1e9
+    traffic = profile_traffic(dom)
+    workload = WORKLOAD if (M, N) == (M_POINTS, N_MODES) else (
+        "3D type-2 + type-1 round trip, complex64, M=%d points (half uniform, half N(0,0.1^2)), "
+        "%d^3 modes, eps=1e-5 (reduced case)" % (M, N))
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic",
+        "config": {"workload": workload, "M": M, "modes": [N, N, N], "eps": EPS,
+                   "kernel_width": w.value, "fine_grid": [nf3[0], nf3[1], nf3[2]],
+                   "l2": "inputs larger than L2 (fine grid %.2f GB, points %.0f MB)"
+                         % (nf_total * 8 / 1e9, M * 12 / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "path": "gbn_nufft3d2f + gbn_nufft3d1f (C ABI), pinned host buffers"},
+        "gpu_launches": int(launches),
+        "stages_ms": {"type2": {"setpts": t2[4], "deconv": t2[2], "fft": t2[1], "interp": t2[0]},
+                      "type1": {"setpts": t1[4], "spread": t1[0], "fft": t1[1],
+                                "deconv": t1[2]}},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes": alg, "traffic": traffic,
+                     "other": {"spread_GBs": alg / (spread_ms * 1e-3) / 1e9,
+                               "interp_GBs": alg / (interp_ms * 1e-3) / 1e9}},
+    }
+    lib.gbn_destroy(p1)
+    lib.gbn_destroy(p2)
+    return finish(args, result, rank, ws)
+
+
+def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, max_over_ranks):
+    """Same round trip through gbn_nufft3d2f/gbn_nufft3d1f with host buffers."""
+    import torch
+
+    from jax_finufft_gb300 import _native
+
+    M, N = args.points, args.modes
     pin_pts = torch.from_numpy(pts_h).pin_memory()
     pin_f = torch.from_numpy(f_h).pin_memory()
     pin_out = torch.empty((N, N, N), dtype=torch.complex64).pin_memory()
@@ -332,41 +382,11 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    e2e_value = ws * 2 * M / (e2e_ms * 1e-3)
-    h2d = pts_h.nbytes + f_h.nbytes
-    d2h = N * N * N * 8
+    return ws * 2 * M / (e2e_ms * 1e-3), e2e_ms
 
-    # ---- roofline of the dominant point kernel (spread vs interp)
-    peak, peak_kind = measured_peak()
-    alg = algorithmic_bytes(M, nf_total)
-    spread_ms, interp_ms = t1[0], t2[0]
-    dom, dom_ms = ("spread", spread_ms) if spread_ms >= interp_ms else ("interp", interp_ms)
-    achieved = alg / (dom_ms * 1e-3) / 1e9
-    traffic = profile_traffic(dom)
-    result = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "M": M, "modes": [N, N, N], "eps": EPS,
-                   "kernel_width": w.value, "fine_grid": [nf3[0], nf3[1], nf3[2]],
-                   "l2": "inputs larger than L2 (fine grid 1.07 GB, points 120 MB)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "clocks": clk,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "path": "gbn_nufft3d2f + gbn_nufft3d1f (C ABI), pinned host buffers"},
-        "gpu_launches": int(launches),
-        "stages_ms": {"type2": {"setpts": t2[4], "deconv": t2[2], "fft": t2[1], "interp": t2[0]},
-                      "type1": {"setpts": t1[4], "spread": t1[0], "fft": t1[1],
-                                "deconv": t1[2]}},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "algorithmic_bytes": alg, "traffic": traffic,
-                     "other": {"spread_GBs": alg / (spread_ms * 1e-3) / 1e9,
-                               "interp_GBs": alg / (interp_ms * 1e-3) / 1e9}},
-    }
-    lib.gbn_destroy(p1)
-    lib.gbn_destroy(p2)
+
+def finish(args, result, rank, ws):
+    import torch
 
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import cpu_nufft
@@ -392,6 +412,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e leg")
+    ap.add_argument("--points", type=int, default=M_POINTS,
+                    help="points per transform (reduced cases for profiling)")
+    ap.add_argument("--modes", type=int, default=N_MODES, help="modes per axis")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -81,8 +81,12 @@ int64_t next235even(int64_t n0) {
 // the width is clamped at kMaxW.
 int kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
   int warn = 0;
-  double wd = (sigma == 2.0) ? std::ceil(-std::log10(eps / 10.0))
-                             : std::ceil(-std::log(eps) / (kPi * std::sqrt(1.0 - 1.0 / sigma)));
+  double a = (sigma == 2.0) ? -std::log10(eps / 10.0)
+                            : -std::log(eps) / (kPi * std::sqrt(1.0 - 1.0 / sigma));
+  // a tolerance given in single precision (1e-5f = 9.99999975e-6) must not
+  // gain a kernel width from its rounding: snap to the integer within 1e-5
+  if (std::fabs(a - std::round(a)) < 1e-5) a = std::round(a);
+  double wd = std::ceil(a);
   if (!(wd >= 2.0)) wd = 2.0;
   if (wd > kMaxW) {
     wd = kMaxW;

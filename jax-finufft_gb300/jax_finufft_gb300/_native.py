@@ -51,8 +51,10 @@ _i64 = ctypes.c_int64
 _i64p = ctypes.POINTER(ctypes.c_int64)
 
 # Every symbol include/gbnufft.h declares, with its argument types.
-_ONESHOT_F = [_vp, ctypes.c_float] + [_i64] * 9 + [ctypes.c_double] + [_i64] * 5
-_ONESHOT_D = [_vp, ctypes.c_double] + [_i64] * 9 + [ctypes.c_double] + [_i64] * 5
+# stream, eps, then iflag n_tot n_transf n_j n_k_1 n_k_2 n_k_3 modeord, upsampfac,
+# then gpu_method gpu_sort gpu_kerevalmeth gpu_maxbatchsize debug
+_ONESHOT_F = [_vp, ctypes.c_float] + [_i64] * 8 + [ctypes.c_double] + [_i64] * 5
+_ONESHOT_D = [_vp, ctypes.c_double] + [_i64] * 8 + [ctypes.c_double] + [_i64] * 5
 SIGNATURES = {
     "gbn_default_opts": (None, [ctypes.POINTER(GbnOpts)]),
     "gbn_makeplan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_int,

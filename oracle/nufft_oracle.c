@@ -72,11 +72,15 @@ int64_t orc_next235even(int64_t n0) {
  * reachable, the reference's FINUFFT_WARN_EPS_TOO_SMALL), else 0. */
 int orc_kernel_params(double eps, double sigma, int *w_out, double *beta_out) {
   int warn = 0;
-  double wd;
+  double a;
   if (sigma == 2.0)
-    wd = ceil(-log10(eps / 10.0));
+    a = -log10(eps / 10.0);
   else
-    wd = ceil(-log(eps) / (ORC_PI * sqrt(1.0 - 1.0 / sigma)));
+    a = -log(eps) / (ORC_PI * sqrt(1.0 - 1.0 / sigma));
+  /* a tolerance given in single precision must not gain a width from its
+   * rounding: snap to the integer within 1e-5 */
+  if (fabs(a - round(a)) < 1e-5) a = round(a);
+  double wd = ceil(a);
   if (!(wd >= 2.0)) wd = 2.0;
   if (wd > ORC_MAX_W) {
     wd = ORC_MAX_W;

@@ -2,8 +2,8 @@
 import numpy as np
 
 # tests/ops_test.py:14-16 -- rtol per output dtype; atol from jax's defaults
-RTOL = {"complex128": 1e-7, "complex64": 1e-4}
-ATOL = {"complex128": 1e-15, "complex64": 1e-6}
+RTOL = {"complex128": 1e-7, "complex64": 1e-4, "float64": 1e-7, "float32": 1e-4}
+ATOL = {"complex128": 1e-15, "complex64": 1e-6, "float64": 1e-15, "float32": 1e-6}
 
 
 def check_close(actual, expected, rtol=None, dtype=None, floor=True):

@@ -40,9 +40,11 @@ GRAD = list(product([1, 2, 3], [-1, 1]))
 
 def _gradcheck(fn, args):
     args = tuple(a.detach().requires_grad_(True) for a in args)
+    # spreading accumulates with atomics, so repeated backward passes differ
+    # in the last bits: allow that nondeterminism, as for any atomic kernel
     assert torch.autograd.gradcheck(fn, args, eps=1e-6, atol=1e-5, rtol=1e-4,
-                                    check_forward_ad=True, check_batched_grad=False,
-                                    fast_mode=True)
+                                    nondet_tol=1e-9, check_forward_ad=True,
+                                    check_batched_grad=False, fast_mode=True)
 
 
 @pytest.mark.parametrize("ndim, iflag", GRAD)

@@ -194,3 +194,33 @@ def test_cpu_tensors_are_rejected():
     c = torch.zeros(10, dtype=torch.complex128)
     with pytest.raises(RuntimeError, match="CUDA"):
         jf.nufft1(8, c, x)
+
+
+def _declared_arity():
+    """Number of parameters of every GBN_API function, macros expanded."""
+    text = open(HEADER).read()
+    macros = {}
+    for m in re.finditer(r"#define (GBN_ONESHOT_ARGS_[FD])((?:.*\\\n)*.*)", text):
+        body = m.group(2).replace("\\\n", " ")
+        macros[m.group(1)] = body.count(",") + 1
+    out = {}
+    for m in re.finditer(r"GBN_API\s+[\w\s\*]*?\b(gbnf?_\w+)\s*\(([^;]*?)\)\s*;", text, re.S):
+        args = m.group(2).strip()
+        if args in ("void", ""):
+            out[m.group(1)] = 0
+            continue
+        n = 0
+        for a in args.split(","):
+            a = a.strip()
+            n += macros.get(a, 1)
+        out[m.group(1)] = n
+    return out
+
+
+def test_ctypes_arity_matches_header():
+    from jax_finufft_gb300 import _native
+
+    arity = _declared_arity()
+    assert len(arity) == len(declared_symbols())
+    for name, n in arity.items():
+        assert len(_native.SIGNATURES[name][1]) == n, (name, n, len(_native.SIGNATURES[name][1]))
