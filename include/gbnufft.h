@@ -201,6 +201,33 @@ GBN_API int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x
                  void* output);
 
 /*
+ * Bin-sort nonuniform points without allocating any memory.  No counterpart
+ * in the reference: it serves callers that cannot call cudaMalloc (plugins
+ * whose host framework owns all device memory, pipelines that reserve every
+ * byte up front, hooks that must not allocate).  It runs the FP64 fold and
+ * bin sort of setpts on caller-provided points (float32 when single = 1,
+ * else float64; device pointers, backend order) for a fine grid of nf[d]
+ * cells in bins of binsize[d] cells per axis, and writes to caller-owned
+ * device arrays: bins[M] (bin of each point, same numbering as setpts),
+ * counts[nbins] (points per bin, nbins = prod ceil(nf/binsize)) and perm[M]
+ * (input index of each point in bin order).
+ * Its scratch (per-point ranks and folded records, scan partial sums) is one
+ * fixed device array of GBN_NOALLOC_SCRATCH_BYTES inside the library, held
+ * by every GPU that loads the library until the process exits; M above
+ * GBN_NOALLOC_MAX_POINTS or more than GBN_NOALLOC_MAX_BINS bins is rejected
+ * with GBN_ERR_ARGS.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU race.  Enqueued on `stream`; no host sync.
+ */
+#define GBN_NOALLOC_MAX_POINTS 262144
+#define GBN_NOALLOC_MAX_BINS 262144
+#define GBN_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+GBN_API int gbn_binsort_noalloc(void* stream, int dim, int single, int64_t M, const void* x,
+                                const void* y, const void* z, const int64_t* nf,
+                                const int* binsize, int* bins, int* counts, int* perm);
+
+/*
  * Generic one-shot call with full options (bin sizes, precision): the torch
  * binding uses this.  single = 1 for complex64/float32 data.  pts/tgts hold
  * dim device pointers each (tgts only for type 3).  n_k in backend order

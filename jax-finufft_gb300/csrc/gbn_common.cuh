@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 namespace gbn {
 
@@ -91,6 +92,10 @@ struct SortState {
 // Count of kernels this library has launched (process-wide, all threads);
 // every launcher adds the launches it makes.  Read through gbn_launch_count().
 void note_launch(int n = 1);
+
+// Record msg as the calling thread's last error (read by gbn_last_error())
+// and return code.
+int set_error(int code, const std::string& msg);
 
 // ---------------------------------------------------------------------------
 // Launchers (defined in the .cu files, called by the host plan code).

@@ -1314,3 +1314,5 @@ int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const 
                  void* output)
     GBN_ONESHOT_BODY(3, 3, 0, double, x, y, z, s, t, u)
 }  // extern "C"
+
+int gbn::set_error(int code, const std::string& msg) { return fail(code, msg); }
