@@ -207,7 +207,9 @@ GBN_API int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x
  * byte up front, hooks that must not allocate).  It runs the FP64 fold and
  * bin sort of setpts on caller-provided points (float32 when single = 1,
  * else float64; device pointers, backend order) for a fine grid of nf[d]
- * cells in bins of binsize[d] cells per axis, and writes to caller-owned
+ * cells in bins of binsize[d] cells per axis and kernel width w (2..16; a
+ * point belongs to the bin holding the first cell of its w-wide support, as
+ * in setpts; gbn_plan_info reports a plan's w), and writes to caller-owned
  * device arrays: bins[M] (bin of each point, same numbering as setpts),
  * counts[nbins] (points per bin, nbins = prod ceil(nf/binsize)) and perm[M]
  * (input index of each point in bin order).
@@ -225,7 +227,7 @@ GBN_API int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x
 #define GBN_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 GBN_API int gbn_binsort_noalloc(void* stream, int dim, int single, int64_t M, const void* x,
                                 const void* y, const void* z, const int64_t* nf,
-                                const int* binsize, int* bins, int* counts, int* perm);
+                                const int* binsize, int w, int* bins, int* counts, int* perm);
 
 /*
  * Generic one-shot call with full options (bin sizes, precision): the torch

@@ -108,7 +108,7 @@ cudaError_t binsort(const Geom& g, int64_t M, const TX* x, const TX* y, const TX
 
 extern "C" int gbn_binsort_noalloc(void* stream, int dim, int single, int64_t M, const void* x,
                                    const void* y, const void* z, const int64_t* nf,
-                                   const int* binsize, int* bins, int* counts, int* perm) {
+                                   const int* binsize, int w, int* bins, int* counts, int* perm) {
   using namespace gbn;
   if (dim < 1 || dim > 3) return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: dim must be 1..3");
   if (!nf || !binsize) return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: NULL nf or binsize");
@@ -116,9 +116,11 @@ extern "C" int gbn_binsort_noalloc(void* stream, int dim, int single, int64_t M,
     return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: M = " + std::to_string(M) +
                                        " exceeds the limit of " + std::to_string(kMaxPoints) +
                                        " points (GBN_NOALLOC_MAX_POINTS)");
+  if (w < 2 || w > kMaxW)
+    return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: kernel width w must be 2..16");
   Geom g{};
   g.dim = dim;
-  g.w = 2;
+  g.w = w;
   g.nbins = 1;
   g.maxsub = 1;
   for (int d = 0; d < 3; ++d) {
@@ -126,8 +128,8 @@ extern "C" int gbn_binsort_noalloc(void* stream, int dim, int single, int64_t M,
     g.bs[d] = 1;
     g.nb[d] = 1;
     if (d < dim) {
-      if (nf[d] < 4 || nf[d] > (int64_t)INT32_MAX || binsize[d] < 1)
-        return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: need 4 <= nf < 2^31 and binsize >= 1");
+      if (nf[d] < 2 * w || nf[d] > (int64_t)INT32_MAX || binsize[d] < 1)
+        return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: need 2w <= nf < 2^31 and binsize >= 1");
       g.nf[d] = nf[d];
       g.bs[d] = binsize[d];
       g.nb[d] = (int)((nf[d] + binsize[d] - 1) / binsize[d]);

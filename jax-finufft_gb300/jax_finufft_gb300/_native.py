@@ -78,7 +78,8 @@ SIGNATURES = {
     "gbn_clear_cache": (None, []),
     "gbn_launch_count": (ctypes.c_longlong, []),
     "gbn_binsort_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,
-                                           _i64p, ctypes.POINTER(ctypes.c_int), _vp, _vp, _vp]),
+                                           _i64p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                           _vp, _vp, _vp]),
     "gbn_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double,
                                ctypes.c_int, _i64, _i64, _i64, _i64p, ctypes.POINTER(GbnOpts),
                                _vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]),

@@ -37,7 +37,8 @@ def _existing_bins(lib, native, dim, single, pts, nmodes, binsize):
         setpts = lib.gbnf_setpts if single else lib.gbn_setpts
         native.check(setpts(plan, pts[0].numel(), ptr[0], ptr[1], ptr[2], 0, None, None, None))
         nf = (ctypes.c_int64 * 3)()
-        native.check(lib.gbn_plan_info(plan, None, nf, None, None))
+        w = ctypes.c_int()
+        native.check(lib.gbn_plan_info(plan, ctypes.byref(w), nf, None, None))
         nbins = ctypes.c_int64()
         lib.gbn_debug_bins(plan, None, None, ctypes.byref(nbins))
         bins = np.empty(pts[0].numel(), dtype=np.int64)
@@ -46,10 +47,10 @@ def _existing_bins(lib, native, dim, single, pts, nmodes, binsize):
                                         counts.ctypes.data_as(I64P), ctypes.byref(nbins)))
     finally:
         lib.gbn_destroy(plan)
-    return [nf[d] for d in range(3)], bins, counts
+    return [nf[d] for d in range(3)], w.value, bins, counts
 
 
-def _noalloc(lib, native, dim, single, pts, nf, binsize, nbins):
+def _noalloc(lib, native, dim, single, pts, nf, binsize, w, nbins):
     M = pts[0].numel()
     dev = pts[0].device
     bins = torch.empty(M, dtype=torch.int32, device=dev)
@@ -60,7 +61,7 @@ def _noalloc(lib, native, dim, single, pts, nf, binsize, nbins):
     bsa = (ctypes.c_int * 3)(*binsize)
     stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     native.check(lib.gbn_binsort_noalloc(stream, dim, int(single), M, ptr[0], ptr[1], ptr[2],
-                                         nfa, bsa, ctypes.c_void_p(bins.data_ptr()),
+                                         nfa, bsa, w, ctypes.c_void_p(bins.data_ptr()),
                                          ctypes.c_void_p(counts.data_ptr()),
                                          ctypes.c_void_p(perm.data_ptr())))
     torch.cuda.synchronize()
@@ -83,9 +84,11 @@ def test_noalloc_binsort_matches_setpts(dim, single):
         for _ in range(dim):
             v = np.concatenate([rng.uniform(-np.pi, np.pi, half), rng.normal(0, 0.2, M - half)])
             pts.append(torch.tensor(v, dtype=dt, device="cuda"))
-        nf, ref_bins, ref_counts = _existing_bins(lib, _native, dim, single, pts, nmodes, binsize)
+        nf, w, ref_bins, ref_counts = _existing_bins(lib, _native, dim, single, pts, nmodes,
+                                                     binsize)
         bs = [min(binsize[d], nf[d]) if d < dim else 1 for d in range(3)]
-        bins, counts, perm = _noalloc(lib, _native, dim, single, pts, nf, bs, ref_counts.size)
+        bins, counts, perm = _noalloc(lib, _native, dim, single, pts, nf, bs, w,
+                                      ref_counts.size)
         np.testing.assert_array_equal(bins.astype(np.int64), ref_bins)
         np.testing.assert_array_equal(counts.astype(np.int64), ref_counts)
         assert np.array_equal(np.sort(perm), np.arange(M))
@@ -99,11 +102,11 @@ def test_noalloc_rejects_oversize():
     M = 262144 + 1  # GBN_NOALLOC_MAX_POINTS + 1
     nf = (ctypes.c_int64 * 3)(64, 1, 1)
     bs = (ctypes.c_int * 3)(8, 1, 1)
-    rc = lib.gbn_binsort_noalloc(None, 1, 1, M, None, None, None, nf, bs, None, None, None)
+    rc = lib.gbn_binsort_noalloc(None, 1, 1, M, None, None, None, nf, bs, 7, None, None, None)
     assert rc == 2
     assert "exceeds the limit" in _native.last_error()
     nf = (ctypes.c_int64 * 3)(1 << 20, 1024, 1)
     bs = (ctypes.c_int * 3)(1, 1, 1)
-    rc = lib.gbn_binsort_noalloc(None, 2, 1, 10, None, None, None, nf, bs, None, None, None)
+    rc = lib.gbn_binsort_noalloc(None, 2, 1, 10, None, None, None, nf, bs, 7, None, None, None)
     assert rc == 2
     assert "bins exceed" in _native.last_error()
