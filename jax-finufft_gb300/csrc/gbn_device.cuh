@@ -53,6 +53,67 @@ __device__ __forceinline__ int64_t wrap_idx(int64_t i, int64_t n) {
   while (i >= n) i -= n;
   return i;
 }
+__device__ __forceinline__ int wrap_i32(int i, int n) {
+  if (i < 0) i += n;
+  if (i >= n) i -= n;
+  if (i >= n) i -= n;
+  return i;
+}
+
+// Bin tile of a subproblem: origin (first grid index, may be negative) and
+// extent bs + w - 1 per axis; points of the bin start at tile offsets
+// [0, bs) (the bin rule of the fold kernel), so their supports fit.
+template <int DIM>
+struct Tile {
+  int org[3];
+  int T[3];
+  int ncell;
+  __device__ __forceinline__ Tile(const Geom& g, int bin) {
+    int rem = bin;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      org[d] = 0;
+      T[d] = 1;
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const int b = rem % g.nb[d];
+      rem /= g.nb[d];
+      org[d] = b * g.bs[d] - (g.w >> 1);
+      T[d] = g.bs[d] + g.w - 1;
+    }
+    ncell = T[0] * T[1] * T[2];
+  }
+};
+
+// Walks the cells tid, tid + step, ... of a T0 x T1 x T2 tile keeping the
+// coordinates (c0, c1, c2) with additions instead of a division per cell.
+struct CellWalk {
+  int c0, c1, c2, d0, d1, d2, T0, T1;
+  __device__ __forceinline__ CellWalk(int start, int step, int T0_, int T1_) : T0(T0_), T1(T1_) {
+    c0 = start % T0;
+    const int r = start / T0;
+    c1 = r % T1;
+    c2 = r / T1;
+    d0 = step % T0;
+    const int rs = step / T0;
+    d1 = rs % T1;
+    d2 = rs / T1;
+  }
+  __device__ __forceinline__ void next() {
+    c0 += d0;
+    if (c0 >= T0) {
+      c0 -= T0;
+      ++c1;
+    }
+    c1 += d1;
+    if (c1 >= T1) {
+      c1 -= T1;
+      ++c2;
+    }
+    c2 += d2;
+  }
+};
 
 __device__ __forceinline__ void atomic_add_c(float2* p, float a, float b) {
   atomicAdd(p, make_float2(a, b));

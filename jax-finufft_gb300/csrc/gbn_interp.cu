@@ -67,32 +67,24 @@ __global__ void __launch_bounds__(kThreads)
   int start, cnt, bin;
   if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
   const int t = blockIdx.y;
-  const int w = g.w, h = w >> 1;
-  int org[3] = {0, 0, 0}, T[3] = {1, 1, 1};
-  {
-    int rem = bin;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      const int b = rem % g.nb[d];
-      rem /= g.nb[d];
-      org[d] = b * g.bs[d] - h;
-      T[d] = g.bs[d] + w;
-    }
-  }
-  const int ncell = T[0] * T[1] * T[2];
+  const int w = g.w;
+  const Tile<DIM> tl(g, bin);
+  const int ncell = tl.ncell;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
   const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
-  for (int i = threadIdx.x; i < ncell; i += kThreads) {
-    const int c0 = i % T[0];
-    const int r1 = i / T[0];
-    const int c1 = r1 % T[1];
-    const int c2 = r1 / T[1];
-    const int64_t g0 = wrap_idx(org[0] + c0, g.nf[0]);
-    const int64_t g1 = DIM > 1 ? wrap_idx(org[1] + c1, g.nf[1]) : 0;
-    const int64_t g2 = DIM > 2 ? wrap_idx(org[2] + c2, g.nf[2]) : 0;
-    tile[i] = ft[(g2 * g.nf[1] + g1) * g.nf[0] + g0];
+  {
+    const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
+    CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
+    for (int i = threadIdx.x; i < ncell; i += kThreads, cw.next()) {
+      const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
+      const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
+      const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
+      tile[i] = ft[(g2 * nf1 + g1) * nf0 + g0];
+    }
   }
+  const int org[3] = {tl.org[0], tl.org[1], tl.org[2]};
+  const int T[3] = {tl.T[0], tl.T[1], tl.T[2]};
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
   TC co[NCO];
   load_coef<TC, NCO>(co, ks, gl, w);
@@ -179,13 +171,14 @@ __global__ void __launch_bounds__(kThreads)
   const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
   cplx_t<TD>* ct = c + (int64_t)t * M;
   const bool lane_on = gl < w;
+  const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
     const bool valid = pi < cnt;
     const int js = start + (valid ? pi : 0);
     const PtRec<TC, DIM> r = recs[js];
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
-    const int64_t gx = wrap_idx((int64_t)r.i[0] + gl, g.nf[0]);
+    const int gx = wrap_i32(r.i[0] + gl, nf0);
     TC ar = TC(0), ai = TC(0);
     if (DIM == 1) {
       if (lane_on) {
@@ -197,9 +190,9 @@ __global__ void __launch_bounds__(kThreads)
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       for (int iy = 0; iy < w; ++iy) {
         const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-        const int64_t gy = wrap_idx((int64_t)r.i[1] + iy, g.nf[1]);
+        const int gy = wrap_i32(r.i[1] + iy, nf1);
         if (lane_on) {
-          const cplx_t<TC> v = ft[gy * g.nf[0] + gx];
+          const cplx_t<TC> v = ft[gy * nf0 + gx];
           ar = fma(v.x, kyv, ar);
           ai = fma(v.y, kyv, ai);
         }
@@ -209,13 +202,13 @@ __global__ void __launch_bounds__(kThreads)
       const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
       for (int iz = 0; iz < w; ++iz) {
         const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
-        const int64_t gz = wrap_idx((int64_t)r.i[2] + iz, g.nf[2]);
+        const int gz = wrap_i32(r.i[2] + iz, nf2);
         TC yr = TC(0), yi = TC(0);
         for (int iy = 0; iy < w; ++iy) {
           const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-          const int64_t gy = wrap_idx((int64_t)r.i[1] + iy, g.nf[1]);
+          const int gy = wrap_i32(r.i[1] + iy, nf1);
           if (lane_on) {
-            const cplx_t<TC> v = ft[(gz * g.nf[1] + gy) * g.nf[0] + gx];
+            const cplx_t<TC> v = ft[(gz * nf1 + gy) * nf0 + gx];
             yr = fma(v.x, kyv, yr);
             yi = fma(v.y, kyv, yi);
           }
@@ -260,7 +253,7 @@ cudaError_t run_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     cplx_t<TD>* ct = (cplx_t<TD>*)c + (int64_t)t0 * M;
     if (method == 2 && sa.sorted) {
       int64_t ncell = 1;
-      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w;
+      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w - 1;
       const size_t smem = (size_t)ncell * sizeof(cplx_t<TC>);
       auto kern = interp_sm_kernel<TC, TD, DIM, G>;
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

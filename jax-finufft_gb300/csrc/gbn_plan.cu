@@ -361,7 +361,7 @@ void default_bins(int dim, bool single, int* bs) {
 
 size_t tile_bytes(int dim, const int* bs, int w, bool single) {
   size_t n = 1;
-  for (int d = 0; d < dim; ++d) n *= (size_t)(bs[d] + w);
+  for (int d = 0; d < dim; ++d) n *= (size_t)(bs[d] + w - 1);
   return n * 2 * (single ? 4 : 8);
 }
 

@@ -17,28 +17,30 @@ namespace {
 
 constexpr double kInv2Pi = 0.159154943091895335768883763372514362;
 
-// Periodic fold onto [0, nf) with one rounding per operation (bit-identical
-// to the CPU restatement, which is compiled with -ffp-contract=off).
-__device__ __forceinline__ double fold_rn(double x, int64_t nf) {
-  if (!isfinite(x)) return 0.0;
-  double t = __dmul_rn(x, kInv2Pi);
-  double f = __dsub_rn(t, floor(t));
-  double X = __dmul_rn(f, (double)nf);
-  if (X >= (double)nf) X = __dsub_rn(X, (double)nf);
-  return X;
+// Grid coordinate of a point minus w/2, i.e. s = X - w/2 with X the point's
+// position in fine-grid cells.  Periodic fold (mode 0): t = x/(2 pi),
+// f = t - floor(t) in [0, 1), s = fma(f, nf, -w/2).  Type-3 rescale (mode 1):
+// s = fma(x - center, scale, nf/2 - w/2).  FP64 with one rounding per
+// operation, the order the CPU restatement uses (bit-identical results).
+// Non-finite coordinates are treated as 0 (mode 0) or as the centre (mode 1).
+__device__ __forceinline__ double grid_shift(double x, int mode, double center, double scale,
+                                             int64_t nf, int w) {
+  const double hw = 0.5 * (double)w;
+  if (mode == 0) {
+    if (!isfinite(x)) x = 0.0;
+    const double t = __dmul_rn(x, kInv2Pi);
+    const double f = __dsub_rn(t, floor(t));
+    return __fma_rn(f, (double)nf, -hw);
+  }
+  const double d = isfinite(x) ? __dsub_rn(x, center) : 0.0;
+  return __fma_rn(d, scale, 0.5 * (double)nf - hw);
 }
 
-// Type-3 rescale: X = (x - center)*scale + nf/2, wrapped once into [0, nf).
-__device__ __forceinline__ double rescale_rn(double x, double center, double scale, int64_t nf) {
-  if (!isfinite(x)) return 0.0;
-  double d = __dsub_rn(x, center);
-  double X = __dmul_rn(d, scale);
-  X = __dadd_rn(X, 0.5 * (double)nf);
-  if (X < 0.0) X = __dadd_rn(X, (double)nf);
-  if (X >= (double)nf) X = __dsub_rn(X, (double)nf);
-  return X;
-}
-
+// Fold, grid start and bin of every point.  The first grid index a point
+// touches is i0 = ceil(s); its offset is delta = i0 - s in [0, 1).  The bin is
+// (i0 + w/2) / bs per axis after wrapping i0 + w/2 into [0, nf), so every
+// point's support starts inside its bin's tile, which therefore needs only
+// bs + w - 1 cells per axis.
 template <typename TX, typename TC, int DIM>
 __global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict__ x,
                             const TX* __restrict__ y, const TX* __restrict__ z,
@@ -52,17 +54,26 @@ __global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict
     const TX* c[3] = {x, y, z};
     PtRec<TC, DIM> r;
     int stride = 1;
+    const int h = g.w >> 1;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      const double xv = (double)c[d][j];
-      const double X = fs.mode == 0 ? fold_rn(xv, g.nf[d])
-                                    : rescale_rn(xv, fs.center[d], fs.scale[d], g.nf[d]);
-      const double s = __dsub_rn(X, 0.5 * (double)g.w);
-      const double cl = ceil(s);
-      r.i[d] = (int)cl;
-      r.d[d] = (TC)__dsub_rn(cl, s);
-      const int fl = (int)floor(X);
-      bin += (fl / g.bs[d]) * stride;
+      const double sh = grid_shift((double)c[d][j], fs.mode, fs.center[d], fs.scale[d],
+                                   g.nf[d], g.w);
+      const double cl = ceil(sh);
+      int i0 = (int)cl;
+      r.d[d] = (TC)__dsub_rn(cl, sh);
+      const int nf = (int)g.nf[d];
+      int tb = i0 + h;
+      if (tb < 0) {
+        tb += nf;
+        i0 += nf;
+      }
+      if (tb >= nf) {
+        tb -= nf;
+        i0 -= nf;
+      }
+      r.i[d] = i0;
+      bin += (tb / g.bs[d]) * stride;
       stride *= g.nb[d];
     }
     recs_in[j] = r;
@@ -204,69 +215,84 @@ __device__ __forceinline__ int64_t fine_to_mode(int64_t g, int64_t N, int64_t nf
   return k >= 0 ? k : k + N;
 }
 
+// Both deconvolution kernels index inside one transform with 32-bit
+// arithmetic (a fine grid has < 2^31 cells), take (x-block, y, z) from the
+// grid, and loop over the transforms inside the thread: no division and no
+// 64-bit multiply per element.
 template <typename TC, typename TD, int DIM>
-__global__ void deconv1_kernel(int64_t N0, int64_t N1, int64_t N2, int64_t nf0, int64_t nf1,
-                               int64_t nf2, int modeord, const TC* __restrict__ p0,
-                               const TC* __restrict__ p1, const TC* __restrict__ p2,
-                               const cplx_t<TC>* __restrict__ fine, cplx_t<TD>* __restrict__ out,
-                               int ntr) {
-  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void deconv1_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
+                               const TC* __restrict__ p0, const TC* __restrict__ p1,
+                               const TC* __restrict__ p2, const cplx_t<TC>* __restrict__ fine,
+                               cplx_t<TD>* __restrict__ out, int ntr, int64_t nftot,
+                               int64_t Ntot) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (i0 >= N0) return;
-  int64_t k0 = mode_freq(i0, N0, modeord);
-  const int64_t g0 = k0 < 0 ? k0 + nf0 : k0;
-  for (int64_t i1 = blockIdx.y; i1 < N1; i1 += gridDim.y) {
-  int64_t g1 = 0;
-  TC f = p0[i0];
-  if (DIM > 1) {
-    int64_t k1 = mode_freq(i1, N1, modeord);
-    g1 = k1 < 0 ? k1 + nf1 : k1;
-    f *= p1[i1];
-  }
-  for (int64_t zz = blockIdx.z; zz < (int64_t)N2 * ntr; zz += gridDim.z) {
-    const int64_t t = zz / N2, i2 = zz - t * N2;
-    int64_t g2 = 0;
-    TC ff = f;
+  int k0 = (int)mode_freq(i0, N0, modeord);
+  const int g0 = k0 < 0 ? k0 + nf0 : k0;
+  const TC f0 = p0[i0];
+  for (int i2 = blockIdx.z; i2 < N2; i2 += gridDim.z) {
+    int g2 = 0;
+    TC f2 = f0;
     if (DIM > 2) {
-      int64_t k2 = mode_freq(i2, N2, modeord);
+      const int k2 = (int)mode_freq(i2, N2, modeord);
       g2 = k2 < 0 ? k2 + nf2 : k2;
-      ff *= p2[i2];
+      f2 *= p2[i2];
     }
-    const cplx_t<TC> v = fine[((t * nf2 + g2) * nf1 + g1) * nf0 + g0];
-    cplx_t<TD> o;
-    o.x = (TD)(v.x * ff);
-    o.y = (TD)(v.y * ff);
-    out[((t * N2 + i2) * N1 + i1) * N0 + i0] = o;
-  }
+    for (int i1 = blockIdx.y; i1 < N1; i1 += gridDim.y) {
+      int g1 = 0;
+      TC f = f2;
+      if (DIM > 1) {
+        const int k1 = (int)mode_freq(i1, N1, modeord);
+        g1 = k1 < 0 ? k1 + nf1 : k1;
+        f *= p1[i1];
+      }
+      const int src = (g2 * nf1 + g1) * nf0 + g0;
+      const int dst = (i2 * N1 + i1) * N0 + i0;
+      for (int t = 0; t < ntr; ++t) {
+        const cplx_t<TC> v = fine[t * nftot + src];
+        cplx_t<TD> o;
+        o.x = (TD)(v.x * f);
+        o.y = (TD)(v.y * f);
+        out[t * Ntot + dst] = o;
+      }
+    }
   }
 }
 
 template <typename TC, typename TD, int DIM>
-__global__ void deconv2_kernel(int64_t N0, int64_t N1, int64_t N2, int64_t nf0, int64_t nf1,
-                               int64_t nf2, int modeord, const TC* __restrict__ p0,
-                               const TC* __restrict__ p1, const TC* __restrict__ p2,
-                               const cplx_t<TD>* __restrict__ in, cplx_t<TC>* __restrict__ fine,
-                               int ntr) {
-  const int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void deconv2_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
+                               const TC* __restrict__ p0, const TC* __restrict__ p1,
+                               const TC* __restrict__ p2, const cplx_t<TD>* __restrict__ in,
+                               cplx_t<TC>* __restrict__ fine, int ntr, int64_t nftot,
+                               int64_t Ntot) {
+  const int g0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (g0 >= nf0) return;
-  const int64_t i0 = fine_to_mode(g0, N0, nf0, modeord);
-  for (int64_t g1 = blockIdx.y; g1 < nf1; g1 += gridDim.y) {
-  const int64_t i1 = DIM > 1 ? fine_to_mode(g1, N1, nf1, modeord) : 0;
-  TC f = 0;
-  if (i0 >= 0 && i1 >= 0) f = p0[i0] * (DIM > 1 ? p1[i1] : TC(1));
-  for (int64_t zz = blockIdx.z; zz < (int64_t)nf2 * ntr; zz += gridDim.z) {
-    const int64_t t = zz / nf2, g2 = zz - t * nf2;
-    const int64_t i2 = DIM > 2 ? fine_to_mode(g2, N2, nf2, modeord) : 0;
-    cplx_t<TC> o;
-    o.x = 0;
-    o.y = 0;
-    if (i0 >= 0 && i1 >= 0 && i2 >= 0) {
-      const TC ff = DIM > 2 ? f * p2[i2] : f;
-      const cplx_t<TD> v = in[((t * N2 + i2) * N1 + i1) * N0 + i0];
-      o.x = (TC)v.x * ff;
-      o.y = (TC)v.y * ff;
+  const int i0 = (int)fine_to_mode(g0, N0, nf0, modeord);
+  const TC f0 = i0 >= 0 ? p0[i0] : TC(0);
+  for (int g2 = blockIdx.z; g2 < nf2; g2 += gridDim.z) {
+    const int i2 = DIM > 2 ? (int)fine_to_mode(g2, N2, nf2, modeord) : 0;
+    for (int g1 = blockIdx.y; g1 < nf1; g1 += gridDim.y) {
+      const int i1 = DIM > 1 ? (int)fine_to_mode(g1, N1, nf1, modeord) : 0;
+      const int dst = (g2 * nf1 + g1) * nf0 + g0;
+      cplx_t<TC> o;
+      o.x = TC(0);
+      o.y = TC(0);
+      if (i0 >= 0 && i1 >= 0 && i2 >= 0) {
+        TC f = f0;
+        if (DIM > 1) f *= p1[i1];
+        if (DIM > 2) f *= p2[i2];
+        const int src = (i2 * N1 + i1) * N0 + i0;
+        for (int t = 0; t < ntr; ++t) {
+          const cplx_t<TD> v = in[t * Ntot + src];
+          cplx_t<TC> r;
+          r.x = (TC)v.x * f;
+          r.y = (TC)v.y * f;
+          fine[t * nftot + dst] = r;
+        }
+      } else {
+        for (int t = 0; t < ntr; ++t) fine[t * nftot + dst] = o;
+      }
     }
-    fine[((t * nf2 + g2) * nf1 + g1) * nf0 + g0] = o;
-  }
   }
 }
 
@@ -512,33 +538,28 @@ template <typename TC, typename TD>
 cudaError_t launch_deconv1(int dim, const int64_t* N, const int64_t* nf, int modeord,
                            const TC* const* phi, const void* fine, void* out, int ntr,
                            cudaStream_t s) {
+  const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
   dim3 grid(grid1(N[0], 128), (unsigned)(N[1] < 65535 ? N[1] : 65535),
-            (unsigned)(N[2] * ntr < 65535 ? N[2] * ntr : 65535));
+            (unsigned)(N[2] < 65535 ? N[2] : 65535));
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
+  auto args = [&](auto kern) {
+    kern<<<grid, 128, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
+                              (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TC>*)fine,
+                              (cplx_t<TD>*)out, ntr, nftot, Ntot);
+  };
   switch (dim) {
     case 1:
-      deconv1_kernel<TC, TD, 1><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
-                                                     modeord, phi[0], p1, p2,
-                                                     (const cplx_t<TC>*)fine, (cplx_t<TD>*)out,
-                                                     ntr);
-      note_launch();
+      args(deconv1_kernel<TC, TD, 1>);
       break;
     case 2:
-      deconv1_kernel<TC, TD, 2><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
-                                                     modeord, phi[0], p1, p2,
-                                                     (const cplx_t<TC>*)fine, (cplx_t<TD>*)out,
-                                                     ntr);
-      note_launch();
+      args(deconv1_kernel<TC, TD, 2>);
       break;
     default:
-      deconv1_kernel<TC, TD, 3><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
-                                                     modeord, phi[0], p1, p2,
-                                                     (const cplx_t<TC>*)fine, (cplx_t<TD>*)out,
-                                                     ntr);
-      note_launch();
+      args(deconv1_kernel<TC, TD, 3>);
       break;
   }
+  note_launch();
   return cudaGetLastError();
 }
 
@@ -546,33 +567,28 @@ template <typename TC, typename TD>
 cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int modeord,
                            const TC* const* phi, const void* in, void* fine, int ntr,
                            cudaStream_t s) {
+  const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
   dim3 grid(grid1(nf[0], 128), (unsigned)(nf[1] < 65535 ? nf[1] : 65535),
-            (unsigned)(nf[2] * ntr < 65535 ? nf[2] * ntr : 65535));
+            (unsigned)(nf[2] < 65535 ? nf[2] : 65535));
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
+  auto args = [&](auto kern) {
+    kern<<<grid, 128, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
+                              (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TD>*)in,
+                              (cplx_t<TC>*)fine, ntr, nftot, Ntot);
+  };
   switch (dim) {
     case 1:
-      deconv2_kernel<TC, TD, 1><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
-                                                     modeord, phi[0], p1, p2,
-                                                     (const cplx_t<TD>*)in, (cplx_t<TC>*)fine,
-                                                     ntr);
-      note_launch();
+      args(deconv2_kernel<TC, TD, 1>);
       break;
     case 2:
-      deconv2_kernel<TC, TD, 2><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
-                                                     modeord, phi[0], p1, p2,
-                                                     (const cplx_t<TD>*)in, (cplx_t<TC>*)fine,
-                                                     ntr);
-      note_launch();
+      args(deconv2_kernel<TC, TD, 2>);
       break;
     default:
-      deconv2_kernel<TC, TD, 3><<<grid, 128, 0, s>>>(N[0], N[1], N[2], nf[0], nf[1], nf[2],
-                                                     modeord, phi[0], p1, p2,
-                                                     (const cplx_t<TD>*)in, (cplx_t<TC>*)fine,
-                                                     ntr);
-      note_launch();
+      args(deconv2_kernel<TC, TD, 3>);
       break;
   }
+  note_launch();
   return cudaGetLastError();
 }
 

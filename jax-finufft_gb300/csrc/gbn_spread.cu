@@ -5,15 +5,21 @@
 // maxsub bin-sorted points of one bin.  Inside a block, G consecutive lanes
 // share a point: lane gl evaluates kernel piece gl in every axis (Horner),
 // the y/z values are broadcast with warp shuffles, and lane gl applies the
-// x offset gl of every (y, z) row.  The 32/G points a warp handles at once
-// hit G consecutive words each, so the shared-memory atomics of a warp
-// instruction land in few banks.
+// x offset gl of every (y, z) row.
 //
 //   method 2 (SM): the block accumulates into a shared-memory tile of
-//     (bs+w)^d cells kept as separate real/imaginary planes, then adds the
+//     (bs+w-1)^d cells kept as separate real/imaginary planes, then adds the
 //     tile to the fine grid with one vector atomic (float2) per non-zero cell.
+//     In FP32 the tile holds 32-bit fixed-point integers: the block scales
+//     its points' strengths by s = 2^30 / sum_j max(|Re c_j|, |Im c_j|), so
+//     no cell sum can exceed 2^30 in magnitude, rounds every contribution to
+//     an integer and adds it with an integer shared-memory atomic (about 3x
+//     the throughput of a float shared-memory atomic on sm_103).  The integer
+//     sums are exact; the only rounding is the per-contribution 0.5/s =
+//     sum|c|/2^31, the size of an FP32 rounding of the contribution itself.
+//     FP64 keeps double atomics.
 //   method 1 (GM): every update is a global atomic; used when the tile would
-//     not fit (FP64 in 3D at large w) or when points are not sorted.
+//     not fit or when points are not sorted.
 #include <cuda_runtime.h>
 
 #include "gbn_common.cuh"
@@ -52,44 +58,70 @@ __device__ __forceinline__ bool sub_range(const SubArgs& sa, const Geom& g, int6
   return cnt > 0;
 }
 
+// Shared-memory accumulators: float/double planes, or int32 fixed point.
+template <typename TC>
+struct Acc {
+  using type = TC;
+};
+template <>
+struct Acc<float> {
+  using type = int;
+};
+
+__device__ __forceinline__ void acc_add(int* p, float v) { atomicAdd(p, __float2int_rn(v)); }
+__device__ __forceinline__ void acc_add(double* p, double v) { atomicAdd(p, v); }
+
 template <typename TC, typename TD, int DIM, int G>
 __global__ void __launch_bounds__(kThreads)
     spread_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
                      SubArgs sa, const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ fine,
                      int64_t nftot) {
+  using A = typename Acc<TC>::type;
+  constexpr bool kFixed = sizeof(A) == 4 && sizeof(TC) == 4;
   constexpr int NCO = GroupCfg<G>::NCO;
   constexpr int PPW = 32 / G;
   constexpr int NWARP = kThreads / 32;
+  __shared__ TC s_red[NWARP];
   int start, cnt, bin;
   if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
   const int t = blockIdx.y;
-  const int w = g.w, h = w >> 1;
-
-  int org[3] = {0, 0, 0}, T[3] = {1, 1, 1};
-  {
-    int rem = bin;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      const int b = rem % g.nb[d];
-      rem /= g.nb[d];
-      org[d] = b * g.bs[d] - h;
-      T[d] = g.bs[d] + w;
-    }
-  }
-  const int ncell = T[0] * T[1] * T[2];
+  const int w = g.w;
+  const Tile<DIM> tl(g, bin);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TC* sre = reinterpret_cast<TC*>(smem_raw);
-  TC* sim = sre + ncell;
-  for (int i = threadIdx.x; i < ncell; i += kThreads) {
-    sre[i] = TC(0);
-    sim[i] = TC(0);
+  A* sre = reinterpret_cast<A*>(smem_raw);
+  A* sim = sre + tl.ncell;
+  for (int i = threadIdx.x; i < tl.ncell; i += kThreads) {
+    sre[i] = A(0);
+    sim[i] = A(0);
   }
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
+  const cplx_t<TD>* ct = c + (int64_t)t * M;
+
+  // fixed-point scale from the subproblem's strengths
+  TC scale = TC(1), inv = TC(1);
+  if (kFixed) {
+    TC part = TC(0);
+    for (int p = threadIdx.x; p < cnt; p += kThreads) {
+      const int js = start + p;
+      TC re, im;
+      load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), re, im);
+      part += fmax(fabs(re), fabs(im));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) s_red[warp] = part;
+    __syncthreads();
+    TC B = TC(0);
+#pragma unroll
+    for (int i = 0; i < NWARP; ++i) B += s_red[i];
+    // B == 0 (or denormal): nothing to spread; the tile stays zero
+    scale = B > TC(1e-30) ? TC(1073741824.0) / B : TC(0);
+    inv = B > TC(1e-30) ? B / TC(1073741824.0) : TC(0);
+  }
   TC co[NCO];
   load_coef<TC, NCO>(co, ks, gl, w);
   __syncthreads();
 
-  const cplx_t<TD>* ct = c + (int64_t)t * M;
   const bool lane_on = gl < w;
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
@@ -98,32 +130,31 @@ __global__ void __launch_bounds__(kThreads)
     const PtRec<TC, DIM> r = recs[js];
     TC cr = TC(0), ci = TC(0);
     if (valid) load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), cr, ci);
-    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
-    const int l0 = r.i[0] - org[0] + gl;
+    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w) * scale;
+    const int l0 = r.i[0] - tl.org[0] + gl;
     const bool on = valid && lane_on;
+    const TC vr = cr * kx, vi = ci * kx;
     if (DIM == 1) {
       if (on) {
-        atomicAdd(&sre[l0], cr * kx);
-        atomicAdd(&sim[l0], ci * kx);
+        acc_add(&sre[l0], vr);
+        acc_add(&sim[l0], vi);
       }
     } else if (DIM == 2) {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      const TC vr = cr * kx, vi = ci * kx;
-      int idx = (r.i[1] - org[1]) * T[0] + l0;
+      int idx = (r.i[1] - tl.org[1]) * tl.T[0] + l0;
       for (int iy = 0; iy < w; ++iy) {
         const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
         if (on) {
-          atomicAdd(&sre[idx], vr * kyv);
-          atomicAdd(&sim[idx], vi * kyv);
+          acc_add(&sre[idx], vr * kyv);
+          acc_add(&sim[idx], vi * kyv);
         }
-        idx += T[0];
+        idx += tl.T[0];
       }
     } else {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
-      const TC vr = cr * kx, vi = ci * kx;
-      const int plane = T[0] * T[1];
-      int zbase = ((r.i[2] - org[2]) * T[1] + (r.i[1] - org[1])) * T[0] + l0;
+      const int plane = tl.T[0] * tl.T[1];
+      int zbase = ((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0;
       for (int iz = 0; iz < w; ++iz) {
         const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
         const TC zr = vr * kzv, zi = vi * kzv;
@@ -131,10 +162,10 @@ __global__ void __launch_bounds__(kThreads)
         for (int iy = 0; iy < w; ++iy) {
           const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
           if (on) {
-            atomicAdd(&sre[idx], zr * kyv);
-            atomicAdd(&sim[idx], zi * kyv);
+            acc_add(&sre[idx], zr * kyv);
+            acc_add(&sim[idx], zi * kyv);
           }
-          idx += T[0];
+          idx += tl.T[0];
         }
         zbase += plane;
       }
@@ -143,17 +174,15 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
 
   cplx_t<TC>* ft = fine + (int64_t)t * nftot;
-  for (int i = threadIdx.x; i < ncell; i += kThreads) {
-    const TC vr = sre[i], vi = sim[i];
-    if (vr == TC(0) && vi == TC(0)) continue;
-    const int c0 = i % T[0];
-    const int r1 = i / T[0];
-    const int c1 = r1 % T[1];
-    const int c2 = r1 / T[1];
-    const int64_t g0 = wrap_idx(org[0] + c0, g.nf[0]);
-    const int64_t g1 = DIM > 1 ? wrap_idx(org[1] + c1, g.nf[1]) : 0;
-    const int64_t g2 = DIM > 2 ? wrap_idx(org[2] + c2, g.nf[2]) : 0;
-    atomic_add_c(&ft[(g2 * g.nf[1] + g1) * g.nf[0] + g0], vr, vi);
+  const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
+  CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
+  for (int i = threadIdx.x; i < tl.ncell; i += kThreads, cw.next()) {
+    const A ar = sre[i], ai = sim[i];
+    if (ar == A(0) && ai == A(0)) continue;
+    const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
+    const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
+    const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
+    atomic_add_c(&ft[(g2 * nf1 + g1) * nf0 + g0], (TC)ar * inv, (TC)ai * inv);
   }
 }
 
@@ -175,6 +204,7 @@ __global__ void __launch_bounds__(kThreads)
   const cplx_t<TD>* ct = c + (int64_t)t * M;
   cplx_t<TC>* ft = fine + (int64_t)t * nftot;
   const bool lane_on = gl < w;
+  const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
     const bool valid = pi < cnt;
@@ -183,7 +213,7 @@ __global__ void __launch_bounds__(kThreads)
     TC cr = TC(0), ci = TC(0);
     if (valid) load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), cr, ci);
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
-    const int64_t gx = wrap_idx((int64_t)r.i[0] + gl, g.nf[0]);
+    const int gx = wrap_i32(r.i[0] + gl, nf0);
     const bool on = valid && lane_on;
     const TC vr = cr * kx, vi = ci * kx;
     if (DIM == 1) {
@@ -192,20 +222,20 @@ __global__ void __launch_bounds__(kThreads)
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       for (int iy = 0; iy < w; ++iy) {
         const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-        const int64_t gy = wrap_idx((int64_t)r.i[1] + iy, g.nf[1]);
-        if (on) atomic_add_c(&ft[gy * g.nf[0] + gx], vr * kyv, vi * kyv);
+        const int gy = wrap_i32(r.i[1] + iy, nf1);
+        if (on) atomic_add_c(&ft[gy * nf0 + gx], vr * kyv, vi * kyv);
       }
     } else {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
       for (int iz = 0; iz < w; ++iz) {
         const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
-        const int64_t gz = wrap_idx((int64_t)r.i[2] + iz, g.nf[2]);
+        const int gz = wrap_i32(r.i[2] + iz, nf2);
         const TC zr = vr * kzv, zi = vi * kzv;
         for (int iy = 0; iy < w; ++iy) {
           const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-          const int64_t gy = wrap_idx((int64_t)r.i[1] + iy, g.nf[1]);
-          if (on) atomic_add_c(&ft[(gz * g.nf[1] + gy) * g.nf[0] + gx], zr * kyv, zi * kyv);
+          const int gy = wrap_i32(r.i[1] + iy, nf1);
+          if (on) atomic_add_c(&ft[(gz * nf1 + gy) * nf0 + gx], zr * kyv, zi * kyv);
         }
       }
     }
@@ -234,10 +264,10 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     dim3 grid((unsigned)nblk, (unsigned)nt);
     const cplx_t<TD>* ct = (const cplx_t<TD>*)c + (int64_t)t0 * M;
     cplx_t<TC>* ft = (cplx_t<TC>*)fine + (int64_t)t0 * nftot;
-    if (method == 2) {
+    if (method == 2 && sa.sorted) {
       int64_t ncell = 1;
-      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w;
-      const size_t smem = (size_t)ncell * 2 * sizeof(TC);
+      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w - 1;
+      const size_t smem = (size_t)ncell * 2 * sizeof(typename Acc<TC>::type);
       auto kern = spread_sm_kernel<TC, TD, DIM, G>;
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);

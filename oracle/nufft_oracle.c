@@ -191,50 +191,57 @@ double orc_fold(double x, int64_t nf) {
   return X;
 }
 
-/* Type-3 rescale onto a non-periodic grid: X = (x - center) * inv + nf/2,
- * kept inside [0, nf) by one wrap in either direction. */
-double orc_rescale(double x, double center, double inv, int64_t nf) {
-  if (!isfinite(x)) return 0.0;
-  double d = x - center;
-  double X = d * inv;
-  X = X + 0.5 * (double)nf;
-  if (X < 0.0) X = X + (double)nf;
-  if (X >= (double)nf) X = X - (double)nf;
-  return X;
+/* Position of a point in fine-grid cells minus w/2: s = X - w/2.
+ * mode 0 (periodic fold): t = x/(2 pi), f = t - floor(t), s = fma(f, nf, -w/2).
+ * mode 1 (type-3 rescale): s = fma(x - center, scale, nf/2 - w/2).
+ * One rounding per operation (fma is a single rounding), the same sequence
+ * the CUDA kernels use.  Non-finite x counts as 0 (mode 0) / the centre. */
+static double orc_grid_shift(double x, int mode, double center, double scale, int64_t nf, int w) {
+  double hw = 0.5 * (double)w;
+  if (mode == 0) {
+    if (!isfinite(x)) x = 0.0;
+    double t = x * ORC_INV2PI;
+    double f = t - floor(t);
+    return fma(f, (double)nf, -hw);
+  }
+  double d = isfinite(x) ? x - center : 0.0;
+  return fma(d, scale, 0.5 * (double)nf - hw);
 }
 
-/* Grid start i0 = ceil(X - w/2) and offset delta = i0 - (X - w/2). */
-static inline void orc_start(double X, int w, int64_t *i0, double *delta) {
-  double s = X - 0.5 * (double)w;
-  double c = ceil(s);
-  *i0 = (int64_t)c;
-  *delta = c - s;
-}
-
-/* Fold points (mode 0) or rescale them (mode 1, type 3) onto grid
- * coordinates, and report per point the grid start, the offset and the bin
- * index bin = floor(X_0)/B_0 + nb_0*(floor(X_1)/B_1 + nb_1*floor(X_2)/B_2).
- * coords[d] may be NULL for d >= dim.  center/inv are read for mode 1 only. */
+/* Per point and axis: grid start i0 = ceil(s) (wrapped so that i0 + w/2 lies
+ * in [0, nf)), offset delta = i0 - s in [0, 1), and the bin index
+ * sum_d ((i0_d + w/2) / B_d) * prod_{e<d} nb_e with nb_d = ceil(nf_d / B_d).
+ * X is the folded coordinate s + w/2 (reported for reference).
+ * coords[d] may be NULL for d >= dim; center/scale are read for mode 1 only. */
 void orc_fold_points(int dim, int mode, int w, const int64_t *nf, const int *binsize, int64_t M,
                      const double *cx, const double *cy, const double *cz,
-                     const double *center, const double *inv, double *X, int64_t *i0,
+                     const double *center, const double *scale, double *X, int64_t *i0,
                      double *delta, int64_t *bin) {
   const double *c[3] = {cx, cy, cz};
   int64_t nb[3];
+  int h = w / 2;
   for (int d = 0; d < 3; ++d) nb[d] = (d < dim) ? (nf[d] + binsize[d] - 1) / binsize[d] : 1;
 #pragma omp parallel for schedule(static)
   for (int64_t j = 0; j < M; ++j) {
     int64_t b = 0, stride = 1;
     for (int d = 0; d < dim; ++d) {
-      double Xd = mode == 0 ? orc_fold(c[d][j], nf[d]) : orc_rescale(c[d][j], center[d], inv[d], nf[d]);
-      int64_t s;
-      double del;
-      orc_start(Xd, w, &s, &del);
-      X[j * 3 + d] = Xd;
-      i0[j * 3 + d] = s;
-      delta[j * 3 + d] = del;
-      int64_t fl = (int64_t)floor(Xd);
-      b += (fl / binsize[d]) * stride;
+      double s = orc_grid_shift(c[d][j], mode, mode ? center[d] : 0.0, mode ? scale[d] : 1.0,
+                                nf[d], w);
+      double cl = ceil(s);
+      int64_t s0 = (int64_t)cl;
+      int64_t tb = s0 + h;
+      if (tb < 0) {
+        tb += nf[d];
+        s0 += nf[d];
+      }
+      if (tb >= nf[d]) {
+        tb -= nf[d];
+        s0 -= nf[d];
+      }
+      X[j * 3 + d] = s + 0.5 * (double)w;
+      i0[j * 3 + d] = s0;
+      delta[j * 3 + d] = cl - s;
+      b += (tb / binsize[d]) * stride;
       stride *= nb[d];
     }
     for (int d = dim; d < 3; ++d) {
