@@ -340,6 +340,9 @@ def run_ours(args):
     }
     lib.gbn_destroy(p1)
     lib.gbn_destroy(p2)
+    if not args.no_extra:
+        result["secondary"] = {"lsq_grad_fwd_bwd": measure_lsq_grad(dev, max(3, args.steps // 2),
+                                                                    args.warmup)}
     return finish(args, result, rank, ws)
 
 
@@ -385,6 +388,57 @@ def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, max_over_
     return ws * 2 * M / (e2e_ms * 1e-3), e2e_ms
 
 
+def measure_lsq_grad(dev, steps, warmup):
+    """Differentiated 3D type-2 least-squares loss (128^3 modes, M=2e6, c64,
+    eps=1e-6): L = sum_j |nufft2(c; x_j, y_j, z_j) - d_j|^2 with gradients
+    with respect to c and x, y, z, through the torch API.  Returns
+    fwd+bwd steps/s for the fused adjoint and for the stacked-transform path
+    of the reference's rules."""
+    import torch
+
+    import jax_finufft_gb300 as jf
+    from jax_finufft_gb300.options import Opts
+
+    rng = np.random.default_rng(SEED + 4)
+    N, M = 128, 2_000_000
+    c = torch.tensor((rng.standard_normal((N, N, N)) + 1j * rng.standard_normal((N, N, N)))
+                     .astype(np.complex64), device=dev)
+    c2 = torch.tensor((rng.standard_normal((N, N, N)) + 1j * rng.standard_normal((N, N, N)))
+                      .astype(np.complex64), device=dev)
+    pts = [torch.tensor(rng.uniform(-np.pi, np.pi, M).astype(np.float32), device=dev)
+           for _ in range(3)]
+    noise = torch.tensor((0.1 * (rng.standard_normal(M) + 1j * rng.standard_normal(M)))
+                         .astype(np.complex64), device=dev)
+    with torch.no_grad():
+        d = jf.nufft2(c2, *pts, eps=1e-6) + noise
+    out = {}
+    for name, fused in (("fused_adjoint", True), ("stacked_transforms", False)):
+        opts = Opts(gpu_fused_adjoint=fused)
+        a = [c.clone().requires_grad_(True)] + [p.clone().requires_grad_(True) for p in pts]
+
+        def step():
+            r = jf.nufft2(a[0], *a[1:], eps=1e-6, opts=opts) - d
+            loss = torch.sum(torch.real(r) ** 2 + torch.imag(r) ** 2)
+            return torch.autograd.grad(loss, a)
+
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms}
+    out["workload"] = ("3D type-2 least-squares loss, 128^3 modes, M=2e6 uniform points, "
+                       "complex64, eps=1e-6, gradients w.r.t. c and x, y, z (torch API)")
+    out["speedup_fused"] = out["stacked_transforms"]["ms_per_step"] / out["fused_adjoint"]["ms_per_step"]
+    return out
+
+
 def finish(args, result, rank, ws):
     import torch
 
@@ -413,6 +467,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the secondary measurements (differentiated loss)")
+    ap.add_argument("--lsq-only", action="store_true",
+                    help="run only the differentiated least-squares measurement")
     ap.add_argument("--points", type=int, default=M_POINTS,
                     help="points per transform (reduced cases for profiling)")
     ap.add_argument("--modes", type=int, default=N_MODES, help="modes per axis")
@@ -421,6 +479,12 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.lsq_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(measure_lsq_grad(torch.device("cuda", 0), args.steps, args.warmup)))
+        return 0
     return run_ours(args)
 
 

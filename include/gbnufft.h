@@ -126,6 +126,40 @@ GBN_API int gbn_debug_bins(gbn_plan plan, int64_t* bins_out, int64_t* counts_out
  * (double, M x 3, input order) computed by setpts (test hook). */
 GBN_API int gbn_debug_fold(gbn_plan plan, int64_t* i0_out, double* delta_out);
 
+/*
+ * Point sets and fused gradients.  No counterpart in the reference: its
+ * plans hold one point set (setpts, lib/kernels.cc.cu:57-80) and its
+ * gradients are separate transforms issued by the JVP/transpose rules
+ * (src/jax_finufft/ops.py:158-314), each sorting the points again.
+ *
+ * gbn_points_create sorts M points (device pointers in the plan's point
+ * precision, backend order) for a type-1 or type-2 plan's geometry into a
+ * point set that lives until gbn_points_destroy, so the forward's sort can
+ * serve the backward.  gbn_execute_points runs ntr transforms on it: dir = +1
+ * the plan's own transform, dir = -1 its adjoint (opposite exponent sign; a
+ * type-1 plan then maps modes f to strengths c, a type-2 plan c to f).
+ *
+ * gbn_grad: gradients of a real loss through the plan's transform, with
+ * g = the output cotangent (2 dL/dconj(out), PyTorch's convention):
+ *   type-1 plan (f = A c, src = c (ntr, M), g (ntr, N...)):
+ *     grad_src = A^H g (ntr, M) if non-NULL;
+ *     grad_x[d][j] = sum_t Re(iflag i c_tj conj((A^H (k_d g_t))_j)).
+ *   type-2 plan (c = B f, src = f (ntr, N...), g (ntr, M)):
+ *     grad_src = B^H g (ntr, N...) if non-NULL;
+ *     grad_x[d][j] = sum_t Re(conj(g_tj) (B (iflag i k_d f_t))_j).
+ * grad_x holds dim pointers (backend order, M reals in the point precision,
+ * NULL to skip an axis).  The coordinate terms and (type 1) the strength
+ * gradient come from one batched cuFFT of the stacked k-weighted grids and
+ * one interpolation pass with shared kernel weights, on the given point set.
+ */
+typedef struct gbn_points_s* gbn_points;
+GBN_API int gbn_points_create(gbn_plan plan, int64_t M, const void* x, const void* y,
+                              const void* z, gbn_points* out);
+GBN_API int gbn_points_destroy(gbn_points pts);
+GBN_API int gbn_execute_points(gbn_plan plan, gbn_points pts, int ntr, int dir, void* c, void* f);
+GBN_API int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void* g,
+                     void* grad_src, void* const* grad_x);
+
 /* Thread-local message describing the last non-zero status. */
 GBN_API const char* gbn_last_error(void);
 

@@ -165,6 +165,26 @@ cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, cons
                                    const double* const* tau, int iflag, int w, double beta,
                                    void* fac, cudaStream_t s);
 
+// Gradient grids: for every transform, E fine grids from its modes `in`
+// (ntr, N): grid e < base holds mode/psihat, grid e >= base holds
+// (a_re + i a_im) * k_{dims[e]} * mode/psihat, with k the integer frequency
+// along backend axis dims[e].  Layout (t*E + e)*nftot + cell.
+template <typename TC, typename TD>
+cudaError_t launch_deconv2w(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                            const TC* const* phi, const void* in, void* grids, int ntr, int E,
+                            int base, const int* dims, double a_re, double a_im, cudaStream_t s);
+
+// Gather all E grids of every transform at each point with shared kernel
+// weights and combine them into gradients (see gbn_grad.cu): mode 0 = the
+// type-1 gradient (w = strengths; grid 0 -> out_c when base = 1), mode 1 =
+// the type-2 coordinate gradient (w = output cotangent).  gx[d] (M reals,
+// may be null) is accumulated.
+template <typename TC, typename TD>
+cudaError_t launch_interp_grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                               const SortState& st, const void* grids, int ntr, int E, int mode,
+                               int iflag, int base, const int* dims, const void* w, void* out_c,
+                               void* const* gx, bool shared, cudaStream_t s);
+
 // out[t, j] = in[t, j] * fac[j] (complex), ntr transforms of length n.
 template <typename TI, typename TO, typename TF>
 cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, void* out,

@@ -279,8 +279,33 @@ size_t rec_size(int dim, bool single) {
 }  // namespace
 
 // =============================================================================
-// plan
+// point sets and plans
 // =============================================================================
+
+// Sorted nonuniform points for a plan's geometry.  A plan owns one (the
+// classic setpts/execute API); gbn_points_create makes more that outlive an
+// execute, so a gradient can reuse the forward's sort.
+struct gbn_points_s {
+  DevBuf pt_bin, pt_rank, bin_count, bin_start, perm, sub_count, sub_start, sub_bin, sub_off,
+      n_sub, recs, recs_in, scan_tmp;
+  SortState st{};
+  int64_t M = 0;
+  bool set = false;
+  // geometry it was sorted for (checked against the plan that uses it)
+  int dim = 0;
+  bool comp_single = true;
+  int64_t nf[3] = {0, 0, 0};
+  int w = 0;
+  cudaStream_t stream = nullptr;
+
+  void release() {
+    DevBuf* bufs[] = {&pt_bin,  &pt_rank, &bin_count, &bin_start, &perm,   &sub_count, &sub_start,
+                      &sub_bin, &sub_off, &n_sub,     &recs,      &recs_in, &scan_tmp};
+    for (DevBuf* b : bufs) b->release(stream);
+  }
+  ~gbn_points_s() { release(); }
+};
+
 struct gbn_plan_s {
   int type = 1, dim = 1, iflag = 1, ntransf = 1;
   bool data_single = true, comp_single = true;
@@ -297,15 +322,11 @@ struct gbn_plan_s {
   int device = 0;
   Geom geom{};
 
-  DevBuf coef, phi[3], fine;
-  DevBuf pt_bin, pt_rank, bin_count, bin_start, perm, sub_count, sub_start, sub_bin, sub_off,
-      n_sub, recs, recs_in, scan_tmp;
-  SortState st{};
-  int64_t M = 0;
-  bool pts_set = false;
+  DevBuf coef, phi[3], fine, gfine;
+  gbn_points_s own;  // the point set of setpts/execute
 
-  cufftHandle fft = 0, fft_rem = 0;
-  int fft_batch = 0, fft_rem_batch = 0;
+  // cuFFT plans by batch count (fine grids per exec)
+  std::vector<std::pair<int, cufftHandle>> ffts;
 
   // type 3
   std::unique_ptr<gbn_plan_s> inner;
@@ -322,14 +343,13 @@ struct gbn_plan_s {
 
   ~gbn_plan_s() {
     cudaStreamSynchronize(stream);
-    DevBuf* bufs[] = {&coef,   &phi[0],    &phi[1],    &phi[2],   &fine,     &pt_bin,
-                      &pt_rank, &bin_count, &bin_start, &perm,     &sub_count, &sub_start,
-                      &sub_bin, &sub_off,   &n_sub,     &recs,     &recs_in,  &scan_tmp,
-                      &t3_tau[0], &t3_tau[1], &t3_tau[2], &t3_pre,  &t3_post,  &t3_cbuf,
-                      &t3_obuf, &t3_minmax};
+    DevBuf* bufs[] = {&coef,      &phi[0],    &phi[1],    &phi[2], &fine,    &gfine,
+                      &t3_tau[0], &t3_tau[1], &t3_tau[2], &t3_pre, &t3_post, &t3_cbuf,
+                      &t3_obuf,   &t3_minmax};
     for (DevBuf* b : bufs) b->release(stream);
-    if (fft) cufftDestroy(fft);
-    if (fft_rem) cufftDestroy(fft_rem);
+    own.stream = stream;
+    own.release();
+    for (auto& h : ffts) cufftDestroy(h.second);
     for (auto& e : ev_exec) cudaEventDestroy(e);
     for (auto& e : ev_setpts) cudaEventDestroy(e);
     cudaStreamSynchronize(stream);
@@ -458,30 +478,26 @@ int make_fft(gbn_plan_s* p, int nbatch, cufftHandle* h) {
   return GBN_OK;
 }
 
-int exec_fft(gbn_plan_s* p, int nb) {
-  cufftHandle* h;
-  if (nb == p->batch) {
-    if (!p->fft) {
-      GBN_TRY(make_fft(p, p->batch, &p->fft));
-      p->fft_batch = p->batch;
+// In-place batched FFT of nb fine grids at buf with exponent sign `sign`.
+int exec_fft(gbn_plan_s* p, void* buf, int nb, int sign) {
+  cufftHandle h = 0;
+  for (auto& e : p->ffts)
+    if (e.first == nb) h = e.second;
+  if (!h) {
+    GBN_TRY(make_fft(p, nb, &h));
+    p->ffts.emplace_back(nb, h);
+    if (p->ffts.size() > 4) {  // keep the cache small: drop the oldest
+      cufftDestroy(p->ffts.front().second);
+      p->ffts.erase(p->ffts.begin());
     }
-    h = &p->fft;
-  } else {
-    if (!p->fft_rem || p->fft_rem_batch != nb) {
-      if (p->fft_rem) cufftDestroy(p->fft_rem);
-      p->fft_rem = 0;
-      GBN_TRY(make_fft(p, nb, &p->fft_rem));
-      p->fft_rem_batch = nb;
-    }
-    h = &p->fft_rem;
   }
-  cufftSetStream(*h, p->stream);
-  const int dir = p->iflag >= 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
+  cufftSetStream(h, p->stream);
+  const int dir = sign >= 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
   cufftResult r;
   if (p->comp_single)
-    r = cufftExecC2C(*h, (cufftComplex*)p->fine.p, (cufftComplex*)p->fine.p, dir);
+    r = cufftExecC2C(h, (cufftComplex*)buf, (cufftComplex*)buf, dir);
   else
-    r = cufftExecZ2Z(*h, (cufftDoubleComplex*)p->fine.p, (cufftDoubleComplex*)p->fine.p, dir);
+    r = cufftExecZ2Z(h, (cufftDoubleComplex*)buf, (cufftDoubleComplex*)buf, dir);
   if (r != CUFFT_SUCCESS) return fail(GBN_ERR_CUFFT, "cufftExec failed with code " + std::to_string((int)r));
   return GBN_OK;
 }
@@ -585,70 +601,84 @@ cudaEvent_t* take_events(std::vector<cudaEvent_t>& pool, size_t& used, size_t n)
   return r;
 }
 
-void fill_sort_state(gbn_plan_s* p) {
-  SortState& st = p->st;
-  st.pt_bin = p->pt_bin.as<int>();
-  st.pt_rank = p->pt_rank.as<int>();
-  st.bin_count = p->sorted ? p->bin_count.as<int>() : nullptr;
-  st.bin_start = p->bin_start.as<int>();
-  st.perm = p->sorted ? p->perm.as<int>() : nullptr;
-  st.sub_count = p->sub_count.as<int>();
-  st.sub_start = p->sub_start.as<int>();
-  st.sub_bin = p->sub_bin.as<int>();
-  st.sub_off = p->sub_off.as<int>();
-  st.n_sub = p->n_sub.as<int>();
-  st.recs = p->recs.p;
-  st.recs_in = p->recs_in.p;
-  st.scan_tmp = p->scan_tmp.as<int>();
+void fill_sort_state(gbn_points_s& ps, bool sorted) {
+  SortState& st = ps.st;
+  st.pt_bin = ps.pt_bin.as<int>();
+  st.pt_rank = ps.pt_rank.as<int>();
+  st.bin_count = sorted ? ps.bin_count.as<int>() : nullptr;
+  st.bin_start = ps.bin_start.as<int>();
+  st.perm = sorted ? ps.perm.as<int>() : nullptr;
+  st.sub_count = ps.sub_count.as<int>();
+  st.sub_start = ps.sub_start.as<int>();
+  st.sub_bin = ps.sub_bin.as<int>();
+  st.sub_off = ps.sub_off.as<int>();
+  st.n_sub = ps.n_sub.as<int>();
+  st.recs = ps.recs.p;
+  st.recs_in = ps.recs_in.p;
+  st.scan_tmp = ps.scan_tmp.as<int>();
 }
 
-// Fold + sort M points (coordinate type TX) onto the plan's geometry.
+// Fold + sort M points (coordinate type TX) onto the plan's geometry into ps.
 template <typename TX>
-int sort_points(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
-                const FoldSpec& fs) {
+int sort_points(gbn_plan_s* p, gbn_points_s& ps, int64_t M, const TX* x, const TX* y,
+                const TX* z, const FoldSpec& fs) {
   if (M < 0) return fail(GBN_ERR_ARGS, "number of points must be >= 0");
   if (M > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "too many points (> 2^31)");
   if (M > 0 && (!x || (p->dim > 1 && !y) || (p->dim > 2 && !z)))
     return fail(GBN_ERR_ARGS, "missing coordinate array");
   cudaStream_t s = p->stream;
+  ps.stream = s;
   const Geom& g = p->geom;
   const size_t rs = rec_size(p->dim, p->comp_single);
   const size_t m = (size_t)std::max<int64_t>(M, 1);
-  GBN_CUDA(p->recs_in.ensure(m * rs, s));
-  GBN_CUDA(p->pt_bin.ensure(m * 4, s));
-  GBN_CUDA(p->pt_rank.ensure(m * 4, s));
+  GBN_CUDA(ps.recs_in.ensure(m * rs, s));
+  GBN_CUDA(ps.pt_bin.ensure(m * 4, s));
+  GBN_CUDA(ps.pt_rank.ensure(m * 4, s));
   if (p->sorted) {
     const int64_t nb = g.nbins;
-    p->st.max_sub = nb + (M + g.maxsub - 1) / g.maxsub;
-    GBN_CUDA(p->recs.ensure(m * rs, s));
-    GBN_CUDA(p->perm.ensure(m * 4, s));
-    GBN_CUDA(p->bin_count.ensure((size_t)nb * 4, s));
-    GBN_CUDA(p->bin_start.ensure((size_t)nb * 4, s));
-    GBN_CUDA(p->sub_count.ensure((size_t)nb * 4, s));
-    GBN_CUDA(p->sub_start.ensure((size_t)nb * 4, s));
-    GBN_CUDA(p->sub_bin.ensure((size_t)p->st.max_sub * 4, s));
-    GBN_CUDA(p->sub_off.ensure((size_t)p->st.max_sub * 4, s));
-    GBN_CUDA(p->n_sub.ensure(4, s));
-    GBN_CUDA(p->scan_tmp.ensure((size_t)scan_tmp_ints(nb) * 4, s));
+    ps.st.max_sub = nb + (M + g.maxsub - 1) / g.maxsub;
+    GBN_CUDA(ps.recs.ensure(m * rs, s));
+    GBN_CUDA(ps.perm.ensure(m * 4, s));
+    GBN_CUDA(ps.bin_count.ensure((size_t)nb * 4, s));
+    GBN_CUDA(ps.bin_start.ensure((size_t)nb * 4, s));
+    GBN_CUDA(ps.sub_count.ensure((size_t)nb * 4, s));
+    GBN_CUDA(ps.sub_start.ensure((size_t)nb * 4, s));
+    GBN_CUDA(ps.sub_bin.ensure((size_t)ps.st.max_sub * 4, s));
+    GBN_CUDA(ps.sub_off.ensure((size_t)ps.st.max_sub * 4, s));
+    GBN_CUDA(ps.n_sub.ensure(4, s));
+    GBN_CUDA(ps.scan_tmp.ensure((size_t)scan_tmp_ints(nb) * 4, s));
   }
-  fill_sort_state(p);
-  if (p->sorted) GBN_CUDA(cudaMemsetAsync(p->bin_count.p, 0, (size_t)g.nbins * 4, s));
+  fill_sort_state(ps, p->sorted);
+  if (p->sorted) GBN_CUDA(cudaMemsetAsync(ps.bin_count.p, 0, (size_t)g.nbins * 4, s));
   if (p->comp_single) {
-    GBN_CUDA((launch_fold<TX, float>(g, fs, M, x, y, z, p->st, s)));
-    GBN_CUDA(launch_sort_finish<float>(g, M, p->st, p->sorted, s));
+    GBN_CUDA((launch_fold<TX, float>(g, fs, M, x, y, z, ps.st, s)));
+    GBN_CUDA(launch_sort_finish<float>(g, M, ps.st, p->sorted, s));
   } else {
     if (std::is_same<TX, float>::value)
       return fail(GBN_ERR_ARGS, "FP64 compute with float32 points is not supported");
     GBN_CUDA((launch_fold<double, double>(g, fs, M, (const double*)x, (const double*)y,
-                                          (const double*)z, p->st, s)));
-    GBN_CUDA(launch_sort_finish<double>(g, M, p->st, p->sorted, s));
+                                          (const double*)z, ps.st, s)));
+    GBN_CUDA(launch_sort_finish<double>(g, M, ps.st, p->sorted, s));
   }
-  p->M = M;
-  p->pts_set = true;
+  ps.M = M;
+  ps.set = true;
+  ps.dim = p->dim;
+  ps.comp_single = p->comp_single;
+  ps.w = p->w;
+  for (int d = 0; d < 3; ++d) ps.nf[d] = p->nf[d];
   return GBN_OK;
 }
 
-int execute_ntr(gbn_plan_s* p, void* c, void* f, int ntr);
+// A point set is usable with a plan when it was sorted for the same geometry.
+bool points_match(const gbn_plan_s* p, const gbn_points_s& ps) {
+  if (!ps.set || ps.dim != p->dim || ps.comp_single != p->comp_single || ps.w != p->w)
+    return false;
+  for (int d = 0; d < 3; ++d)
+    if (ps.nf[d] != p->nf[d]) return false;
+  return true;
+}
+
+int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int dir);
 
 template <typename TX>
 int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z, int64_t N,
@@ -659,7 +689,7 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
   if (p->type != 3) {
     FoldSpec fs{};
     fs.mode = 0;
-    GBN_TRY(sort_points<TX>(p, M, x, y, z, fs));
+    GBN_TRY(sort_points<TX>(p, p->own, M, x, y, z, fs));
   } else {
     if (N < 0) return fail(GBN_ERR_ARGS, "number of targets must be >= 0");
     if (N > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "too many targets (> 2^31)");
@@ -722,7 +752,7 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
     {
       FoldSpec fs{};
       fs.mode = 0;
-      GBN_TRY(sort_points<double>(p->inner.get(), N, taus[0], taus[1], taus[2], fs));
+      GBN_TRY(sort_points<double>(p->inner.get(), p->inner->own, N, taus[0], taus[1], taus[2], fs));
     }
     // sources -> spreading grid
     {
@@ -732,7 +762,7 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
         fs.center[d] = p->t3_cx[d];
         fs.scale[d] = p->t3_scale[d];
       }
-      GBN_TRY(sort_points<TX>(p, M, x, y, z, fs));
+      GBN_TRY(sort_points<TX>(p, p->own, M, x, y, z, fs));
     }
     const size_t cs = cplx_size(p->comp_single);
     GBN_CUDA(p->t3_pre.ensure((size_t)std::max<int64_t>(M, 1) * cs, st));
@@ -766,37 +796,38 @@ KerSpec<TC> ker_spec(gbn_plan_s* p) {
   return ks;
 }
 
-int do_spread(gbn_plan_s* p, const void* c, int nb, bool c_is_compute) {
+int do_spread(gbn_plan_s* p, gbn_points_s& ps, const void* c, int nb, bool c_is_compute,
+              void* grid) {
   const Geom& g = p->geom;
   cudaError_t e;
   if (p->comp_single) {
     if (p->data_single || c_is_compute)
-      e = launch_spread<float, float>(g, ker_spec<float>(p), p->method, p->M, p->st, c,
-                                      p->fine.p, nb, p->stream);
+      e = launch_spread<float, float>(g, ker_spec<float>(p), p->method, ps.M, ps.st, c, grid, nb,
+                                      p->stream);
     else
-      e = launch_spread<float, double>(g, ker_spec<float>(p), p->method, p->M, p->st, c,
-                                       p->fine.p, nb, p->stream);
+      e = launch_spread<float, double>(g, ker_spec<float>(p), p->method, ps.M, ps.st, c, grid,
+                                       nb, p->stream);
   } else {
-    e = launch_spread<double, double>(g, ker_spec<double>(p), p->method, p->M, p->st, c,
-                                      p->fine.p, nb, p->stream);
+    e = launch_spread<double, double>(g, ker_spec<double>(p), p->method, ps.M, ps.st, c, grid,
+                                      nb, p->stream);
   }
   GBN_CUDA(e);
   return GBN_OK;
 }
 
-int do_interp(gbn_plan_s* p, void* c, int nb) {
+int do_interp(gbn_plan_s* p, gbn_points_s& ps, void* c, int nb, const void* grid) {
   const Geom& g = p->geom;
   cudaError_t e;
   if (p->comp_single) {
     if (p->data_single)
-      e = launch_interp<float, float>(g, ker_spec<float>(p), p->method, p->M, p->st, p->fine.p,
-                                      c, nb, p->stream);
+      e = launch_interp<float, float>(g, ker_spec<float>(p), p->method, ps.M, ps.st, grid, c, nb,
+                                      p->stream);
     else
-      e = launch_interp<float, double>(g, ker_spec<float>(p), p->method, p->M, p->st,
-                                       p->fine.p, c, nb, p->stream);
+      e = launch_interp<float, double>(g, ker_spec<float>(p), p->method, ps.M, ps.st, grid, c,
+                                       nb, p->stream);
   } else {
-    e = launch_interp<double, double>(g, ker_spec<double>(p), p->method, p->M, p->st, p->fine.p,
-                                      c, nb, p->stream);
+    e = launch_interp<double, double>(g, ker_spec<double>(p), p->method, ps.M, ps.st, grid, c,
+                                      nb, p->stream);
   }
   GBN_CUDA(e);
   return GBN_OK;
@@ -832,57 +863,65 @@ void ev_record(cudaEvent_t* ev, int i, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[i], s);
 }
 
-// Execute ntr (<= batch for inner type-2 plans, any for others) transforms.
-int execute_ntr(gbn_plan_s* p, void* c, void* f, int ntr) {
-  if (!p->pts_set) return fail(GBN_ERR_STATE, "execute called before setpts");
+// Execute ntr transforms on point set ps.  dir = +1 runs the plan's own
+// transform; dir = -1 its adjoint with the opposite exponent sign (a type-1
+// plan maps modes f to strengths c like a type-2 transform, a type-2 plan
+// maps c to f like a type-1 transform), reusing the same sort.
+int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int dir) {
+  if (!ps.set) return fail(GBN_ERR_STATE, "execute called before setpts");
+  if (p->type != 3 && !points_match(p, ps))
+    return fail(GBN_ERR_ARGS, "point set was sorted for a different plan geometry");
+  if (p->type == 3 && dir != 1) return fail(GBN_ERR_ARGS, "type-3 plans have no adjoint execute");
   cudaStream_t s = p->stream;
   const size_t dsz = cplx_size(p->data_single);
   const size_t csz = cplx_size(p->comp_single);
+  const int op = dir > 0 ? p->type : (p->type == 1 ? 2 : 1);
+  const int sign = dir > 0 ? p->iflag : -p->iflag;
   GBN_CUDA(p->fine.ensure((size_t)p->batch * p->nftot * csz, s));
   for (int t0 = 0; t0 < ntr; t0 += p->batch) {
     const int nb = std::min(p->batch, ntr - t0);
     cudaEvent_t* ev = p->ev_ok ? take_events(p->ev_exec, p->ev_exec_used, 4) : nullptr;
-    if (p->type == 1) {
-      const char* cb = (const char*)c + (size_t)t0 * p->M * dsz;
+    if (op == 1) {
+      const char* cb = (const char*)c + (size_t)t0 * ps.M * dsz;
       char* fb = (char*)f + (size_t)t0 * p->Ntot * dsz;
       ev_record(ev, 0, s);
       GBN_CUDA(cudaMemsetAsync(p->fine.p, 0, (size_t)nb * p->nftot * csz, s));
-      GBN_TRY(do_spread(p, cb, nb, false));
+      GBN_TRY(do_spread(p, ps, cb, nb, false, p->fine.p));
       ev_record(ev, 1, s);
-      GBN_TRY(exec_fft(p, nb));
+      GBN_TRY(exec_fft(p, p->fine.p, nb, sign));
       ev_record(ev, 2, s);
       GBN_TRY(do_deconv(p, fb, nb, true));
       ev_record(ev, 3, s);
-    } else if (p->type == 2) {
-      char* cb = (char*)c + (size_t)t0 * p->M * dsz;
+    } else if (op == 2) {
+      char* cb = (char*)c + (size_t)t0 * ps.M * dsz;
       const char* fb = (const char*)f + (size_t)t0 * p->Ntot * dsz;
       ev_record(ev, 0, s);
       GBN_TRY(do_deconv(p, (void*)fb, nb, false));
       ev_record(ev, 1, s);
-      GBN_TRY(exec_fft(p, nb));
+      GBN_TRY(exec_fft(p, p->fine.p, nb, sign));
       ev_record(ev, 2, s);
-      GBN_TRY(do_interp(p, cb, nb));
+      GBN_TRY(do_interp(p, ps, cb, nb, p->fine.p));
       ev_record(ev, 3, s);
     } else {
-      const char* cb = (const char*)c + (size_t)t0 * p->M * dsz;
+      const char* cb = (const char*)c + (size_t)t0 * ps.M * dsz;
       char* fb = (char*)f + (size_t)t0 * p->Nt * dsz;
-      GBN_CUDA(p->t3_cbuf.ensure((size_t)p->batch * std::max<int64_t>(p->M, 1) * csz, s));
+      GBN_CUDA(p->t3_cbuf.ensure((size_t)p->batch * std::max<int64_t>(ps.M, 1) * csz, s));
       GBN_CUDA(p->t3_obuf.ensure((size_t)p->batch * std::max<int64_t>(p->Nt, 1) * csz, s));
       ev_record(ev, 0, s);
       cudaError_t e;
       if (p->comp_single)
-        e = p->data_single ? launch_cmul<float, float, float>(p->M, nb, cb, p->t3_pre.p,
+        e = p->data_single ? launch_cmul<float, float, float>(ps.M, nb, cb, p->t3_pre.p,
                                                               p->t3_cbuf.p, s)
-                           : launch_cmul<double, float, float>(p->M, nb, cb, p->t3_pre.p,
+                           : launch_cmul<double, float, float>(ps.M, nb, cb, p->t3_pre.p,
                                                                p->t3_cbuf.p, s);
       else
-        e = launch_cmul<double, double, double>(p->M, nb, cb, p->t3_pre.p, p->t3_cbuf.p, s);
+        e = launch_cmul<double, double, double>(ps.M, nb, cb, p->t3_pre.p, p->t3_cbuf.p, s);
       GBN_CUDA(e);
       GBN_CUDA(cudaMemsetAsync(p->fine.p, 0, (size_t)nb * p->nftot * csz, s));
-      GBN_TRY(do_spread(p, p->t3_cbuf.p, nb, true));
+      GBN_TRY(do_spread(p, ps, p->t3_cbuf.p, nb, true, p->fine.p));
       ev_record(ev, 1, s);
       // inner type 2: modes = spread grid (CMCL order), points = rescaled targets
-      GBN_TRY(execute_ntr(p->inner.get(), p->t3_obuf.p, p->fine.p, nb));
+      GBN_TRY(execute_ntr(p->inner.get(), p->inner->own, p->t3_obuf.p, p->fine.p, nb, 1));
       ev_record(ev, 2, s);
       if (p->comp_single)
         e = p->data_single ? launch_cmul<float, float, float>(p->Nt, nb, p->t3_obuf.p,
@@ -894,6 +933,79 @@ int execute_ntr(gbn_plan_s* p, void* c, void* f, int ntr) {
       GBN_CUDA(e);
       ev_record(ev, 3, s);
     }
+  }
+  GBN_CUDA(cudaGetLastError());
+  return GBN_OK;
+}
+
+// Gradients of a type-1 or type-2 plan on point set ps (see gbn_grad).
+int plan_grad(gbn_plan_s* p, gbn_points_s& ps, int ntr, const void* src, const void* g,
+              void* grad_src, void* const* gx) {
+  if (p->type == 3) return fail(GBN_ERR_ARGS, "gbn_grad supports type-1 and type-2 plans");
+  if (!points_match(p, ps)) return fail(GBN_ERR_ARGS, "point set does not match the plan");
+  if (ntr < 1) return fail(GBN_ERR_ARGS, "ntr must be >= 1");
+  cudaStream_t s = p->stream;
+  const size_t csz = cplx_size(p->comp_single), dsz = cplx_size(p->data_single);
+  const size_t rsz = p->data_single ? 4 : 8;
+  int req[3], nd = 0;
+  for (int d = 0; d < p->dim; ++d)
+    if (gx && gx[d]) req[nd++] = d;
+  void* gxx[3] = {nullptr, nullptr, nullptr};
+  for (int d = 0; d < p->dim; ++d) {
+    gxx[d] = gx ? gx[d] : nullptr;
+    if (gxx[d] && ps.M > 0) GBN_CUDA(cudaMemsetAsync(gxx[d], 0, (size_t)ps.M * rsz, s));
+  }
+  if (p->type == 2 && grad_src) GBN_TRY(execute_ntr(p, ps, (void*)g, grad_src, ntr, -1));
+  const int base = (p->type == 1 && grad_src) ? 1 : 0;
+  const int E = base + nd;
+  if (E == 0 || ps.M == 0) return GBN_OK;
+  int dims[4] = {0, 0, 0, 0};
+  for (int e = base; e < E; ++e) dims[e] = req[e - base];
+  const double grid_bytes = (double)p->nftot * csz * E;
+  int nbmax = (int)std::max(1.0, std::floor(8.0 * (1 << 30) / grid_bytes));
+  if (nbmax > ntr) nbmax = ntr;
+  GBN_CUDA(p->gfine.ensure((size_t)nbmax * E * p->nftot * csz, s));
+  const int mode = p->type == 1 ? 0 : 1;
+  const int sign = p->type == 1 ? -p->iflag : p->iflag;
+  const double a_re = p->type == 1 ? 1.0 : 0.0, a_im = p->type == 1 ? 0.0 : (double)p->iflag;
+  // modes that feed the grids: the cotangent (type 1) or the forward modes (type 2)
+  const char* modes = (const char*)(p->type == 1 ? g : src);
+  const char* wsrc = (const char*)(p->type == 1 ? src : g);
+  for (int t0 = 0; t0 < ntr; t0 += nbmax) {
+    const int nb = std::min(nbmax, ntr - t0);
+    const void* min = modes + (size_t)t0 * p->Ntot * dsz;
+    const void* win = wsrc + (size_t)t0 * ps.M * dsz;
+    void* outc = base ? (void*)((char*)grad_src + (size_t)t0 * ps.M * dsz) : nullptr;
+    cudaError_t e;
+    if (p->comp_single) {
+      const float* phi[3] = {p->phi[0].as<float>(), p->phi[1].as<float>(), p->phi[2].as<float>()};
+      e = p->data_single
+              ? launch_deconv2w<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
+                                              p->gfine.p, nb, E, base, dims, a_re, a_im, s)
+              : launch_deconv2w<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
+                                               p->gfine.p, nb, E, base, dims, a_re, a_im, s);
+    } else {
+      const double* phi[3] = {p->phi[0].as<double>(), p->phi[1].as<double>(),
+                              p->phi[2].as<double>()};
+      e = launch_deconv2w<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
+                                          p->gfine.p, nb, E, base, dims, a_re, a_im, s);
+    }
+    GBN_CUDA(e);
+    GBN_TRY(exec_fft(p, p->gfine.p, nb * E, sign));
+    if (p->comp_single) {
+      e = p->data_single
+              ? launch_interp_grad<float, float>(p->geom, ker_spec<float>(p), ps.M, ps.st,
+                                                 p->gfine.p, nb, E, mode, p->iflag, base, dims,
+                                                 win, outc, gxx, p->method == 2, s)
+              : launch_interp_grad<float, double>(p->geom, ker_spec<float>(p), ps.M, ps.st,
+                                                  p->gfine.p, nb, E, mode, p->iflag, base, dims,
+                                                  win, outc, gxx, p->method == 2, s);
+    } else {
+      e = launch_interp_grad<double, double>(p->geom, ker_spec<double>(p), ps.M, ps.st,
+                                             p->gfine.p, nb, E, mode, p->iflag, base, dims, win,
+                                             outc, gxx, p->method == 2, s);
+    }
+    GBN_CUDA(e);
   }
   GBN_CUDA(cudaGetLastError());
   return GBN_OK;
@@ -1025,9 +1137,11 @@ int run_oneshot(int type, int dim, bool single, void* stream, double eps, int if
     const char* src = (const char*)source;
     char* out = (char*)output;
     if (type == 2)
-      ret = execute_ntr(p, out + (size_t)j * dsz, (void*)(src + (size_t)k * dsz), p->ntransf);
+      ret = execute_ntr(p, p->own, out + (size_t)j * dsz, (void*)(src + (size_t)k * dsz),
+                        p->ntransf, 1);
     else
-      ret = execute_ntr(p, (void*)(src + (size_t)j * dsz), out + (size_t)k * dsz, p->ntransf);
+      ret = execute_ntr(p, p->own, (void*)(src + (size_t)j * dsz), out + (size_t)k * dsz,
+                        p->ntransf, 1);
   }
   if (ret >= 2) {
     delete p;  // state unknown after a failure: do not cache
@@ -1092,7 +1206,7 @@ int gbnf_setpts(gbn_plan plan, int64_t M, const float* x, const float* y, const 
 
 int gbn_execute(gbn_plan plan, void* c, void* f) {
   if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
-  return execute_ntr(plan, c, f, plan->ntransf);
+  return execute_ntr(plan, plan->own, c, f, plan->ntransf, 1);
 }
 
 int gbn_set_stream(gbn_plan plan, void* stream) {
@@ -1152,16 +1266,16 @@ int gbn_get_timings(gbn_plan plan, float* ms5, int* nbatch) {
 int gbn_debug_bins(gbn_plan plan, int64_t* bins_out, int64_t* counts_out, int64_t* nbins) {
   if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
   if (nbins) *nbins = plan->geom.nbins;
-  if (!plan->pts_set || !plan->sorted) return fail(GBN_ERR_STATE, "no sorted points");
+  if (!plan->own.set || !plan->sorted) return fail(GBN_ERR_STATE, "no sorted points");
   GBN_CUDA(cudaStreamSynchronize(plan->stream));
-  if (bins_out && plan->M > 0) {
-    std::vector<int> b((size_t)plan->M);
-    GBN_CUDA(cudaMemcpy(b.data(), plan->pt_bin.p, b.size() * 4, cudaMemcpyDeviceToHost));
+  if (bins_out && plan->own.M > 0) {
+    std::vector<int> b((size_t)plan->own.M);
+    GBN_CUDA(cudaMemcpy(b.data(), plan->own.pt_bin.p, b.size() * 4, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < b.size(); ++i) bins_out[i] = b[i];
   }
   if (counts_out) {
     std::vector<int> b((size_t)plan->geom.nbins);
-    GBN_CUDA(cudaMemcpy(b.data(), plan->bin_count.p, b.size() * 4, cudaMemcpyDeviceToHost));
+    GBN_CUDA(cudaMemcpy(b.data(), plan->own.bin_count.p, b.size() * 4, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < b.size(); ++i) counts_out[i] = b[i];
   }
   return GBN_OK;
@@ -1169,14 +1283,14 @@ int gbn_debug_bins(gbn_plan plan, int64_t* bins_out, int64_t* counts_out, int64_
 
 int gbn_debug_fold(gbn_plan plan, int64_t* i0_out, double* delta_out) {
   if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
-  if (!plan->pts_set) return fail(GBN_ERR_STATE, "no points");
+  if (!plan->own.set) return fail(GBN_ERR_STATE, "no points");
   GBN_CUDA(cudaStreamSynchronize(plan->stream));
   const int dim = plan->dim;
   const size_t rs = rec_size(dim, plan->comp_single);
-  std::vector<unsigned char> raw((size_t)plan->M * rs);
-  if (plan->M > 0)
-    GBN_CUDA(cudaMemcpy(raw.data(), plan->recs_in.p, raw.size(), cudaMemcpyDeviceToHost));
-  for (int64_t j = 0; j < plan->M; ++j) {
+  std::vector<unsigned char> raw((size_t)plan->own.M * rs);
+  if (plan->own.M > 0)
+    GBN_CUDA(cudaMemcpy(raw.data(), plan->own.recs_in.p, raw.size(), cudaMemcpyDeviceToHost));
+  for (int64_t j = 0; j < plan->own.M; ++j) {
     const unsigned char* r = raw.data() + (size_t)j * rs;
     for (int d = 0; d < 3; ++d) {
       int64_t iv = 0;
@@ -1203,6 +1317,42 @@ int gbn_debug_fold(gbn_plan plan, int64_t* i0_out, double* delta_out) {
     }
   }
   return GBN_OK;
+}
+
+int gbn_points_create(gbn_plan plan, int64_t M, const void* x, const void* y, const void* z,
+                      gbn_points* out) {
+  if (!plan || !out) return fail(GBN_ERR_ARGS, "NULL argument");
+  *out = nullptr;
+  if (plan->type == 3) return fail(GBN_ERR_ARGS, "point sets are for type-1 and type-2 plans");
+  std::unique_ptr<gbn_points_s> ps(new gbn_points_s());
+  FoldSpec fs{};
+  fs.mode = 0;
+  int r = plan->data_single
+              ? sort_points<float>(plan, *ps, M, (const float*)x, (const float*)y,
+                                   (const float*)z, fs)
+              : sort_points<double>(plan, *ps, M, (const double*)x, (const double*)y,
+                                    (const double*)z, fs);
+  if (r >= 2) return r;
+  *out = ps.release();
+  return GBN_OK;
+}
+
+int gbn_points_destroy(gbn_points pts) {
+  delete pts;
+  return GBN_OK;
+}
+
+int gbn_execute_points(gbn_plan plan, gbn_points pts, int ntr, int dir, void* c, void* f) {
+  if (!plan || !pts) return fail(GBN_ERR_ARGS, "NULL plan or point set");
+  if (dir != 1 && dir != -1) return fail(GBN_ERR_ARGS, "dir must be +1 or -1");
+  if (ntr < 1) return fail(GBN_ERR_ARGS, "ntr must be >= 1");
+  return execute_ntr(plan, *pts, c, f, ntr, dir);
+}
+
+int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void* g,
+             void* grad_src, void* const* grad_x) {
+  if (!plan || !pts || !src || !g) return fail(GBN_ERR_ARGS, "NULL argument");
+  return plan_grad(plan, *pts, ntr, src, g, grad_src, grad_x);
 }
 
 void gbn_clear_cache(void) { cache().clear(); }

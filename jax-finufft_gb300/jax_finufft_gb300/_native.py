@@ -77,6 +77,10 @@ SIGNATURES = {
     "gbn_last_error": (ctypes.c_char_p, []),
     "gbn_clear_cache": (None, []),
     "gbn_launch_count": (ctypes.c_longlong, []),
+    "gbn_points_create": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "gbn_points_destroy": (ctypes.c_int, [_vp]),
+    "gbn_execute_points": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+    "gbn_grad": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "gbn_binsort_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,
                                            _i64p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                            _vp, _vp, _vp]),

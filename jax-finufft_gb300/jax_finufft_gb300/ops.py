@@ -10,17 +10,26 @@ as torch's conjugate-Wirtinger VJP) and the same vmap batching rule
 (:317-353).  Tensors must live on a CUDA device; every transform runs in
 libgbnufft.so through the C ABI (gbn_run) on the current torch stream.
 
-Reverse mode stacks the d+1 adjoint transforms a gradient needs (strengths
-plus one per coordinate) into ONE native call: one setpts (sort) shared by
-all of them, one batched cuFFT over the stacked grids and one spread/interp
-launch -- the fused adjoint.
+Reverse mode, when a type-1/2 input requires grad, runs the fused adjoint:
+the forward keeps its sorted point sets and the backward calls gbn_grad,
+which builds the d+1 k-weighted grids in one pass, transforms them with one
+batched cuFFT and gathers the strength gradient and every coordinate
+gradient in a single interpolation pass on the forward's sort
+(``Opts(gpu_fused_adjoint=False)`` selects the stacked-transform rules of the
+reference instead; type 3 always uses them).
 """
+import threading
+
 import numpy as np
 import torch
 
-from . import _native
+from . import _fused, _native
 from .options import Opts, to_native, unpack_opts
 from .shapes import broadcast_and_flatten_inputs, check_canonical
+
+# forward -> setup_context hand-off of a fused forward's point sets (torch
+# calls the two back to back on the same thread)
+_tls = threading.local()
 
 __all__ = ["nufft1", "nufft2", "nufft3", "get_frequency_array"]
 
@@ -92,17 +101,57 @@ def _freq_tensor(n, modeord, dim, ndim, like):
     return k.reshape(shape)
 
 
+def _execute_fused(nufft_type, source, points, output_shape, iflag, eps, opts):
+    """Type-1/2 forward that keeps its sorted point sets for the backward."""
+    single = check_canonical(source, points, nufft_type)
+    dev = source.device
+    if dev.type != "cuda" or any(p.device != dev for p in points):
+        raise RuntimeError("jax_finufft_gb300 runs on CUDA tensors only (all inputs on one "
+                           "device); got %s" % ([str(dev)] + [str(p.device) for p in points]))
+    ndim = len(points)
+    n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
+    n_j = int(points[0].shape[1])
+    if nufft_type == 1:
+        out_shape = (n_tot, n_transf) + tuple(int(n) for n in output_shape)
+    else:
+        out_shape = (n_tot, n_transf, n_j)
+    out = torch.empty(out_shape, dtype=source.dtype, device=dev)
+    if out.numel() == 0 or source.numel() == 0 or n_j == 0:
+        return _execute(nufft_type, source, points, output_shape, iflag, eps, opts), None
+    with torch.cuda.device(dev):
+        state = _fused.forward(nufft_type, source, points, output_shape, iflag, eps, opts, out,
+                               single, ndim)
+    return out, state
+
+
+def _wants_fused(nufft_type, opts, source, points):
+    if nufft_type == 3 or not torch.is_grad_enabled():
+        return False
+    fwd = unpack_opts(opts, nufft_type, True)
+    if fwd is not None and not getattr(fwd, "gpu_fused_adjoint", True):
+        return False
+    return bool(source.requires_grad or any(p.requires_grad for p in points))
+
+
 class _Nufft(torch.autograd.Function):
     """One canonical NUFFT call with its VJP, JVP and vmap rules."""
 
     @staticmethod
-    def forward(source, nufft_type, output_shape, iflag, eps, opts, *points):
+    def forward(source, nufft_type, output_shape, iflag, eps, opts, fused, *points):
+        if fused:
+            out, state = _execute_fused(nufft_type, source, points, output_shape, iflag, eps,
+                                        opts)
+            _tls.state = state
+            return out
+        _tls.state = None
         return _execute(nufft_type, source, points, output_shape, iflag, eps, opts)
 
     @staticmethod
     def setup_context(ctx, inputs, output):
-        source, nufft_type, output_shape, iflag, eps, opts, *points = inputs
+        source, nufft_type, output_shape, iflag, eps, opts, fused, *points = inputs
         ctx.cfg = (nufft_type, output_shape, iflag, eps, opts)
+        ctx.fused_state = getattr(_tls, "state", None) if fused else None
+        _tls.state = None
         ctx.save_for_backward(source, *points)
         ctx.save_for_forward(source, *points)
 
@@ -113,8 +162,15 @@ class _Nufft(torch.autograd.Function):
         source, *points = ctx.saved_tensors
         need = ctx.needs_input_grad
         need_src = need[0]
-        need_pts = list(need[6:])
+        need_pts = list(need[7:])
         ndim = len(points) // 2 if nufft_type == 3 else len(points)
+        if ctx.fused_state is not None and not torch.is_grad_enabled():
+            # one fused adjoint on the forward's sort (not differentiable again:
+            # a graph of the backward takes the stacked path below)
+            with torch.cuda.device(source.device):
+                grad_src, gpts = _fused.backward(ctx.fused_state, nufft_type, source, points, g,
+                                                 need_src, need_pts)
+            return (grad_src, None, None, None, None, None, None, *gpts)
         grads_pts = [None] * len(points)
         grad_src = None
         g = g.contiguous()
@@ -127,7 +183,7 @@ class _Nufft(torch.autograd.Function):
                 g * _freq_tensor(output_shape[d], mo, d, ndim, g) for d in dims]
             if stack:
                 G = torch.stack(stack, dim=2).reshape((n_tot, n_tr * len(stack)) + tuple(g.shape[2:]))
-                H = _Nufft.apply(G, 2, None, -iflag, eps, unpack_opts(opts, 2, False), *points)
+                H = _Nufft.apply(G, 2, None, -iflag, eps, unpack_opts(opts, 2, False), False, *points)
                 H = H.reshape(n_tot, n_tr, len(stack), -1)
                 off = 0
                 if need_src:
@@ -141,13 +197,13 @@ class _Nufft(torch.autograd.Function):
             N = tuple(source.shape[2:])
             if need_src:
                 grad_src = _Nufft.apply(g, 1, N, -iflag, eps, unpack_opts(opts, 1, False),
-                                        *points)
+                                        False, *points)
             dims = [d for d in range(ndim) if need_pts[d]]
             if dims:
                 stack = [(1j * iflag) * _freq_tensor(N[d], mo, d, ndim, source) * source
                          for d in dims]
                 A = torch.stack(stack, dim=2).reshape((n_tot, n_tr * len(dims)) + N)
-                H = _Nufft.apply(A, 2, None, iflag, eps, opts, *points)
+                H = _Nufft.apply(A, 2, None, iflag, eps, opts, False, *points)
                 H = H.reshape(n_tot, n_tr, len(dims), -1)
                 for i, d in enumerate(dims):
                     grads_pts[d] = torch.real(torch.conj(g) * H[:, :, i]).sum(dim=1)
@@ -159,7 +215,7 @@ class _Nufft(torch.autograd.Function):
             stack = ([g] if need_src else []) + [g * ss[d][:, None, :] for d in dims_x]
             if stack:
                 G = torch.stack(stack, dim=2).reshape(n_tot, n_tr * len(stack), -1)
-                H = _Nufft.apply(G, 3, None, -iflag, eps, bopts, *ss, *xs)
+                H = _Nufft.apply(G, 3, None, -iflag, eps, bopts, False, *ss, *xs)
                 H = H.reshape(n_tot, n_tr, len(stack), -1)
                 off = 0
                 if need_src:
@@ -171,15 +227,15 @@ class _Nufft(torch.autograd.Function):
             if dims_s:
                 A = torch.stack([(1j * iflag) * xs[d][:, None, :] * source for d in dims_s],
                                 dim=2).reshape(n_tot, n_tr * len(dims_s), -1)
-                H2 = _Nufft.apply(A, 3, None, iflag, eps, opts, *xs, *ss)
+                H2 = _Nufft.apply(A, 3, None, iflag, eps, opts, False, *xs, *ss)
                 H2 = H2.reshape(n_tot, n_tr, len(dims_s), -1)
                 for i, d in enumerate(dims_s):
                     grads_pts[ndim + d] = torch.real(torch.conj(g) * H2[:, :, i]).sum(dim=1)
-        return (grad_src, None, None, None, None, None, *grads_pts)
+        return (grad_src, None, None, None, None, None, None, *grads_pts)
 
     # --- forward mode (ops.py:158-277) ----------------------------------------
     @staticmethod
-    def jvp(ctx, dsource, _t, _o, _i, _e, _p, *dpoints):
+    def jvp(ctx, dsource, _t, _o, _i, _e, _p, _f, *dpoints):
         nufft_type, output_shape, iflag, eps, opts = ctx.cfg
         source, *points = ctx.saved_tensors
         ndim = len(points) // 2 if nufft_type == 3 else len(points)
@@ -202,19 +258,19 @@ class _Nufft(torch.autograd.Function):
                 scales.append((1j * iflag) * _freq_tensor(output_shape[d], mo, d, ndim, source))
             if args:
                 R = _Nufft.apply(torch.stack(args, 2).reshape(n_tot, n_tr * len(args), -1), 1,
-                                 output_shape, iflag, eps, opts, *points)
+                                 output_shape, iflag, eps, opts, False, *points)
                 R = R.reshape((n_tot, n_tr, len(args)) + tuple(output_shape))
                 for i, s in enumerate(scales):
                     out = add(out, R[:, :, i] if s is None else s * R[:, :, i])
         elif nufft_type == 2:
             N = tuple(source.shape[2:])
             if dsource is not None:
-                out = add(out, _Nufft.apply(dsource, 2, None, iflag, eps, opts, *points))
+                out = add(out, _Nufft.apply(dsource, 2, None, iflag, eps, opts, False, *points))
             dims = [d for d in range(ndim) if dpoints[d] is not None]
             if dims:
                 A = torch.stack([(1j * iflag) * _freq_tensor(N[d], mo, d, ndim, source) * source
                                  for d in dims], 2).reshape((n_tot, n_tr * len(dims)) + N)
-                R = _Nufft.apply(A, 2, None, iflag, eps, opts, *points)
+                R = _Nufft.apply(A, 2, None, iflag, eps, opts, False, *points)
                 R = R.reshape(n_tot, n_tr, len(dims), -1)
                 for i, d in enumerate(dims):
                     out = add(out, dpoints[d][:, None, :] * R[:, :, i])
@@ -231,7 +287,7 @@ class _Nufft(torch.autograd.Function):
                 scales.append((1j * iflag) * ss[d][:, None, :])
             if args:
                 R = _Nufft.apply(torch.stack(args, 2).reshape(n_tot, n_tr * len(args), -1), 3,
-                                 None, iflag, eps, opts, *points)
+                                 None, iflag, eps, opts, False, *points)
                 R = R.reshape(n_tot, n_tr, len(args), -1)
                 for i, s in enumerate(scales):
                     out = add(out, R[:, :, i] if s is None else s * R[:, :, i])
@@ -239,7 +295,7 @@ class _Nufft(torch.autograd.Function):
             if dims_s:
                 A = torch.stack([(1j * iflag) * xs[d][:, None, :] * source for d in dims_s],
                                 2).reshape(n_tot, n_tr * len(dims_s), -1)
-                R = _Nufft.apply(A, 3, None, iflag, eps, opts, *points)
+                R = _Nufft.apply(A, 3, None, iflag, eps, opts, False, *points)
                 R = R.reshape(n_tot, n_tr, len(dims_s), -1)
                 for i, d in enumerate(dims_s):
                     out = add(out, dpoints[ndim + d][:, None, :] * R[:, :, i])
@@ -250,16 +306,16 @@ class _Nufft(torch.autograd.Function):
 
     # --- vmap (ops.py:317-353) -------------------------------------------------
     @staticmethod
-    def vmap(info, in_dims, source, nufft_type, output_shape, iflag, eps, opts, *points):
+    def vmap(info, in_dims, source, nufft_type, output_shape, iflag, eps, opts, fused, *points):
         sdim = in_dims[0]
-        pdims = in_dims[6:]
+        pdims = in_dims[7:]
         B = info.batch_size
         if all(d is None for d in pdims):
             # unmapped points: one transform stack of n_transf * B
             src = source.movedim(sdim, 0)
             n_tot, n_tr = src.shape[1], src.shape[2]
             src = src.movedim(0, 1).reshape((n_tot, B * n_tr) + tuple(src.shape[3:]))
-            out = _Nufft.apply(src, nufft_type, output_shape, iflag, eps, opts, *points)
+            out = _Nufft.apply(src, nufft_type, output_shape, iflag, eps, opts, fused, *points)
             out = out.reshape((n_tot, B, n_tr) + tuple(out.shape[2:]))
             return out, 1
         src = source.movedim(sdim, 0) if sdim is not None else source.unsqueeze(0).expand(
@@ -269,7 +325,7 @@ class _Nufft(torch.autograd.Function):
         n_tot = src.shape[1]
         src = src.reshape((B * n_tot,) + tuple(src.shape[2:]))
         pts = [p.reshape((B * n_tot,) + tuple(p.shape[2:])) for p in pts]
-        out = _Nufft.apply(src, nufft_type, output_shape, iflag, eps, opts, *pts)
+        out = _Nufft.apply(src, nufft_type, output_shape, iflag, eps, opts, fused, *pts)
         return out.reshape((B, n_tot) + tuple(out.shape[1:])), 0
 
 
@@ -285,7 +341,8 @@ def nufft1(output_shape, source, *points, iflag=1, eps=1e-6, opts=None):
         raise ValueError(f"output_shape must have shape: ({ndim},)")
     output_shape = tuple(int(n) for n in output_shape)
     index, source, *points = broadcast_and_flatten_inputs(1, output_shape, source, *points)
-    result = _Nufft.apply(source, 1, output_shape, iflag, eps, opts, *points)
+    fused = _wants_fused(1, opts, source, points)
+    result = _Nufft.apply(source, 1, output_shape, iflag, eps, opts, fused, *points)
     return index.unflatten(result)
 
 
@@ -297,7 +354,8 @@ def nufft2(source, *points, iflag=-1, eps=1e-6, opts=None):
     if not 1 <= ndim <= 3:
         raise ValueError("Only 1-, 2-, and 3-dimensions are supported")
     index, source, *points = broadcast_and_flatten_inputs(2, None, source, *points)
-    result = _Nufft.apply(source, 2, None, iflag, eps, opts, *points)
+    fused = _wants_fused(2, opts, source, points)
+    result = _Nufft.apply(source, 2, None, iflag, eps, opts, fused, *points)
     return index.unflatten(result)
 
 
@@ -312,5 +370,5 @@ def nufft3(source, *points, iflag=-1, eps=1e-6, opts=None):
     if not 1 <= ndim <= 3:
         raise ValueError("Only 1-, 2-, and 3-dimensions are supported")
     index, source, *points = broadcast_and_flatten_inputs(3, None, source, *points)
-    result = _Nufft.apply(source, 3, None, iflag, eps, opts, *points)
+    result = _Nufft.apply(source, 3, None, iflag, eps, opts, False, *points)
     return index.unflatten(result)

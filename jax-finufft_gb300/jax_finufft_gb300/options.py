@@ -100,8 +100,11 @@ class Opts:
     gpu_maxbatchsize: int = 0
     gpu_debug: GpuDebugLevel = GpuDebugLevel.Silent
 
-    # GB300 engine extension.
+    # GB300 engine extensions.
     gpu_precision: GpuPrecision = 0
+    # reverse mode through one fused adjoint on the forward's sorted points
+    # (False: the stacked-transform rules of the reference's JVP/transpose)
+    gpu_fused_adjoint: bool = True
 
     def __post_init__(self):
         if int(self.modeord) not in (0, 1):
