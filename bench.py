@@ -341,8 +341,9 @@ def run_ours(args):
     lib.gbn_destroy(p1)
     lib.gbn_destroy(p2)
     if not args.no_extra:
-        result["secondary"] = {"lsq_grad_fwd_bwd": measure_lsq_grad(dev, max(3, args.steps // 2),
-                                                                    args.warmup)}
+        result["secondary"] = {
+            "lsq_grad_fwd_bwd": measure_lsq_grad(dev, max(3, args.steps // 2), args.warmup),
+            "batched_2d": measure_batched(dev, max(3, args.steps // 2), args.warmup)}
     return finish(args, result, rank, ws)
 
 
@@ -439,6 +440,72 @@ def measure_lsq_grad(dev, steps, warmup):
     return out
 
 
+def measure_batched(dev, steps, warmup):
+    """Batched 2D workloads, complex64, eps=1e-6:
+    (a) 32 stacked type-1 transforms sharing M=4e6 uniform points, 512^2 modes;
+    (b) 64 independent type-2 transforms, M_k = floor(10^U(3,6)) points each,
+        modes drawn from {128^2, 256^2, 512^2, 1024^2}.
+    Plain = the per-call path (nufft1 with 32 stacked transforms; 64 nufft2
+    calls); batched = one NufftBatch pass replayed from a CUDA graph.
+    Returns NU points/s/transform for each."""
+    import torch
+
+    import jax_finufft_gb300 as jf
+    from jax_finufft_gb300.batch import NufftBatch
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    rng = np.random.default_rng(SEED + 3)
+    out = {}
+    # (a) stacked transforms sharing points
+    M, N, T = 4_000_000, 512, 32
+    x = [torch.tensor(rng.uniform(-np.pi, np.pi, M).astype(np.float32), device=dev)
+         for _ in range(2)]
+    c = torch.tensor((rng.standard_normal((T, M)) + 1j * rng.standard_normal((T, M)))
+                     .astype(np.complex64), device=dev)
+    ms_plain = timed(lambda: jf.nufft1((N, N), c, *x, eps=1e-6))
+    b = NufftBatch(1, [(N, N)], [M], ntransf=T, eps=1e-6, use_graph=True)
+    P = torch.stack(x)
+    f = b.empty_modes()
+    cb = c.reshape(-1)
+    ms_batch = timed(lambda: b.run_packed(P, cb, f))
+    out["stacked_type1_32x4e6_512sq"] = {
+        "plain_pts_per_s": T * M / (ms_plain * 1e-3), "batched_pts_per_s": T * M / (ms_batch * 1e-3),
+        "plain_ms": ms_plain, "batched_ms": ms_batch}
+    del b, c, f
+    # (b) independent uneven problems
+    K = 64
+    Ms = [int(10 ** rng.uniform(3, 6)) for _ in range(K)]
+    shapes = [(n, n) for n in rng.choice([128, 256, 512, 1024], size=K)]
+    pts = [[torch.tensor(rng.uniform(-np.pi, np.pi, m).astype(np.float32), device=dev)
+            for _ in range(2)] for m in Ms]
+    fs = [torch.tensor((rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64),
+                       device=dev) for s in shapes]
+    ms_plain = timed(lambda: [jf.nufft2(fk, *pk, eps=1e-6) for fk, pk in zip(fs, pts)])
+    b = NufftBatch(2, shapes, Ms, eps=1e-6, use_graph=True)
+    P = b.pack_points(pts)
+    fb = torch.cat([fk.reshape(-1) for fk in fs])
+    cb = b.empty_strengths()
+    ms_batch = timed(lambda: b.run_packed(P, cb, fb))
+    tot = sum(Ms)
+    out["independent_type2_64"] = {
+        "plain_pts_per_s": tot / (ms_plain * 1e-3), "batched_pts_per_s": tot / (ms_batch * 1e-3),
+        "plain_ms": ms_plain, "batched_ms": ms_batch, "total_points": tot,
+        "fft_groups": b.info()["fft_groups"]}
+    return out
+
+
 def finish(args, result, rank, ws):
     import torch
 
@@ -471,6 +538,8 @@ def main():
                     help="skip the secondary measurements (differentiated loss)")
     ap.add_argument("--lsq-only", action="store_true",
                     help="run only the differentiated least-squares measurement")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run only the batched 2D measurement")
     ap.add_argument("--points", type=int, default=M_POINTS,
                     help="points per transform (reduced cases for profiling)")
     ap.add_argument("--modes", type=int, default=N_MODES, help="modes per axis")
@@ -479,11 +548,12 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    if args.lsq_only:
+    if args.lsq_only or args.batched_only:
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps(measure_lsq_grad(torch.device("cuda", 0), args.steps, args.warmup)))
+        fn = measure_lsq_grad if args.lsq_only else measure_batched
+        print(json.dumps(fn(torch.device("cuda", 0), args.steps, args.warmup)))
         return 0
     return run_ours(args)
 

@@ -160,6 +160,37 @@ GBN_API int gbn_execute_points(gbn_plan plan, gbn_points pts, int ntr, int dir, 
 GBN_API int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void* g,
                      void* grad_src, void* const* grad_x);
 
+/*
+ * Batched plans.  No counterpart in the reference, which loops over n_tot
+ * point sets on the host with one plan (lib/kernels.cc.cu:57-80) and needs
+ * one FFI call per independent problem of a different shape.  A batch holds K
+ * independent type-1 or type-2 problems of one dimension and precision, each
+ * with its own points and mode shape (nmodes: K x 3, backend order) and T
+ * transforms.  Data are packed problem after problem:
+ *   points x/y/z: sum_k M_k values, problem k at offset sum_{i<k} M_i;
+ *   strengths/values c: problem k's (T, M_k) block at offset T*sum_{i<k} M_i;
+ *   modes f: problem k's (T, N_k...) block at offset T*sum_{i<k} N_i.
+ * upsampfac (K entries, or NULL for opts->upsampfac) sets sigma per problem.
+ * gbn_batch_run sorts every problem's points and executes all transforms:
+ * per-problem deconvolution, one batched cuFFT per group of equal grid
+ * shapes over a shared grid arena, and one persistent spread (type 1) or
+ * interpolation (type 2) kernel over a work queue of (problem, subproblem,
+ * transform) items.  With use_graph = 1 the whole pass is captured into a
+ * CUDA graph on the first call (after one eager pass, whose results it
+ * returns) and replayed on later calls with the same five pointers.
+ * The batch runs on a stream of its own (capture needs a non-legacy stream),
+ * ordered by events after the work already on `stream` and before the work
+ * queued on `stream` after gbn_batch_run returns.
+ */
+typedef struct gbn_batch_s* gbn_batch;
+GBN_API int gbn_batch_create(int type, int dim, int single, int K, const int64_t* nmodes,
+                             const int64_t* M, const double* upsampfac, int ntransf, int iflag,
+                             double eps, const gbn_opts* opts, void* stream, gbn_batch* out);
+GBN_API int gbn_batch_run(gbn_batch b, const void* x, const void* y, const void* z, void* c,
+                          void* f, int use_graph);
+GBN_API int gbn_batch_info(gbn_batch b, int* ngroups, int* queue, int64_t* arena_bytes);
+GBN_API int gbn_batch_destroy(gbn_batch b);
+
 /* Thread-local message describing the last non-zero status. */
 GBN_API const char* gbn_last_error(void);
 

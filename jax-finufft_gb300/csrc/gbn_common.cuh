@@ -185,6 +185,42 @@ cudaError_t launch_interp_grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                int iflag, int base, const int* dims, const void* w, void* out_c,
                                void* const* gx, bool shared, cudaStream_t s);
 
+// One problem of a batched plan, as the work-queue kernels see it: its
+// geometry, kernel, sorted points, and where its strengths/values (T, M)
+// and its T fine grids live inside the packed arrays.
+template <typename TC>
+struct BatchProb {
+  Geom g;
+  KerSpec<TC> ks;
+  int64_t M;
+  const void* recs;
+  const int* sub_bin;
+  const int* sub_off;
+  const int* n_sub;
+  const int* bin_start;
+  const int* bin_count;
+  const int* perm;
+  int64_t c_off;     // element offset of the problem's (T, M) block
+  int64_t grid_off;  // element offset of its T grids in the arena
+  int64_t nftot;
+};
+
+// item_start[k] = T * sum_{i<k} n_sub_i for k = 0..K (device, one block).
+template <typename TC>
+cudaError_t launch_item_prefix(const BatchProb<TC>* probs, int K, int T, int64_t* item_start,
+                               cudaStream_t s);
+
+// Persistent spread/interp over every (problem, subproblem, transform) item
+// of a batch, pulled from one atomic counter (reset by the caller).
+template <typename TC, typename TD>
+cudaError_t launch_spread_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+                                const int64_t* item_start, int* counter, int T, const void* c,
+                                void* arena, size_t smem, cudaStream_t s);
+template <typename TC, typename TD>
+cudaError_t launch_interp_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+                                const int64_t* item_start, int* counter, int T,
+                                const void* arena, void* c, size_t smem, cudaStream_t s);
+
 // out[t, j] = in[t, j] * fac[j] (complex), ntr transforms of length n.
 template <typename TI, typename TO, typename TF>
 cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, void* out,

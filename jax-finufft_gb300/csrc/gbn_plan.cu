@@ -833,27 +833,27 @@ int do_interp(gbn_plan_s* p, gbn_points_s& ps, void* c, int nb, const void* grid
   return GBN_OK;
 }
 
-int do_deconv(gbn_plan_s* p, void* modes, int nb, bool to_modes) {
+int do_deconv(gbn_plan_s* p, void* modes, int nb, bool to_modes, void* grid) {
   cudaError_t e;
   if (p->comp_single) {
     const float* phi[3] = {p->phi[0].as<float>(), p->phi[1].as<float>(), p->phi[2].as<float>()};
     if (p->data_single)
       e = to_modes ? launch_deconv1<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi,
-                                                  p->fine.p, modes, nb, p->stream)
+                                                  grid, modes, nb, p->stream)
                    : launch_deconv2<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi,
-                                                  modes, p->fine.p, nb, p->stream);
+                                                  modes, grid, nb, p->stream);
     else
       e = to_modes ? launch_deconv1<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
-                                                   p->fine.p, modes, nb, p->stream)
+                                                   grid, modes, nb, p->stream)
                    : launch_deconv2<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
-                                                   modes, p->fine.p, nb, p->stream);
+                                                   modes, grid, nb, p->stream);
   } else {
     const double* phi[3] = {p->phi[0].as<double>(), p->phi[1].as<double>(),
                             p->phi[2].as<double>()};
     e = to_modes ? launch_deconv1<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
-                                                  p->fine.p, modes, nb, p->stream)
+                                                  grid, modes, nb, p->stream)
                  : launch_deconv2<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi,
-                                                  modes, p->fine.p, nb, p->stream);
+                                                  modes, grid, nb, p->stream);
   }
   GBN_CUDA(e);
   return GBN_OK;
@@ -890,13 +890,13 @@ int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int 
       ev_record(ev, 1, s);
       GBN_TRY(exec_fft(p, p->fine.p, nb, sign));
       ev_record(ev, 2, s);
-      GBN_TRY(do_deconv(p, fb, nb, true));
+      GBN_TRY(do_deconv(p, fb, nb, true, p->fine.p));
       ev_record(ev, 3, s);
     } else if (op == 2) {
       char* cb = (char*)c + (size_t)t0 * ps.M * dsz;
       const char* fb = (const char*)f + (size_t)t0 * p->Ntot * dsz;
       ev_record(ev, 0, s);
-      GBN_TRY(do_deconv(p, (void*)fb, nb, false));
+      GBN_TRY(do_deconv(p, (void*)fb, nb, false, p->fine.p));
       ev_record(ev, 1, s);
       GBN_TRY(exec_fft(p, p->fine.p, nb, sign));
       ev_record(ev, 2, s);
@@ -1466,3 +1466,338 @@ int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x, const 
 }  // extern "C"
 
 int gbn::set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+// =============================================================================
+// batched plans: K independent problems (own points, own mode shape) of one
+// type/dimension/precision, T transforms each, in packed arrays.
+// =============================================================================
+struct gbn_batch_s {
+  int type = 1, dim = 1, K = 0, T = 1, iflag = 1;
+  bool data_single = true, comp_single = true;
+  cudaStream_t user = nullptr;    // the caller's stream
+  cudaStream_t stream = nullptr;  // the batch's own stream (capturable; joined to `user`)
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  std::vector<std::unique_ptr<gbn_plan_s>> sub;  // geometry, kernel, deconvolution, points
+  std::vector<int64_t> M, pt_off, c_off, f_off, grid_off;
+  struct Group {
+    int first;  // problem whose plan runs the group's FFT
+    int count;  // problems in the group (T grids each)
+    int64_t off;
+  };
+  std::vector<Group> groups;
+  DevBuf arena, probs, item_start, counter;
+  std::vector<unsigned char> probs_host;  // last uploaded table (stays alive for the copy)
+  bool queue = true, wide = false;
+  size_t smem = 0;
+  cudaGraphExec_t gexec = nullptr;
+  const void* gkey[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+
+  ~gbn_batch_s() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    DevBuf* bufs[] = {&arena, &probs, &item_start, &counter};
+    for (DevBuf* b : bufs) b->release(stream);
+    sub.clear();
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+  }
+};
+
+namespace {
+
+int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, const int64_t* M,
+                 const double* sigma, int T, int iflag, double eps, const gbn_opts* opts,
+                 void* stream, gbn_batch_s** out) {
+  *out = nullptr;
+  if (type != 1 && type != 2) return fail(GBN_ERR_ARGS, "batched plans support types 1 and 2");
+  if (K < 1) return fail(GBN_ERR_ARGS, "K must be >= 1");
+  if (T < 1) return fail(GBN_ERR_ARGS, "ntransf must be >= 1");
+  std::unique_ptr<gbn_batch_s> b(new gbn_batch_s());
+  b->type = type;
+  b->dim = dim;
+  b->K = K;
+  b->T = T;
+  b->iflag = iflag >= 0 ? 1 : -1;
+  b->data_single = single;
+  b->user = (cudaStream_t)stream;
+  GBN_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  GBN_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming));
+  GBN_CUDA(cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming));
+  gbn_opts base;
+  if (opts)
+    base = *opts;
+  else
+    gbn_default_opts(&base);
+  int warn = 0;
+  int64_t pts = 0, modes = 0;
+  for (int k = 0; k < K; ++k) {
+    gbn_opts o = base;
+    if (sigma && sigma[k] > 0.0) o.upsampfac = sigma[k];
+    o.gpu_maxbatchsize = T;
+    o.debug = 0;
+    gbn_plan_s* p = nullptr;
+    int r = plan_create(type, dim, nmodes + 3 * k, iflag, T, eps, single, &o, (void*)b->stream,
+                        &p);
+    if (r >= 2) return r;
+    warn |= r;
+    b->sub.emplace_back(p);
+    if (p->method != 2 || !p->sorted) b->queue = false;
+    b->comp_single = p->comp_single;
+    if (p->w > 8) b->wide = true;
+    const size_t tb = tile_bytes(dim, p->geom.bs, p->w, p->comp_single);
+    b->smem = std::max(b->smem, tb);
+    if (M[k] < 0) return fail(GBN_ERR_ARGS, "negative number of points");
+    b->M.push_back(M[k]);
+    b->pt_off.push_back(pts);
+    b->c_off.push_back(pts * T);
+    b->f_off.push_back(modes * T);
+    pts += M[k];
+    modes += p->Ntot;
+  }
+  // group problems by fine-grid shape: each group's grids are contiguous
+  b->grid_off.assign(K, 0);
+  std::vector<bool> placed(K, false);
+  int64_t off = 0;
+  for (int k = 0; k < K; ++k) {
+    if (placed[k]) continue;
+    gbn_batch_s::Group g{k, 0, off};
+    for (int j = k; j < K; ++j) {
+      if (placed[j]) continue;
+      const gbn_plan_s* a = b->sub[k].get();
+      const gbn_plan_s* c = b->sub[j].get();
+      if (a->nf[0] != c->nf[0] || a->nf[1] != c->nf[1] || a->nf[2] != c->nf[2]) continue;
+      placed[j] = true;
+      b->grid_off[j] = off;
+      off += (int64_t)T * c->nftot;
+      ++g.count;
+    }
+    b->groups.push_back(g);
+  }
+  const size_t csz = cplx_size(b->comp_single);
+  cudaStream_t s = b->stream;
+  GBN_CUDA(b->arena.ensure((size_t)off * csz, s));
+  GBN_CUDA(b->item_start.ensure((size_t)(K + 1) * sizeof(int64_t), s));
+  GBN_CUDA(b->counter.ensure(sizeof(int), s));
+  *out = b.release();
+  return warn ? GBN_WARN_EPS_TOO_SMALL : GBN_OK;
+}
+
+template <typename TC>
+void fill_probs(gbn_batch_s* b, std::vector<unsigned char>& host) {
+  host.assign(sizeof(BatchProb<TC>) * b->K, 0);
+  BatchProb<TC>* pr = reinterpret_cast<BatchProb<TC>*>(host.data());
+  for (int k = 0; k < b->K; ++k) {
+    gbn_plan_s* p = b->sub[k].get();
+    BatchProb<TC>& q = pr[k];
+    q.g = p->geom;
+    q.ks = ker_spec<TC>(p);
+    q.M = p->own.M;
+    q.recs = p->own.st.recs;
+    q.sub_bin = p->own.st.sub_bin;
+    q.sub_off = p->own.st.sub_off;
+    q.n_sub = p->own.st.n_sub;
+    q.bin_start = p->own.st.bin_start;
+    q.bin_count = p->own.st.bin_count;
+    q.perm = p->own.st.perm;
+    q.c_off = b->c_off[k];
+    q.grid_off = b->grid_off[k];
+    q.nftot = p->nftot;
+  }
+}
+
+// Sort every problem's points and refresh the work-queue table.
+template <typename TX>
+int batch_setpts(gbn_batch_s* b, const TX* x, const TX* y, const TX* z) {
+  cudaStream_t s = b->stream;
+  FoldSpec fs{};
+  fs.mode = 0;
+  for (int k = 0; k < b->K; ++k) {
+    const int64_t o = b->pt_off[k];
+    GBN_TRY(sort_points<TX>(b->sub[k].get(), b->sub[k]->own, b->M[k], x ? x + o : nullptr,
+                            y ? y + o : nullptr, z ? z + o : nullptr, fs));
+  }
+  if (!b->queue) return GBN_OK;
+  std::vector<unsigned char> host;
+  if (b->comp_single)
+    fill_probs<float>(b, host);
+  else
+    fill_probs<double>(b, host);
+  if (host != b->probs_host) {  // pointers change only when point buffers grow
+    cudaStreamCaptureStatus cs;
+    GBN_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(GBN_ERR_STATE, "batched point buffers changed during graph capture");
+    b->probs_host.swap(host);
+    GBN_CUDA(b->probs.ensure(b->probs_host.size(), s));
+    GBN_CUDA(cudaMemcpyAsync(b->probs.p, b->probs_host.data(), b->probs_host.size(),
+                             cudaMemcpyHostToDevice, s));
+  }
+  cudaError_t e = b->comp_single
+                      ? launch_item_prefix<float>((const BatchProb<float>*)b->probs.p, b->K,
+                                                  b->T, b->item_start.as<int64_t>(), s)
+                      : launch_item_prefix<double>((const BatchProb<double>*)b->probs.p, b->K,
+                                                   b->T, b->item_start.as<int64_t>(), s);
+  GBN_CUDA(e);
+  return GBN_OK;
+}
+
+int batch_execute(gbn_batch_s* b, void* c, void* f) {
+  cudaStream_t s = b->stream;
+  const size_t dsz = cplx_size(b->data_single), csz = cplx_size(b->comp_single);
+  char* arena = (char*)b->arena.p;
+  if (!b->queue) {  // a problem needs global-memory atomics: run problems one by one
+    for (int k = 0; k < b->K; ++k) {
+      gbn_plan_s* p = b->sub[k].get();
+      GBN_TRY(execute_ntr(p, p->own, (char*)c + b->c_off[k] * dsz, (char*)f + b->f_off[k] * dsz,
+                          b->T, 1));
+    }
+    return GBN_OK;
+  }
+  if (b->type == 2) {
+    for (int k = 0; k < b->K; ++k)
+      GBN_TRY(do_deconv(b->sub[k].get(), (char*)f + b->f_off[k] * dsz, b->T, false,
+                        arena + b->grid_off[k] * csz));
+    for (const auto& g : b->groups)
+      GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
+    GBN_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(int), s));
+    cudaError_t e;
+    if (b->comp_single)
+      e = b->data_single
+              ? launch_interp_queue<float, float>(b->dim, b->wide,
+                                                  (const BatchProb<float>*)b->probs.p, b->K,
+                                                  b->item_start.as<int64_t>(),
+                                                  b->counter.as<int>(), b->T, arena, c, b->smem, s)
+              : launch_interp_queue<float, double>(b->dim, b->wide,
+                                                   (const BatchProb<float>*)b->probs.p, b->K,
+                                                   b->item_start.as<int64_t>(),
+                                                   b->counter.as<int>(), b->T, arena, c, b->smem,
+                                                   s);
+    else
+      e = launch_interp_queue<double, double>(b->dim, b->wide,
+                                              (const BatchProb<double>*)b->probs.p, b->K,
+                                              b->item_start.as<int64_t>(), b->counter.as<int>(),
+                                              b->T, arena, c, b->smem, s);
+    GBN_CUDA(e);
+  } else {
+    GBN_CUDA(cudaMemsetAsync(arena, 0, b->arena.n, s));
+    GBN_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(int), s));
+    cudaError_t e;
+    if (b->comp_single)
+      e = b->data_single
+              ? launch_spread_queue<float, float>(b->dim, b->wide,
+                                                  (const BatchProb<float>*)b->probs.p, b->K,
+                                                  b->item_start.as<int64_t>(),
+                                                  b->counter.as<int>(), b->T, c, arena, b->smem, s)
+              : launch_spread_queue<float, double>(b->dim, b->wide,
+                                                   (const BatchProb<float>*)b->probs.p, b->K,
+                                                   b->item_start.as<int64_t>(),
+                                                   b->counter.as<int>(), b->T, c, arena, b->smem,
+                                                   s);
+    else
+      e = launch_spread_queue<double, double>(b->dim, b->wide,
+                                              (const BatchProb<double>*)b->probs.p, b->K,
+                                              b->item_start.as<int64_t>(), b->counter.as<int>(),
+                                              b->T, c, arena, b->smem, s);
+    GBN_CUDA(e);
+    for (const auto& g : b->groups)
+      GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
+    for (int k = 0; k < b->K; ++k)
+      GBN_TRY(do_deconv(b->sub[k].get(), (char*)f + b->f_off[k] * dsz, b->T, true,
+                        arena + b->grid_off[k] * csz));
+  }
+  GBN_CUDA(cudaGetLastError());
+  return GBN_OK;
+}
+
+int batch_pass(gbn_batch_s* b, const void* x, const void* y, const void* z, void* c, void* f) {
+  if (b->data_single) {
+    GBN_TRY(batch_setpts<float>(b, (const float*)x, (const float*)y, (const float*)z));
+  } else {
+    GBN_TRY(batch_setpts<double>(b, (const double*)x, (const double*)y, (const double*)z));
+  }
+  return batch_execute(b, c, f);
+}
+
+int batch_run_on_own(gbn_batch_s* b, const void* x, const void* y, const void* z, void* c,
+                     void* f, int use_graph);
+
+// Work runs on the batch's own stream, ordered after everything already on
+// the caller's stream and before anything the caller enqueues next.
+int batch_run(gbn_batch_s* b, const void* x, const void* y, const void* z, void* c, void* f,
+              int use_graph) {
+  GBN_CUDA(cudaEventRecord(b->ev_in, b->user));
+  GBN_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
+  const int r = batch_run_on_own(b, x, y, z, c, f, use_graph);
+  GBN_CUDA(cudaEventRecord(b->ev_out, b->stream));
+  GBN_CUDA(cudaStreamWaitEvent(b->user, b->ev_out, 0));
+  return r;
+}
+
+int batch_run_on_own(gbn_batch_s* b, const void* x, const void* y, const void* z, void* c,
+                     void* f, int use_graph) {
+  if (!use_graph) return batch_pass(b, x, y, z, c, f);
+  const void* key[5] = {x, y, z, c, f};
+  const bool same = b->gexec && std::memcmp(key, b->gkey, sizeof(key)) == 0;
+  if (same) {
+    GBN_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    return GBN_OK;
+  }
+  // an eager pass sizes every buffer and creates every cuFFT plan, so the
+  // captured pass allocates nothing; its results are the call's results
+  GBN_TRY(batch_pass(b, x, y, z, c, f));
+  if (b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  GBN_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int r = batch_pass(b, x, y, z, c, f);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (r >= 2) {
+    if (graph) cudaGraphDestroy(graph);
+    return r;
+  }
+  GBN_CUDA(e);
+  e = cudaGraphInstantiate(&b->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  GBN_CUDA(e);
+  std::memcpy(b->gkey, key, sizeof(key));
+  return GBN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbn_batch_create(int type, int dim, int single, int K, const int64_t* nmodes,
+                     const int64_t* M, const double* upsampfac, int ntransf, int iflag,
+                     double eps, const gbn_opts* opts, void* stream, gbn_batch* out) {
+  if (!out || !nmodes || !M) return fail(GBN_ERR_ARGS, "NULL argument");
+  return batch_create(type, dim, single != 0, K, nmodes, M, upsampfac, ntransf, iflag, eps, opts,
+                      stream, out);
+}
+
+int gbn_batch_run(gbn_batch b, const void* x, const void* y, const void* z, void* c, void* f,
+                  int use_graph) {
+  if (!b) return fail(GBN_ERR_ARGS, "NULL batch");
+  return batch_run(b, x, y, z, c, f, use_graph);
+}
+
+int gbn_batch_info(gbn_batch b, int* ngroups, int* queue, int64_t* arena_bytes) {
+  if (!b) return fail(GBN_ERR_ARGS, "NULL batch");
+  if (ngroups) *ngroups = (int)b->groups.size();
+  if (queue) *queue = b->queue ? 1 : 0;
+  if (arena_bytes) *arena_bytes = (int64_t)b->arena.n;
+  return GBN_OK;
+}
+
+int gbn_batch_destroy(gbn_batch b) {
+  delete b;
+  return GBN_OK;
+}
+
+}  // extern "C"

@@ -441,6 +441,47 @@ __global__ void cmul_kernel(int64_t n, int ntr, const cplx_t<TI>* __restrict__ i
   }
 }
 
+// item_start[k] = T * sum_{i<k} n_sub_i, k = 0..K, one block of 1024 threads
+// walking the problems in chunks with a running carry.
+template <typename TC>
+__global__ void item_prefix_kernel(const BatchProb<TC>* __restrict__ probs, int K, int T,
+                                   int64_t* __restrict__ out) {
+  __shared__ int64_t warp_sums[32];
+  __shared__ int64_t carry_s;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k0 = 0; k0 < K; k0 += blockDim.x) {
+    const int k = k0 + threadIdx.x;
+    const int64_t v = k < K ? (int64_t)(*probs[k].n_sub) * T : 0;
+    int64_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t n = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += n;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const int64_t ws = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+      int64_t wi = ws;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t n = __shfl_up_sync(0xffffffffu, wi, o);
+        if (lane >= o) wi += n;
+      }
+      warp_sums[lane] = wi - ws;
+    }
+    __syncthreads();
+    const int64_t carry = carry_s;
+    if (k < K) out[k] = carry + incl - v + warp_sums[warp];
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry_s = carry + incl + warp_sums[warp];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[K] = carry_s;
+}
+
 inline unsigned grid1(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 }  // namespace
@@ -717,6 +758,18 @@ cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, voi
   note_launch();
   return cudaGetLastError();
 }
+
+template <typename TC>
+cudaError_t launch_item_prefix(const BatchProb<TC>* probs, int K, int T, int64_t* item_start,
+                               cudaStream_t s) {
+  item_prefix_kernel<TC><<<1, 1024, 0, s>>>(probs, K, T, item_start);
+  note_launch();
+  return cudaGetLastError();
+}
+template cudaError_t launch_item_prefix<float>(const BatchProb<float>*, int, int, int64_t*,
+                                               cudaStream_t);
+template cudaError_t launch_item_prefix<double>(const BatchProb<double>*, int, int, int64_t*,
+                                                cudaStream_t);
 
 // explicit instantiations
 #define GBN_INST_FOLD(TX, TC)                                                                 \

@@ -71,11 +71,15 @@ struct Acc<float> {
 __device__ __forceinline__ void acc_add(int* p, float v) { atomicAdd(p, __float2int_rn(v)); }
 __device__ __forceinline__ void acc_add(double* p, double v) { atomicAdd(p, v); }
 
+// One subproblem of one transform, executed by the whole block (shared by
+// the per-subproblem kernel and the work-queue kernel of batched plans).
 template <typename TC, typename TD, int DIM, int G>
-__global__ void __launch_bounds__(kThreads)
-    spread_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
-                     SubArgs sa, const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ fine,
-                     int64_t nftot) {
+__device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                                                const PtRec<TC, DIM>* __restrict__ recs,
+                                                const SubArgs& sa, int sub, int t,
+                                                const cplx_t<TD>* __restrict__ c,
+                                                cplx_t<TC>* __restrict__ fine, int64_t nftot,
+                                                unsigned char* smem_raw) {
   using A = typename Acc<TC>::type;
   constexpr bool kFixed = sizeof(A) == 4 && sizeof(TC) == 4;
   constexpr int NCO = GroupCfg<G>::NCO;
@@ -83,11 +87,9 @@ __global__ void __launch_bounds__(kThreads)
   constexpr int NWARP = kThreads / 32;
   __shared__ TC s_red[NWARP];
   int start, cnt, bin;
-  if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
-  const int t = blockIdx.y;
+  if (!sub_range(sa, g, M, sub, start, cnt, bin)) return;
   const int w = g.w;
   const Tile<DIM> tl(g, bin);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   A* sre = reinterpret_cast<A*>(smem_raw);
   A* sim = sre + tl.ncell;
   for (int i = threadIdx.x; i < tl.ncell; i += kThreads) {
@@ -188,6 +190,16 @@ __global__ void __launch_bounds__(kThreads)
 
 template <typename TC, typename TD, int DIM, int G>
 __global__ void __launch_bounds__(kThreads)
+    spread_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
+                     SubArgs sa, const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ fine,
+                     int64_t nftot) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  spread_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, c, fine, nftot,
+                                  smem_raw);
+}
+
+template <typename TC, typename TD, int DIM, int G>
+__global__ void __launch_bounds__(kThreads)
     spread_gm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
                      SubArgs sa, const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ fine,
                      int64_t nftot) {
@@ -240,6 +252,57 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
   }
+}
+
+
+template <typename TC, typename TD, int DIM, int G>
+__global__ void __launch_bounds__(kThreads)
+    spread_queue_kernel(const BatchProb<TC>* __restrict__ probs, int K,
+                        const int64_t* __restrict__ item_start, int* counter, int T,
+                        const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ arena) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  const int64_t total = item_start[K];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int64_t item = s_item;
+    if (item >= total) break;
+    int lo = 0, hi = K - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (item_start[mid] <= item)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const BatchProb<TC> P = probs[lo];
+    const int64_t local = item - item_start[lo];
+    const int sub = (int)(local / T), t = (int)(local - (int64_t)sub * T);
+    SubArgs sa{P.sub_bin, P.sub_off, P.n_sub, P.bin_start, P.bin_count, P.perm, 1};
+    spread_sm_block<TC, TD, DIM, G>(P.g, P.ks, P.M, (const PtRec<TC, DIM>*)P.recs, sa, sub, t,
+                                    c + P.c_off, arena + P.grid_off, P.nftot, smem_raw);
+  }
+}
+
+template <typename TC, typename TD, int DIM, int G>
+cudaError_t run_spread_queue(const BatchProb<TC>* probs, int K, const int64_t* item_start,
+                             int* counter, int T, const void* c, void* arena, size_t smem,
+                             cudaStream_t s) {
+  auto kern = spread_queue_kernel<TC, TD, DIM, G>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  kern<<<nsm * per_sm, kThreads, smem, s>>>(probs, K, item_start, counter, T,
+                                            (const cplx_t<TD>*)c, (cplx_t<TC>*)arena);
+  note_launch();
+  return cudaGetLastError();
 }
 
 template <typename TC, typename TD, int DIM, int G>
@@ -315,5 +378,33 @@ template cudaError_t launch_spread<float, double>(const Geom&, const KerSpec<flo
 template cudaError_t launch_spread<double, double>(const Geom&, const KerSpec<double>&, int,
                                                    int64_t, const SortState&, const void*,
                                                    void*, int, cudaStream_t);
+
+
+template <typename TC, typename TD>
+cudaError_t launch_spread_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+                                const int64_t* item_start, int* counter, int T, const void* c,
+                                void* arena, size_t smem, cudaStream_t s) {
+  if (K == 0) return cudaSuccess;
+  switch (dim) {
+    case 1:
+      return wide ? run_spread_queue<TC, TD, 1, 16>(probs, K, item_start, counter, T, c, arena, smem, s)
+                  : run_spread_queue<TC, TD, 1, 8>(probs, K, item_start, counter, T, c, arena, smem, s);
+    case 2:
+      return wide ? run_spread_queue<TC, TD, 2, 16>(probs, K, item_start, counter, T, c, arena, smem, s)
+                  : run_spread_queue<TC, TD, 2, 8>(probs, K, item_start, counter, T, c, arena, smem, s);
+    default:
+      return wide ? run_spread_queue<TC, TD, 3, 16>(probs, K, item_start, counter, T, c, arena, smem, s)
+                  : run_spread_queue<TC, TD, 3, 8>(probs, K, item_start, counter, T, c, arena, smem, s);
+  }
+}
+
+#define GBN_INST_SQ(TC, TD)                                                                  \
+  template cudaError_t launch_spread_queue<TC, TD>(int, bool, const BatchProb<TC>*, int,     \
+                                                   const int64_t*, int*, int, const void*,   \
+                                                   void*, size_t, cudaStream_t);
+GBN_INST_SQ(float, float)
+GBN_INST_SQ(float, double)
+GBN_INST_SQ(double, double)
+
 
 }  // namespace gbn

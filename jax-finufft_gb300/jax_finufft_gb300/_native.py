@@ -81,6 +81,14 @@ SIGNATURES = {
     "gbn_points_destroy": (ctypes.c_int, [_vp]),
     "gbn_execute_points": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "gbn_grad": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "gbn_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        _i64p, _i64p, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.POINTER(GbnOpts), _vp, ctypes.POINTER(_vp)]),
+    "gbn_batch_run": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    "gbn_batch_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int), _i64p]),
+    "gbn_batch_destroy": (ctypes.c_int, [_vp]),
     "gbn_binsort_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,
                                            _i64p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                            _vp, _vp, _vp]),
