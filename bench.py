@@ -306,6 +306,7 @@ def run_ours(args):
     if not args.no_e2e:
         e2e_value, e2e_ms = run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws,
                                     barrier, max_over_ranks)
+    accuracy = round_trip_errors(dev, pts_h, f, c, g, N)
     peak, peak_kind = measured_peak()
     alg = algorithmic_bytes(M, nf_total)
     spread_ms, interp_ms = t1[0], t2[0]
@@ -329,6 +330,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                 "path": "gbn_nufft3d2f + gbn_nufft3d1f (C ABI), pinned host buffers"},
         "gpu_launches": int(launches),
+        "accuracy": accuracy,
         "stages_ms": {"type2": {"setpts": t2[4], "deconv": t2[2], "fft": t2[1], "interp": t2[0]},
                       "type1": {"setpts": t1[4], "spread": t1[0], "fft": t1[1],
                                 "deconv": t1[2]}},
@@ -343,7 +345,9 @@ def run_ours(args):
     if not args.no_extra:
         result["secondary"] = {
             "lsq_grad_fwd_bwd": measure_lsq_grad(dev, max(3, args.steps // 2), args.warmup),
-            "batched_2d": measure_batched(dev, max(3, args.steps // 2), args.warmup)}
+            "batched_2d": measure_batched(dev, max(3, args.steps // 2), args.warmup),
+            "plain_2d_type1": measure_plain2d(dev, args.steps, args.warmup, cpu=not args.no_cpu),
+            "type3_3d": measure_type3(dev, max(3, args.steps // 2), args.warmup)}
     return finish(args, result, rank, ws)
 
 
@@ -387,6 +391,199 @@ def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, max_over_
     barrier()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     return ws * 2 * M / (e2e_ms * 1e-3), e2e_ms
+
+
+def _freqs(n, like):
+    import torch
+
+    return torch.arange(-(n // 2), (n + 1) // 2, dtype=torch.float64, device=like.device)
+
+
+def direct_type2_subset(f, pts, idx, iflag):
+    """FP64 c_j = sum_k f_k exp(iflag i k.x_j) for the points idx (user axis
+    order: pts[u] pairs with mode axis u), by separable contraction on the GPU."""
+    import torch
+
+    f = f.to(torch.complex128)
+    x = [p[idx].to(torch.float64) for p in pts]
+    d = f.dim()
+    E = [torch.exp(1j * iflag * torch.outer(_freqs(f.shape[u], f), x[u])) for u in range(d)]
+    g = (f.reshape(-1, f.shape[-1]) @ E[-1]).reshape(*f.shape[:-1], -1)  # (..., m)
+    for u in range(d - 2, -1, -1):
+        shp = [1] * (u + 2)
+        shp[u] = f.shape[u]
+        shp[-1] = -1
+        g = (g * E[u].reshape(shp)).sum(dim=u)
+    return g
+
+
+def direct_type1_subset(c, pts, kidx, n_modes, iflag, chunk=100_000):
+    """FP64 f_k = sum_j c_j exp(iflag i k.x_j) for the mode multi-indices
+    kidx (m x d, storage order, modeord 0), chunked over points on the GPU."""
+    import torch
+
+    ks = [(kidx[:, u] - n_modes[u] // 2).to(torch.float64) for u in range(len(n_modes))]
+    out = torch.zeros(kidx.shape[0], dtype=torch.complex128, device=c.device)
+    M = c.shape[-1]
+    for lo in range(0, M, chunk):
+        hi = min(M, lo + chunk)
+        ph = torch.zeros((kidx.shape[0], hi - lo), dtype=torch.float64, device=c.device)
+        for u, k in enumerate(ks):
+            ph += torch.outer(k, pts[u][lo:hi].to(torch.float64))
+        out += torch.exp(1j * iflag * ph) @ c[lo:hi].to(torch.complex128)
+    return out
+
+
+def direct_type3_subset(c, src, tgt, tidx, iflag, chunk=100_000):
+    """FP64 f_k = sum_j c_j exp(iflag i s_k.x_j) for the targets tidx."""
+    import torch
+
+    s = [t[tidx].to(torch.float64) for t in tgt]
+    out = torch.zeros(len(tidx), dtype=torch.complex128, device=c.device)
+    M = c.shape[-1]
+    for lo in range(0, M, chunk):
+        hi = min(M, lo + chunk)
+        ph = torch.zeros((len(tidx), hi - lo), dtype=torch.float64, device=c.device)
+        for u in range(len(src)):
+            ph += torch.outer(s[u], src[u][lo:hi].to(torch.float64))
+        out += torch.exp(1j * iflag * ph) @ c[lo:hi].to(torch.complex128)
+    return out
+
+
+def rel_err(a, b):
+    import torch
+
+    a = a.to(torch.complex128)
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+
+def round_trip_errors(dev, pts_h, f, c, g, N, m=1000):
+    """Errors of the headline round trip against FP64 direct sums: the
+    type-2 values at m random points and the type-1 modes at m random mode
+    indices.  The plan-API calls pass the point arrays in backend order
+    (first array with the fastest mode axis), so the user order is reversed."""
+    import torch
+
+    rng = np.random.default_rng(SEED + 9)
+    M = pts_h.shape[1]
+    pts_user = [torch.from_numpy(pts_h[d]).to(dev) for d in (2, 1, 0)]
+    idx = torch.from_numpy(rng.choice(M, size=m, replace=False)).to(dev)
+    t2 = direct_type2_subset(f, pts_user, idx, -1)
+    e2 = rel_err(c[idx], t2)
+    kidx = torch.from_numpy(rng.integers(0, N, size=(m, 3))).to(dev)
+    t1 = direct_type1_subset(c, pts_user, kidx, (N, N, N), +1)
+    e1 = rel_err(g[kidx[:, 0], kidx[:, 1], kidx[:, 2]], t1)
+    return {"type2_rel_l2_vs_fp64_direct_%d_points" % m: e2,
+            "type1_rel_l2_vs_fp64_direct_%d_modes" % m: e1}
+
+
+def measure_plain2d(dev, steps, warmup, cpu=True):
+    """Plain 2D type-1 (the CPU-runnable workload): M=1e5 uniform points,
+    complex128 strengths, 256^2 modes, eps=1e-6, iflag=+1, through nufft1;
+    error against the full FP64 direct sum; the oracle port timed beside it."""
+    import torch
+
+    import jax_finufft_gb300 as jf
+
+    rng = np.random.default_rng(SEED + 1)
+    M, N = 100_000, 256
+    x = rng.uniform(-np.pi, np.pi, M)
+    y = rng.uniform(-np.pi, np.pi, M)
+    ch = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    xt, yt = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+    ct = torch.from_numpy(ch).to(dev)
+    fn = lambda: jf.nufft1((N, N), ct, xt, yt, eps=1e-6, iflag=1)
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    kk = _freqs(N, xt)
+    Ex = torch.exp(1j * torch.outer(kk, xt))
+    Ey = torch.exp(1j * torch.outer(kk, yt))
+    truth = (Ex * ct[None, :]) @ Ey.T
+    res = {"workload": "2D type-1, M=1e5 uniform points, complex128, 256^2 modes, eps=1e-6 "
+                       "(nufft1, one transform per call)",
+           "ms_per_call": ms, "pts_per_s": M / (ms * 1e-3),
+           "rel_l2_vs_fp64_direct": rel_err(out, truth)}
+    if cpu:
+        from oracle import cpu_nufft
+
+        cores = cpu_cores()
+        cpu_nufft.set_threads(cores)
+        cpu_nufft.nufft1((N, N), ch, x, y, eps=1e-6, iflag=1)
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            cpu_nufft.nufft1((N, N), ch, x, y, eps=1e-6, iflag=1)
+        t_cpu = (time.perf_counter() - t0) / reps
+        res["cpu_port"] = {"ms_per_call": t_cpu * 1e3, "pts_per_s": M / t_cpu, "cores": cores,
+                           "kind": "port"}
+    return res
+
+
+def measure_type3(dev, steps, warmup):
+    """3D type-3, M=1e6 sources U[-pi,pi)^3, N=1e6 targets U[-64,64)^3, in
+    complex64 at eps=1e-6 and complex128 at eps=1e-12: forward, and forward
+    plus the vjp with respect to strengths and source points (torch API);
+    errors against the FP64 direct sum on 500 random targets."""
+    import torch
+
+    import jax_finufft_gb300 as jf
+
+    rng = np.random.default_rng(SEED + 5)
+    M = Nt = 1_000_000
+    src_h = rng.uniform(-np.pi, np.pi, (3, M))
+    tgt_h = rng.uniform(-64.0, 64.0, (3, Nt))
+    c_h = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    gbar_h = rng.standard_normal(Nt) + 1j * rng.standard_normal(Nt)
+    tidx = torch.from_numpy(rng.choice(Nt, size=500, replace=False)).to(dev)
+    out = {}
+    for name, cdt, rdt, eps in (("complex64_eps1e-6", torch.complex64, torch.float32, 1e-6),
+                                ("complex128_eps1e-12", torch.complex128, torch.float64, 1e-12)):
+        src = [torch.from_numpy(src_h[d]).to(dev, rdt) for d in range(3)]
+        tgt = [torch.from_numpy(tgt_h[d]).to(dev, rdt) for d in range(3)]
+        c = torch.from_numpy(c_h).to(dev, cdt)
+        gbar = torch.from_numpy(gbar_h).to(dev, cdt)
+
+        def fwd():
+            return jf.nufft3(c, *src, *tgt, eps=eps, iflag=-1)
+
+        a = [c.clone().requires_grad_(True)] + [s.clone().requires_grad_(True) for s in src]
+
+        def fwd_bwd():
+            r = jf.nufft3(a[0], *a[1:], *tgt, eps=eps, iflag=-1)
+            return torch.autograd.grad(r, a, grad_outputs=gbar)
+
+        res = {}
+        for label, fn in (("forward", fwd), ("forward_vjp", fwd_bwd)):
+            for _ in range(warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            res[label] = {"ms": ms, "pts_per_s": M / (ms * 1e-3)}
+        f = fwd()
+        truth = direct_type3_subset(c, src, tgt, tidx, -1)
+        res["rel_l2_vs_fp64_direct_500_targets"] = rel_err(f[tidx], truth)
+        out[name] = res
+        del a, c, src, tgt, gbar, f
+        torch.cuda.empty_cache()
+    out["workload"] = ("3D type-3, M=1e6 sources U[-pi,pi)^3, 1e6 targets U[-64,64)^3, "
+                       "iflag=-1; vjp w.r.t. strengths and sources (torch API)")
+    return out
 
 
 def measure_lsq_grad(dev, steps, warmup):
@@ -540,6 +737,8 @@ def main():
                     help="run only the differentiated least-squares measurement")
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the batched 2D measurement")
+    ap.add_argument("--only", choices=["lsq", "batched", "plain2d", "type3"],
+                    help="run only one secondary measurement")
     ap.add_argument("--points", type=int, default=M_POINTS,
                     help="points per transform (reduced cases for profiling)")
     ap.add_argument("--modes", type=int, default=N_MODES, help="modes per axis")
@@ -548,11 +747,16 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    if args.lsq_only or args.batched_only:
+    if args.lsq_only:
+        args.only = "lsq"
+    if args.batched_only:
+        args.only = "batched"
+    if args.only:
         import torch
 
         torch.cuda.set_device(0)
-        fn = measure_lsq_grad if args.lsq_only else measure_batched
+        fn = {"lsq": measure_lsq_grad, "batched": measure_batched, "plain2d": measure_plain2d,
+              "type3": measure_type3}[args.only]
         print(json.dumps(fn(torch.device("cuda", 0), args.steps, args.warmup)))
         return 0
     return run_ours(args)
