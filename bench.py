@@ -642,8 +642,9 @@ def measure_batched(dev, steps, warmup):
     (a) 32 stacked type-1 transforms sharing M=4e6 uniform points, 512^2 modes;
     (b) 64 independent type-2 transforms, M_k = floor(10^U(3,6)) points each,
         modes drawn from {128^2, 256^2, 512^2, 1024^2}.
-    Plain = the per-call path (nufft1 with 32 stacked transforms; 64 nufft2
-    calls); batched = one NufftBatch pass replayed from a CUDA graph.
+    Plain = the per-call path with default settings (nufft1 with 32 stacked
+    transforms; 64 nufft2 calls); batched = one autotuned NufftBatch pass
+    replayed from a CUDA graph (tuning and planning timed separately).
     Returns NU points/s/transform for each."""
     import torch
 
@@ -672,14 +673,16 @@ def measure_batched(dev, steps, warmup):
     c = torch.tensor((rng.standard_normal((T, M)) + 1j * rng.standard_normal((T, M)))
                      .astype(np.complex64), device=dev)
     ms_plain = timed(lambda: jf.nufft1((N, N), c, *x, eps=1e-6))
-    b = NufftBatch(1, [(N, N)], [M], ntransf=T, eps=1e-6, use_graph=True)
+    t0 = time.perf_counter()
+    b = NufftBatch(1, [(N, N)], [M], ntransf=T, eps=1e-6, use_graph=True, autotune=True)
+    tune_a = time.perf_counter() - t0
     P = torch.stack(x)
     f = b.empty_modes()
     cb = c.reshape(-1)
     ms_batch = timed(lambda: b.run_packed(P, cb, f))
     out["stacked_type1_32x4e6_512sq"] = {
         "plain_pts_per_s": T * M / (ms_plain * 1e-3), "batched_pts_per_s": T * M / (ms_batch * 1e-3),
-        "plain_ms": ms_plain, "batched_ms": ms_batch}
+        "plain_ms": ms_plain, "batched_ms": ms_batch, "plan_and_tune_s": tune_a}
     del b, c, f
     # (b) independent uneven problems
     K = 64
@@ -690,7 +693,9 @@ def measure_batched(dev, steps, warmup):
     fs = [torch.tensor((rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64),
                        device=dev) for s in shapes]
     ms_plain = timed(lambda: [jf.nufft2(fk, *pk, eps=1e-6) for fk, pk in zip(fs, pts)])
-    b = NufftBatch(2, shapes, Ms, eps=1e-6, use_graph=True)
+    t0 = time.perf_counter()
+    b = NufftBatch(2, shapes, Ms, eps=1e-6, use_graph=True, autotune=True)
+    tune_b = time.perf_counter() - t0
     P = b.pack_points(pts)
     fb = torch.cat([fk.reshape(-1) for fk in fs])
     cb = b.empty_strengths()
@@ -699,7 +704,7 @@ def measure_batched(dev, steps, warmup):
     out["independent_type2_64"] = {
         "plain_pts_per_s": tot / (ms_plain * 1e-3), "batched_pts_per_s": tot / (ms_batch * 1e-3),
         "plain_ms": ms_plain, "batched_ms": ms_batch, "total_points": tot,
-        "fft_groups": b.info()["fft_groups"]}
+        "fft_groups": b.info()["fft_groups"], "plan_and_tune_s": tune_b}
     return out
 
 

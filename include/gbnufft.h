@@ -65,7 +65,14 @@ typedef struct gbn_opts {
                              FP64, as cuFINUFFT); 1 = FP32; 2 = FP64 (complex128 only);
                              3 = split rule: FP32 when eps >= 1e-6, FP64 otherwise.  Point
                              folding and binning are FP64 in every mode. */
+  int gpu_autotune;       /* batched plans: 0 off; GBN_TUNE_ON (| GBN_TUNE_SM_ONLY,
+                             | GBN_TUNE_KEEP_SIGMA) picks each problem's settings with
+                             gbn_autotune.  Ignored by the plan and one-shot entry points. */
 } gbn_opts;
+
+#define GBN_TUNE_ON 1         /* tune sigma, method, bin size and points per subproblem */
+#define GBN_TUNE_SM_ONLY 2    /* only the shared-memory method (keeps batches on the work queue) */
+#define GBN_TUNE_KEEP_SIGMA 4 /* keep opts->upsampfac (or a batch's per-problem sigma) */
 
 /* Fill *o with the defaults (cuFINUFFT's, per options.py:66-79). */
 GBN_API void gbn_default_opts(gbn_opts* o);
@@ -190,6 +197,31 @@ GBN_API int gbn_batch_run(gbn_batch b, const void* x, const void* y, const void*
                           void* f, int use_graph);
 GBN_API int gbn_batch_info(gbn_batch b, int* ngroups, int* queue, int64_t* arena_bytes);
 GBN_API int gbn_batch_destroy(gbn_batch b);
+
+/*
+ * Autotuner (no counterpart in the reference, whose settings are fixed
+ * per call).  For one problem class -- type (1 or 2), dim, precision, the
+ * mode shape nmodes (backend order), M rounded up to a power of two,
+ * ntransf, eps and the options' precision/kernel-evaluation fields -- times
+ * candidate settings on seeded synthetic uniform points: sigma in {2, 1.25},
+ * method 2 or 1, three bin shapes and 256..4096 points per subproblem.  The
+ * fastest candidate whose relative l2 error against an FP64 transform at
+ * eps/100 is at most max(eps, 1.5 x the default settings' error) is
+ * written into *out (a copy of *base with upsampfac, gpu_method, bin sizes
+ * and gpu_maxsubprobsize replaced).  base->gpu_autotune's GBN_TUNE_SM_ONLY
+ * and GBN_TUNE_KEEP_SIGMA bits narrow the search.  Results are cached per
+ * class and GPU model in memory and in a text file: $GBN_AUTOTUNE_CACHE
+ * ("off" for none), else $XDG_CACHE_HOME/gbnufft/autotune.txt, else
+ * $HOME/.cache/gbnufft/autotune.txt.  A cache miss synchronises `stream`
+ * and allocates; do not call it while capturing.  info (NULL or 3
+ * doubles): median ms of one setpts + execute, its error, 1 if cached.
+ */
+GBN_API int gbn_autotune(int type, int dim, int single, const int64_t* nmodes, int64_t M,
+                         int ntransf, double eps, int iflag, const gbn_opts* base, void* stream,
+                         gbn_opts* out, double* info);
+/* Forget the in-memory autotuner cache; forget_file = 1 also stops it from
+ * reloading the cache file in this process. */
+GBN_API void gbn_autotune_clear(int forget_file);
 
 /* Thread-local message describing the last non-zero status. */
 GBN_API const char* gbn_last_error(void);

@@ -1537,6 +1537,16 @@ int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, c
   for (int k = 0; k < K; ++k) {
     gbn_opts o = base;
     if (sigma && sigma[k] > 0.0) o.upsampfac = sigma[k];
+    if ((base.gpu_autotune & GBN_TUNE_ON) && M[k] > 0) {
+      // per-problem settings, shared-memory method only so the work queue applies
+      gbn_opts q = o;
+      q.gpu_autotune = base.gpu_autotune | GBN_TUNE_SM_ONLY;
+      if (sigma && sigma[k] > 0.0) q.gpu_autotune |= GBN_TUNE_KEEP_SIGMA;
+      const int r = gbn_autotune(type, dim, single ? 1 : 0, nmodes + 3 * k, M[k], T, eps, iflag,
+                                 &q, (void*)b->stream, &o, nullptr);
+      if (r >= 2) return r;
+    }
+    o.gpu_autotune = 0;
     o.gpu_maxbatchsize = T;
     o.debug = 0;
     gbn_plan_s* p = nullptr;

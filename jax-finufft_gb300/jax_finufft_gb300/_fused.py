@@ -79,10 +79,17 @@ class FusedState:
         self.handles = []
 
 
-def plan_key(nufft_type, dim, single, nk_b, iflag, n_transf, eps_v, opts, device, stream):
+def plan_key(nufft_type, dim, single, nk_b, iflag, n_transf, eps_v, opts, device, stream,
+             n_j=0):
     fwd = unpack_opts(opts, nufft_type, True) or Opts()
+    native = to_native(fwd)
+    if getattr(fwd, "gpu_autotune", False) and n_j > 0:
+        from . import tune
+
+        native, _ = tune.tuned_native(nufft_type, dim, single, nk_b, n_j, n_transf, eps_v,
+                                      iflag, native, stream)
     return (nufft_type, dim, bool(single), tuple(int(v) for v in nk_b), int(iflag), int(n_transf),
-            float(eps_v), _opts_key(to_native(fwd)), int(stream), str(device))
+            float(eps_v), _opts_key(native), int(stream), str(device))
 
 
 def forward(nufft_type, source, points, output_shape, iflag, eps, opts, out, single, dim):
@@ -98,7 +105,8 @@ def forward(nufft_type, source, points, output_shape, iflag, eps, opts, out, sin
     nk_b = list(nk[::-1]) + [1] * (3 - dim)
     eps_v = float(np.float32(eps)) if single else float(eps)
     stream = torch.cuda.current_stream(dev).cuda_stream
-    key = plan_key(nufft_type, dim, single, nk_b, iflag, n_transf, eps_v, opts, dev, stream)
+    key = plan_key(nufft_type, dim, single, nk_b, iflag, n_transf, eps_v, opts, dev, stream,
+                   n_j)
     plan = get_plan(key)
     src = source.contiguous()
     pts = [p.contiguous() for p in points][::-1]  # backend order

@@ -43,6 +43,7 @@ class GbnOpts(ctypes.Structure):
         ("gpu_binsizez", ctypes.c_int),
         ("gpu_maxsubprobsize", ctypes.c_int),
         ("gpu_precision", ctypes.c_int),
+        ("gpu_autotune", ctypes.c_int),
     ]
 
 
@@ -89,6 +90,10 @@ SIGNATURES = {
     "gbn_batch_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int), _i64p]),
     "gbn_batch_destroy": (ctypes.c_int, [_vp]),
+    "gbn_autotune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _i64p, _i64,
+                                    ctypes.c_int, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp,
+                                    _vp]),
+    "gbn_autotune_clear": (None, [ctypes.c_int]),
     "gbn_binsort_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,
                                            _i64p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                            _vp, _vp, _vp]),

@@ -31,6 +31,8 @@ class NufftBatch:
     n_points: K point counts.
     ntransf: transforms per problem (stacked strengths/modes).
     upsampfac: optional K upsampling factors (sigma per problem).
+    autotune: pick each problem's sigma (unless upsampfac is given), bin size
+        and points per subproblem with the autotuner (cached per class).
 
     Work runs on a stream the batch owns (the legacy default stream cannot be
     captured into a graph), ordered after everything already queued on the
@@ -40,7 +42,7 @@ class NufftBatch:
 
     def __init__(self, nufft_type, n_modes, n_points, ntransf=1, iflag=None, eps=1e-6,
                  dtype=torch.complex64, opts=None, upsampfac=None, device=None,
-                 use_graph=True):
+                 use_graph=True, autotune=False):
         if nufft_type not in (1, 2):
             raise ValueError("NufftBatch supports types 1 and 2")
         self.type = nufft_type
@@ -71,6 +73,8 @@ class NufftBatch:
         if upsampfac is not None:
             sig = (ctypes.c_double * self.K)(*[float(v) for v in upsampfac])
         native = to_native(opts or Opts())
+        if autotune:
+            native.gpu_autotune = 1  # per problem, shared-memory method (work queue)
         eps_v = float(np.float32(eps)) if self.single else float(eps)
         self.stream = torch.cuda.current_stream(self.device)
         self.handle = ctypes.c_void_p()

@@ -23,7 +23,7 @@ import threading
 import numpy as np
 import torch
 
-from . import _fused, _native
+from . import _fused, _native, tune
 from .options import Opts, to_native, unpack_opts
 from .shapes import broadcast_and_flatten_inputs, check_canonical
 
@@ -86,8 +86,12 @@ def _execute(nufft_type, source, points, output_shape, iflag, eps, opts):
     eps_v = float(np.float32(eps)) if single else float(eps)
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev).cuda_stream
+        native = to_native(fwd)
+        if getattr(fwd, "gpu_autotune", False) and nufft_type in (1, 2):
+            native, _ = tune.tuned_native(nufft_type, ndim, single, nk_b, n_j, n_transf, eps_v,
+                                          int(iflag), native, stream)
         _native.run(nufft_type, ndim, single, stream, eps_v, int(iflag), n_tot, n_transf, n_j,
-                    nk_b, to_native(fwd), src.data_ptr(), [p.data_ptr() for p in pts],
+                    nk_b, native, src.data_ptr(), [p.data_ptr() for p in pts],
                     [p.data_ptr() for p in tgts], out.data_ptr())
     return out
 

@@ -7,8 +7,9 @@ here (pydantic is not available everywhere this package runs), keeping
 equality, hashing and keyword construction identical.  Only the GPU fields
 and ``modeord`` reach the GB300 engine (as in ``to_cufinufft_opts``,
 options.py:105-119), plus the bin-size / subproblem fields that the reference
-carries but never forwards, and one extra field, ``gpu_precision``, that
-selects the compute precision (0 = the data's, the reference behaviour).
+carries but never forwards, and the engine's own fields: ``gpu_precision`` (compute precision; 0 = the
+data's, the reference behaviour), ``gpu_fused_adjoint`` and
+``gpu_autotune``.
 """
 from dataclasses import dataclass
 from enum import IntEnum
@@ -105,6 +106,9 @@ class Opts:
     # reverse mode through one fused adjoint on the forward's sorted points
     # (False: the stacked-transform rules of the reference's JVP/transpose)
     gpu_fused_adjoint: bool = True
+    # types 1/2: look up (or tune, on a cache miss) sigma, method, bin sizes
+    # and points per subproblem for each call's class (see tune.py)
+    gpu_autotune: bool = False
 
     def __post_init__(self):
         if int(self.modeord) not in (0, 1):

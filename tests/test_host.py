@@ -183,7 +183,7 @@ def test_default_opts_and_struct_layout(native):
     assert (o.modeord, o.upsampfac, o.gpu_method, o.gpu_sort, o.gpu_kerevalmeth) == (
         0, 2.0, 0, 1, 1)
     assert o.gpu_maxsubprobsize == 1024 and o.gpu_precision == 0
-    assert ctypes.sizeof(_native.GbnOpts) == 56
+    assert ctypes.sizeof(_native.GbnOpts) == 64
 
 
 def test_cpu_tensors_are_rejected():
