@@ -307,6 +307,10 @@ def run_ours(args):
         e2e_value, e2e_ms = run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws,
                                     barrier, max_over_ranks)
     accuracy = round_trip_errors(dev, pts_h, f, c, g, N)
+    rate = ctypes.c_double()
+    _native.check(lib.gbn_probe_smem_atomics(sp, min(w.value, 8), ctypes.byref(rate)), "probe")
+    updates = M * w.value ** 3  # grid cells touched per transform
+    ceiling = rate.value / 2  # two int32 atomics per complex update
     peak, peak_kind = measured_peak()
     alg = algorithmic_bytes(M, nf_total)
     spread_ms, interp_ms = t1[0], t2[0]
@@ -339,6 +343,15 @@ def run_ours(args):
                      "algorithmic_bytes": alg, "traffic": traffic,
                      "other": {"spread_GBs": alg / (spread_ms * 1e-3) / 1e9,
                                "interp_GBs": alg / (interp_ms * 1e-3) / 1e9}},
+        "grid_updates": {
+            "spread_per_s": updates / (spread_ms * 1e-3),
+            "interp_per_s": updates / (interp_ms * 1e-3),
+            "smem_int32_atomics_per_s": rate.value,
+            "spread_ceiling_per_s": ceiling,
+            "spread_frac_of_ceiling": updates / (spread_ms * 1e-3) / ceiling,
+            "note": "M w^3 complex cell updates per transform; the shared-memory spread "
+                    "issues two int32 atomics per update, so its ceiling is half the "
+                    "probed atomic rate (gbn_probe_smem_atomics, same access pattern)"},
     }
     lib.gbn_destroy(p1)
     lib.gbn_destroy(p2)

@@ -223,6 +223,12 @@ GBN_API int gbn_autotune(int type, int dim, int single, const int64_t* nmodes, i
  * reloading the cache file in this process. */
 GBN_API void gbn_autotune_clear(int forget_file);
 
+/* Measurement aid (no counterpart in the reference): int32 shared-memory
+ * atomic adds per second over the whole GPU with the access pattern of the
+ * fixed-point spread (w lanes x w rows per point, 8-lane groups), the
+ * ceiling its point phase is held against.  Synchronises `stream`. */
+GBN_API int gbn_probe_smem_atomics(void* stream, int w, double* atomics_per_s);
+
 /* Thread-local message describing the last non-zero status. */
 GBN_API const char* gbn_last_error(void);
 
