@@ -223,6 +223,11 @@ GBN_API int gbn_autotune(int type, int dim, int single, const int64_t* nmodes, i
  * reloading the cache file in this process. */
 GBN_API void gbn_autotune_clear(int forget_file);
 
+/* Number of bounded device-side waits (the bulk tensor copy of a tile into
+ * shared memory) that gave up on the current device since the last reset;
+ * 0 in a healthy run.  reset = 1 clears it.  Synchronous. */
+GBN_API int gbn_wait_timeouts(long long* count, int reset);
+
 /* Measurement aid (no counterpart in the reference): int32 shared-memory
  * atomic adds per second over the whole GPU with the access pattern of the
  * fixed-point spread (w lanes x w rows per point, 8-lane groups), the

@@ -12,6 +12,7 @@
 //                  chunks of at most maxsub points
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (a plain struct; the encoder is resolved at run time)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -52,6 +53,17 @@ struct Geom {
   int64_t nbins;
   int maxsub;
 };
+
+// Shared-memory tile of one bin: bs + w - 1 cells per axis from the bin's
+// first grid start, except along x, where the tile starts on the even cell at
+// or below it and spans an even number of cells (one or two more): a TMA copy
+// of a float2 grid needs 16-byte aligned x offsets and extents.
+__host__ __device__ inline int tile_x(int bs0, int w) { return (bs0 + w + 1) & ~1; }
+__host__ __device__ inline int64_t tile_cells(int dim, const int* bs, int w) {
+  int64_t n = tile_x(bs[0], w);
+  for (int d = 1; d < dim; ++d) n *= bs[d] + w - 1;
+  return n;
+}
 
 // How points map onto the grid: mode 0 folds periodically (types 1/2),
 // mode 1 rescales (type-3 sources): X = (x - center)*scale + nf/2.
@@ -119,16 +131,30 @@ cudaError_t launch_sort_finish(const Geom& g, int64_t M, SortState& st, bool sor
 
 // Spread ntr transforms: c (ntr, M) data precision -> fine (ntr, nf) compute precision.
 // method 1 = global atomics per update, 2 = shared-memory subproblems.
+// tmap (optional, FP32 compute, method 2): a TMA map of the ntr fine grids
+// from tile_tensor_map; interior tiles are then added to the grid with one
+// bulk tensor reduce-add (spread) or staged with one bulk tensor copy
+// (interp) instead of per-cell loops.
 template <typename TC, typename TD>
 cudaError_t launch_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                           const SortState& st, const void* c, void* fine, int ntr,
-                          cudaStream_t s);
+                          cudaStream_t s, const CUtensorMap* tmap = nullptr);
+
+// Encode a TMA map over nb float2 fine grids of geometry g (rank = dim:
+// x as 2*nf0 floats, the last axis stacked over the nb grids) whose box is
+// one bin tile.  False (and no map) when TMA does not apply: 1D, a box
+// extent above 256 elements, or no driver entry point.
+bool tile_tensor_map(const Geom& g, const void* grid, int nb, CUtensorMap* out);
+
+// Number of bounded waits in the point kernels that gave up (a wait that
+// should take microseconds); 0 in a healthy run.  reset clears the count.
+cudaError_t read_wait_timeouts(unsigned* out, bool reset);
 
 // Interpolate ntr transforms: fine -> c (ntr, M).
 template <typename TC, typename TD>
 cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                           const SortState& st, const void* fine, void* c, int ntr,
-                          cudaStream_t s);
+                          cudaStream_t s, const CUtensorMap* tmap = nullptr);
 
 // Type-1 deconvolution + mode reorder: fine (ntr, nf) -> out (ntr, N).
 // phi[d] holds 1/psihat for each output index along axis d.

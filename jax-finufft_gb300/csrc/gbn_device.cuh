@@ -61,8 +61,10 @@ __device__ __forceinline__ int wrap_i32(int i, int n) {
 }
 
 // Bin tile of a subproblem: origin (first grid index, may be negative) and
-// extent bs + w - 1 per axis; points of the bin start at tile offsets
-// [0, bs) (the bin rule of the fold kernel), so their supports fit.
+// extent per axis; points of the bin start at grid offsets [0, bs) from the
+// bin's first grid start bin*bs - floor(w/2) (the bin rule of the fold
+// kernel), so their w-wide supports fit in bs + w - 1 cells.  Along x the
+// origin is rounded down to an even cell and the extent is tile_x(bs, w).
 template <int DIM>
 struct Tile {
   int org[3];
@@ -82,9 +84,101 @@ struct Tile {
       org[d] = b * g.bs[d] - (g.w >> 1);
       T[d] = g.bs[d] + g.w - 1;
     }
+    org[0] -= org[0] & 1;  // even start (two's complement: rounds negatives down too)
+    T[0] = tile_x(g.bs[0], g.w);
     ncell = T[0] * T[1] * T[2];
   }
+  // The tile lies inside one period of the grid on every axis (no wrap).
+  __device__ __forceinline__ bool interior(const Geom& g) const {
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) in = in && org[d] >= 0 && org[d] + T[d] <= (int)g.nf[d];
+    return in;
+  }
 };
+
+// ---------------------------------------------------------------------------
+// Bulk tensor copies (TMA) and mbarriers, inline PTX for sm_90+ / sm_103a.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Wait for phase `parity` of bar, giving up after `limit` polls (each poll
+// suspends for a hardware-bounded time); false if it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// Copy the box at coordinates c (floats along x) of the map into dst,
+// completing `bytes` transactions on bar.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+      : "memory");
+}
+// Element-wise add of the shared-memory box src into the map's box at c.
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, const void* src, int c0,
+                                                  int c1) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group"
+      " [%0, {%2, %3}], [%1];" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(smem_addr(src)), "r"(c0), "r"(c1)
+      : "memory");
+}
+__device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap* map, const void* src, int c0,
+                                                  int c1, int c2) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group"
+      " [%0, {%2, %3, %4}], [%1];" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(smem_addr(src)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Wait until every committed bulk operation of this thread has read its
+// shared-memory source.
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// Order this thread's generic-proxy shared-memory writes before later bulk
+// (async-proxy) reads of them.
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 // Walks the cells tid, tid + step, ... of a T0 x T1 x T2 tile keeping the
 // coordinates (c0, c1, c2) with additions instead of a division per cell.

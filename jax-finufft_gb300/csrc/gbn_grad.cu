@@ -364,11 +364,9 @@ cudaError_t run_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t M,
   sa.perm = st.perm;
   sa.sorted = 1;
   if (st.max_sub == 0) return cudaSuccess;
-  int64_t nftot = 1, ncell = 1;
-  for (int d = 0; d < DIM; ++d) {
-    nftot *= g.nf[d];
-    ncell *= g.bs[d] + g.w - 1;
-  }
+  int64_t nftot = 1;
+  for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
+  const int64_t ncell = tile_cells(DIM, g.bs, g.w);
   GradOut<TD> go;
   go.w = (const cplx_t<TD>*)w;
   go.out_c = (cplx_t<TD>*)out_c;

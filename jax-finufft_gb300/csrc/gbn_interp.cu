@@ -6,11 +6,15 @@
 // the G partial sums are reduced with xor shuffles and one lane writes the
 // result to the point's original position.
 //
-//   method 2 (SM): the block first stages its bin's (bs+w)^d tile from the
-//     fine grid into shared memory (coalesced rows, periodic wrap), so the
-//     gathers never touch HBM.
+//   method 2 (SM): the block first stages its bin's tile from the fine grid
+//     into shared memory -- one bulk tensor copy (TMA, FP32) when the tile
+//     does not wrap around the grid, else a cell loop with periodic wrap --
+//     so the gathers never touch HBM.
 //   method 1 (GM): gathers straight from the fine grid through L1/L2.
 #include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
 
 #include "gbn_common.cuh"
 #include "gbn_device.cuh"
@@ -18,6 +22,10 @@
 namespace gbn {
 
 namespace {
+
+// Bounded waits that gave up (see read_wait_timeouts).
+__device__ unsigned g_wait_timeouts;
+constexpr int kWaitPolls = 1 << 20;
 
 struct SubArgs {
   const int* sub_bin;
@@ -58,13 +66,16 @@ __device__ __forceinline__ void group_reduce(TC& a, TC& b) {
 
 // One subproblem of one transform, executed by the whole block (shared by
 // the per-subproblem kernel and the work-queue kernel of batched plans).
+// tmap (or null): TMA map of the grids; t_map = this transform's index in it.
 template <typename TC, typename TD, int DIM, int G>
 __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                                 const PtRec<TC, DIM>* __restrict__ recs,
                                                 const SubArgs& sa, int sub, int t,
                                                 const cplx_t<TC>* __restrict__ fine,
                                                 cplx_t<TD>* __restrict__ c, int64_t nftot,
-                                                unsigned char* smem_raw) {
+                                                unsigned char* smem_raw,
+                                                const CUtensorMap* tmap = nullptr,
+                                                int t_map = 0) {
   constexpr int NCO = GroupCfg<G>::NCO;
   constexpr int PPW = 32 / G;
   constexpr int NWARP = kThreads / 32;
@@ -75,7 +86,28 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
   const int ncell = tl.ncell;
   cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
   const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
-  {
+  bool staged = false;
+  if constexpr (sizeof(TC) == 4 && DIM > 1) {
+    if (tmap != nullptr && tl.interior(g)) {
+      __shared__ alignas(8) uint64_t s_bar;
+      if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_expect_tx(&s_bar, (uint32_t)(ncell * sizeof(cplx_t<TC>)));
+        if (DIM == 2)
+          tma_load_2d(tile, tmap, &s_bar, 2 * tl.org[0], tl.org[1] + t_map * (int)g.nf[1]);
+        else
+          tma_load_3d(tile, tmap, &s_bar, 2 * tl.org[0], tl.org[1],
+                      tl.org[2] + t_map * (int)g.nf[2]);
+      }
+      __syncthreads();  // the barrier is initialised before anyone polls it
+      if (!mbar_wait_bounded(&s_bar, 0, kWaitPolls)) {
+        if (threadIdx.x == 0) atomicAdd(&g_wait_timeouts, 1u);
+        mbar_wait_bounded(&s_bar, 0, kWaitPolls);  // the copy in flight, bounded again
+      }
+      staged = true;
+    }
+  }
+  if (!staged) {
     const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
     CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
     for (int i = threadIdx.x; i < ncell; i += kThreads, cw.next()) {
@@ -159,10 +191,12 @@ template <typename TC, typename TD, int DIM, int G>
 __global__ void __launch_bounds__(kThreads)
     interp_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
                      SubArgs sa, const cplx_t<TC>* __restrict__ fine, cplx_t<TD>* __restrict__ c,
-                     int64_t nftot) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+                     int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
+                     int t_base) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   interp_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, fine, c, nftot,
-                                  smem_raw);
+                                  smem_raw, use_tma ? &tmap : nullptr,
+                                  t_base + (int)blockIdx.y);
 }
 
 template <typename TC, typename TD, int DIM, int G>
@@ -295,7 +329,7 @@ cudaError_t run_interp_queue(const BatchProb<TC>* probs, int K, const int64_t* i
 template <typename TC, typename TD, int DIM, int G>
 cudaError_t run_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                        const SortState& st, const void* fine, void* c, int ntr,
-                       cudaStream_t s) {
+                       cudaStream_t s, const CUtensorMap* tmap) {
   SubArgs sa;
   sa.sub_bin = st.sub_bin;
   sa.sub_off = st.sub_off;
@@ -315,14 +349,17 @@ cudaError_t run_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     const cplx_t<TC>* ft = (const cplx_t<TC>*)fine + (int64_t)t0 * nftot;
     cplx_t<TD>* ct = (cplx_t<TD>*)c + (int64_t)t0 * M;
     if (method == 2 && sa.sorted) {
-      int64_t ncell = 1;
-      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w - 1;
+      const int64_t ncell = tile_cells(DIM, g.bs, g.w);
       const size_t smem = (size_t)ncell * sizeof(cplx_t<TC>);
       auto kern = interp_sm_kernel<TC, TD, DIM, G>;
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
       if (e != cudaSuccess) return e;
-      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ft, ct, nftot);
+      CUtensorMap m;
+      memset(&m, 0, sizeof(m));
+      const int use = tmap != nullptr && sizeof(TC) == 4;
+      if (use) m = *tmap;
+      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ft, ct, nftot, m, use, t0);
       note_launch();
     } else {
       interp_gm_kernel<TC, TD, DIM, G><<<grid, kThreads, 0, s>>>(g, ks, M, recs, sa, ft, ct,
@@ -340,32 +377,99 @@ cudaError_t run_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
 template <typename TC, typename TD>
 cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                           const SortState& st, const void* fine, void* c, int ntr,
-                          cudaStream_t s) {
+                          cudaStream_t s, const CUtensorMap* tmap) {
   if (M == 0) return cudaSuccess;
   const bool wide = g.w > 8;
   switch (g.dim) {
     case 1:
-      return wide ? run_interp<TC, TD, 1, 16>(g, ks, method, M, st, fine, c, ntr, s)
-                  : run_interp<TC, TD, 1, 8>(g, ks, method, M, st, fine, c, ntr, s);
+      return wide ? run_interp<TC, TD, 1, 16>(g, ks, method, M, st, fine, c, ntr, s, nullptr)
+                  : run_interp<TC, TD, 1, 8>(g, ks, method, M, st, fine, c, ntr, s, nullptr);
     case 2:
-      return wide ? run_interp<TC, TD, 2, 16>(g, ks, method, M, st, fine, c, ntr, s)
-                  : run_interp<TC, TD, 2, 8>(g, ks, method, M, st, fine, c, ntr, s);
+      return wide ? run_interp<TC, TD, 2, 16>(g, ks, method, M, st, fine, c, ntr, s, tmap)
+                  : run_interp<TC, TD, 2, 8>(g, ks, method, M, st, fine, c, ntr, s, tmap);
     default:
-      return wide ? run_interp<TC, TD, 3, 16>(g, ks, method, M, st, fine, c, ntr, s)
-                  : run_interp<TC, TD, 3, 8>(g, ks, method, M, st, fine, c, ntr, s);
+      return wide ? run_interp<TC, TD, 3, 16>(g, ks, method, M, st, fine, c, ntr, s, tmap)
+                  : run_interp<TC, TD, 3, 8>(g, ks, method, M, st, fine, c, ntr, s, tmap);
   }
 }
 
 template cudaError_t launch_interp<float, float>(const Geom&, const KerSpec<float>&, int,
                                                  int64_t, const SortState&, const void*, void*,
-                                                 int, cudaStream_t);
+                                                 int, cudaStream_t, const CUtensorMap*);
 template cudaError_t launch_interp<float, double>(const Geom&, const KerSpec<float>&, int,
                                                   int64_t, const SortState&, const void*, void*,
-                                                  int, cudaStream_t);
+                                                  int, cudaStream_t, const CUtensorMap*);
 template cudaError_t launch_interp<double, double>(const Geom&, const KerSpec<double>&, int,
                                                    int64_t, const SortState&, const void*,
-                                                   void*, int, cudaStream_t);
+                                                   void*, int, cudaStream_t, const CUtensorMap*);
 
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null when unavailable.
+EncodeTiledFn tiled_encoder() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+}  // namespace
+
+bool tile_tensor_map(const Geom& g, const void* grid, int nb, CUtensorMap* out) {
+  if (g.dim < 2 || g.dim > 3 || nb < 1 || grid == nullptr) return false;
+  if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0 || (g.nf[0] & 1) != 0) return false;
+  const int64_t tx = tile_x(g.bs[0], g.w);
+  const int64_t ty = g.bs[1] + g.w - 1, tz = g.bs[2] + g.w - 1;
+  cuuint64_t dims[3] = {0, 0, 0}, strides[2] = {0, 0};
+  cuuint32_t box[3] = {1, 1, 1}, es[3] = {1, 1, 1};
+  dims[0] = (cuuint64_t)(2 * g.nf[0]);
+  box[0] = (cuuint32_t)(2 * tx);
+  strides[0] = (cuuint64_t)(8 * g.nf[0]);
+  if (g.dim == 2) {
+    dims[1] = (cuuint64_t)(g.nf[1] * nb);
+    box[1] = (cuuint32_t)ty;
+  } else {
+    dims[1] = (cuuint64_t)g.nf[1];
+    dims[2] = (cuuint64_t)(g.nf[2] * nb);
+    strides[1] = (cuuint64_t)(8 * g.nf[0] * g.nf[1]);
+    box[1] = (cuuint32_t)ty;
+    box[2] = (cuuint32_t)tz;
+  }
+  for (int d = 0; d < g.dim; ++d) {
+    if (box[d] > 256 || box[d] > dims[d] || dims[d] > ((cuuint64_t)1 << 32)) return false;
+  }
+  EncodeTiledFn fn = tiled_encoder();
+  if (!fn) return false;
+  const CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)g.dim,
+                        const_cast<void*>(grid), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+cudaError_t read_wait_timeouts(unsigned* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_wait_timeouts, sizeof(unsigned));
+  if (e == cudaSuccess && reset) {
+    const unsigned zero = 0;
+    e = cudaMemcpyToSymbol(g_wait_timeouts, &zero, sizeof(unsigned));
+  }
+  return e;
+}
 
 template <typename TC, typename TD>
 cudaError_t launch_interp_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,

@@ -20,6 +20,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <list>
 #include <memory>
@@ -380,9 +381,7 @@ void default_bins(int dim, bool single, int* bs) {
 }
 
 size_t tile_bytes(int dim, const int* bs, int w, bool single) {
-  size_t n = 1;
-  for (int d = 0; d < dim; ++d) n *= (size_t)(bs[d] + w - 1);
-  return n * 2 * (single ? 4 : 8);
+  return (size_t)tile_cells(dim, bs, w) * 2 * (single ? 4 : 8);
 }
 
 // Fill geometry (bins, nb) for the current nf and options; choose method.
@@ -796,17 +795,29 @@ KerSpec<TC> ker_spec(gbn_plan_s* p) {
   return ks;
 }
 
+// TMA map of nb FP32 grids for the shared-memory point kernels (null when
+// not applicable; GBN_DISABLE_TMA=1 selects the per-cell tile loops).
+const CUtensorMap* grid_map(const gbn_plan_s* p, const gbn_points_s& ps, const void* grid,
+                            int nb, CUtensorMap* storage) {
+  if (!p->comp_single || p->method != 2 || !ps.st.perm) return nullptr;
+  const char* off = std::getenv("GBN_DISABLE_TMA");
+  if (off && off[0] == '1') return nullptr;
+  return tile_tensor_map(p->geom, grid, nb, storage) ? storage : nullptr;
+}
+
 int do_spread(gbn_plan_s* p, gbn_points_s& ps, const void* c, int nb, bool c_is_compute,
               void* grid) {
   const Geom& g = p->geom;
   cudaError_t e;
   if (p->comp_single) {
+    CUtensorMap map;
+    const CUtensorMap* tm = grid_map(p, ps, grid, nb, &map);
     if (p->data_single || c_is_compute)
       e = launch_spread<float, float>(g, ker_spec<float>(p), p->method, ps.M, ps.st, c, grid, nb,
-                                      p->stream);
+                                      p->stream, tm);
     else
       e = launch_spread<float, double>(g, ker_spec<float>(p), p->method, ps.M, ps.st, c, grid,
-                                       nb, p->stream);
+                                       nb, p->stream, tm);
   } else {
     e = launch_spread<double, double>(g, ker_spec<double>(p), p->method, ps.M, ps.st, c, grid,
                                       nb, p->stream);
@@ -819,12 +830,14 @@ int do_interp(gbn_plan_s* p, gbn_points_s& ps, void* c, int nb, const void* grid
   const Geom& g = p->geom;
   cudaError_t e;
   if (p->comp_single) {
+    CUtensorMap map;
+    const CUtensorMap* tm = grid_map(p, ps, grid, nb, &map);
     if (p->data_single)
       e = launch_interp<float, float>(g, ker_spec<float>(p), p->method, ps.M, ps.st, grid, c, nb,
-                                      p->stream);
+                                      p->stream, tm);
     else
       e = launch_interp<float, double>(g, ker_spec<float>(p), p->method, ps.M, ps.st, grid, c,
-                                       nb, p->stream);
+                                       nb, p->stream, tm);
   } else {
     e = launch_interp<double, double>(g, ker_spec<double>(p), p->method, ps.M, ps.st, grid, c,
                                       nb, p->stream);
@@ -1358,6 +1371,14 @@ int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void
 void gbn_clear_cache(void) { cache().clear(); }
 
 long long gbn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int gbn_wait_timeouts(long long* count, int reset) {
+  if (!count) return fail(GBN_ERR_ARGS, "NULL argument");
+  unsigned v = 0;
+  GBN_CUDA(read_wait_timeouts(&v, reset != 0));
+  *count = (long long)v;
+  return GBN_OK;
+}
 
 int gbn_run(int type, int dim, int single, void* stream, double eps, int iflag, int64_t n_tot,
             int64_t n_transf, int64_t n_j, const int64_t* n_k, const gbn_opts* opts,

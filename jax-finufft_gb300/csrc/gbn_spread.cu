@@ -7,9 +7,12 @@
 // the y/z values are broadcast with warp shuffles, and lane gl applies the
 // x offset gl of every (y, z) row.
 //
-//   method 2 (SM): the block accumulates into a shared-memory tile of
-//     (bs+w-1)^d cells kept as separate real/imaginary planes, then adds the
-//     tile to the fine grid with one vector atomic (float2) per non-zero cell.
+//   method 2 (SM): the block accumulates into a shared-memory tile of the
+//     bin (bs+w-1 cells per axis, x widened to an even start and extent),
+//     real and imaginary parts interleaved, then adds the tile to the fine
+//     grid: a tile that does not wrap around the grid goes back with one
+//     bulk tensor reduce-add (TMA, FP32), any other with one vector atomic
+//     (float2) per non-zero cell.
 //     In FP32 the tile holds 32-bit fixed-point integers: the block scales
 //     its points' strengths by s = 2^30 / sum_j max(|Re c_j|, |Im c_j|), so
 //     no cell sum can exceed 2^30 in magnitude, rounds every contribution to
@@ -21,6 +24,8 @@
 //   method 1 (GM): every update is a global atomic; used when the tile would
 //     not fit or when points are not sorted.
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "gbn_common.cuh"
 #include "gbn_device.cuh"
@@ -73,13 +78,16 @@ __device__ __forceinline__ void acc_add(double* p, double v) { atomicAdd(p, v); 
 
 // One subproblem of one transform, executed by the whole block (shared by
 // the per-subproblem kernel and the work-queue kernel of batched plans).
+// tmap (or null): TMA map of the grids; t_map = this transform's index in it.
 template <typename TC, typename TD, int DIM, int G>
 __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                                 const PtRec<TC, DIM>* __restrict__ recs,
                                                 const SubArgs& sa, int sub, int t,
                                                 const cplx_t<TD>* __restrict__ c,
                                                 cplx_t<TC>* __restrict__ fine, int64_t nftot,
-                                                unsigned char* smem_raw) {
+                                                unsigned char* smem_raw,
+                                                const CUtensorMap* tmap = nullptr,
+                                                int t_map = 0) {
   using A = typename Acc<TC>::type;
   constexpr bool kFixed = sizeof(A) == 4 && sizeof(TC) == 4;
   constexpr int NCO = GroupCfg<G>::NCO;
@@ -90,12 +98,8 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
   if (!sub_range(sa, g, M, sub, start, cnt, bin)) return;
   const int w = g.w;
   const Tile<DIM> tl(g, bin);
-  A* sre = reinterpret_cast<A*>(smem_raw);
-  A* sim = sre + tl.ncell;
-  for (int i = threadIdx.x; i < tl.ncell; i += kThreads) {
-    sre[i] = A(0);
-    sim[i] = A(0);
-  }
+  A* sacc = reinterpret_cast<A*>(smem_raw);  // cell i: [2i] real, [2i+1] imaginary
+  for (int i = threadIdx.x; i < 2 * tl.ncell; i += kThreads) sacc[i] = A(0);
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
   const cplx_t<TD>* ct = c + (int64_t)t * M;
 
@@ -138,25 +142,25 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
     const TC vr = cr * kx, vi = ci * kx;
     if (DIM == 1) {
       if (on) {
-        acc_add(&sre[l0], vr);
-        acc_add(&sim[l0], vi);
+        acc_add(&sacc[2 * l0], vr);
+        acc_add(&sacc[2 * l0 + 1], vi);
       }
     } else if (DIM == 2) {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      int idx = (r.i[1] - tl.org[1]) * tl.T[0] + l0;
+      int idx = 2 * ((r.i[1] - tl.org[1]) * tl.T[0] + l0);
       for (int iy = 0; iy < w; ++iy) {
         const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
         if (on) {
-          acc_add(&sre[idx], vr * kyv);
-          acc_add(&sim[idx], vi * kyv);
+          acc_add(&sacc[idx], vr * kyv);
+          acc_add(&sacc[idx + 1], vi * kyv);
         }
-        idx += tl.T[0];
+        idx += 2 * tl.T[0];
       }
     } else {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
-      const int plane = tl.T[0] * tl.T[1];
-      int zbase = ((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0;
+      const int plane = 2 * tl.T[0] * tl.T[1];
+      int zbase = 2 * (((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0);
       for (int iz = 0; iz < w; ++iz) {
         const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
         const TC zr = vr * kzv, zi = vi * kzv;
@@ -164,10 +168,10 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
         for (int iy = 0; iy < w; ++iy) {
           const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
           if (on) {
-            acc_add(&sre[idx], zr * kyv);
-            acc_add(&sim[idx], zi * kyv);
+            acc_add(&sacc[idx], zr * kyv);
+            acc_add(&sacc[idx + 1], zi * kyv);
           }
-          idx += tl.T[0];
+          idx += 2 * tl.T[0];
         }
         zbase += plane;
       }
@@ -175,11 +179,29 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
   }
   __syncthreads();
 
-  cplx_t<TC>* ft = fine + (int64_t)t * nftot;
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
+  if constexpr (kFixed && DIM > 1) {
+    if (tmap != nullptr && tl.interior(g)) {
+      // fixed point -> float in place, then one bulk reduce-add of the box
+      for (int i = threadIdx.x; i < 2 * tl.ncell; i += kThreads)
+        sacc[i] = __float_as_int((TC)sacc[i] * inv);
+      fence_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        if (DIM == 2)
+          tma_reduce_add_2d(tmap, sacc, 2 * tl.org[0], tl.org[1] + t_map * nf1);
+        else
+          tma_reduce_add_3d(tmap, sacc, 2 * tl.org[0], tl.org[1], tl.org[2] + t_map * nf2);
+        bulk_commit();
+        bulk_wait_read();  // the tile stays allocated until the copy has read it
+      }
+      return;
+    }
+  }
+  cplx_t<TC>* ft = fine + (int64_t)t * nftot;
   CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
   for (int i = threadIdx.x; i < tl.ncell; i += kThreads, cw.next()) {
-    const A ar = sre[i], ai = sim[i];
+    const A ar = sacc[2 * i], ai = sacc[2 * i + 1];
     if (ar == A(0) && ai == A(0)) continue;
     const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
     const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
@@ -192,10 +214,12 @@ template <typename TC, typename TD, int DIM, int G>
 __global__ void __launch_bounds__(kThreads)
     spread_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
                      SubArgs sa, const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ fine,
-                     int64_t nftot) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+                     int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
+                     int t_base) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   spread_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, c, fine, nftot,
-                                  smem_raw);
+                                  smem_raw, use_tma ? &tmap : nullptr,
+                                  t_base + (int)blockIdx.y);
 }
 
 template <typename TC, typename TD, int DIM, int G>
@@ -308,7 +332,7 @@ cudaError_t run_spread_queue(const BatchProb<TC>* probs, int K, const int64_t* i
 template <typename TC, typename TD, int DIM, int G>
 cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                        const SortState& st, const void* c, void* fine, int ntr,
-                       cudaStream_t s) {
+                       cudaStream_t s, const CUtensorMap* tmap) {
   SubArgs sa;
   sa.sub_bin = st.sub_bin;
   sa.sub_off = st.sub_off;
@@ -328,14 +352,17 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     const cplx_t<TD>* ct = (const cplx_t<TD>*)c + (int64_t)t0 * M;
     cplx_t<TC>* ft = (cplx_t<TC>*)fine + (int64_t)t0 * nftot;
     if (method == 2 && sa.sorted) {
-      int64_t ncell = 1;
-      for (int d = 0; d < DIM; ++d) ncell *= g.bs[d] + g.w - 1;
+      const int64_t ncell = tile_cells(DIM, g.bs, g.w);
       const size_t smem = (size_t)ncell * 2 * sizeof(typename Acc<TC>::type);
       auto kern = spread_sm_kernel<TC, TD, DIM, G>;
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
       if (e != cudaSuccess) return e;
-      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ct, ft, nftot);
+      CUtensorMap m;
+      memset(&m, 0, sizeof(m));
+      const int use = tmap != nullptr && sizeof(TC) == 4;
+      if (use) m = *tmap;
+      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ct, ft, nftot, m, use, t0);
       note_launch();
     } else {
       spread_gm_kernel<TC, TD, DIM, G><<<grid, kThreads, 0, s>>>(g, ks, M, recs, sa, ct, ft,
@@ -353,31 +380,31 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
 template <typename TC, typename TD>
 cudaError_t launch_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                           const SortState& st, const void* c, void* fine, int ntr,
-                          cudaStream_t s) {
+                          cudaStream_t s, const CUtensorMap* tmap) {
   if (M == 0) return cudaSuccess;
   const bool wide = g.w > 8;
   switch (g.dim) {
     case 1:
-      return wide ? run_spread<TC, TD, 1, 16>(g, ks, method, M, st, c, fine, ntr, s)
-                  : run_spread<TC, TD, 1, 8>(g, ks, method, M, st, c, fine, ntr, s);
+      return wide ? run_spread<TC, TD, 1, 16>(g, ks, method, M, st, c, fine, ntr, s, nullptr)
+                  : run_spread<TC, TD, 1, 8>(g, ks, method, M, st, c, fine, ntr, s, nullptr);
     case 2:
-      return wide ? run_spread<TC, TD, 2, 16>(g, ks, method, M, st, c, fine, ntr, s)
-                  : run_spread<TC, TD, 2, 8>(g, ks, method, M, st, c, fine, ntr, s);
+      return wide ? run_spread<TC, TD, 2, 16>(g, ks, method, M, st, c, fine, ntr, s, tmap)
+                  : run_spread<TC, TD, 2, 8>(g, ks, method, M, st, c, fine, ntr, s, tmap);
     default:
-      return wide ? run_spread<TC, TD, 3, 16>(g, ks, method, M, st, c, fine, ntr, s)
-                  : run_spread<TC, TD, 3, 8>(g, ks, method, M, st, c, fine, ntr, s);
+      return wide ? run_spread<TC, TD, 3, 16>(g, ks, method, M, st, c, fine, ntr, s, tmap)
+                  : run_spread<TC, TD, 3, 8>(g, ks, method, M, st, c, fine, ntr, s, tmap);
   }
 }
 
 template cudaError_t launch_spread<float, float>(const Geom&, const KerSpec<float>&, int,
                                                  int64_t, const SortState&, const void*, void*,
-                                                 int, cudaStream_t);
+                                                 int, cudaStream_t, const CUtensorMap*);
 template cudaError_t launch_spread<float, double>(const Geom&, const KerSpec<float>&, int,
                                                   int64_t, const SortState&, const void*, void*,
-                                                  int, cudaStream_t);
+                                                  int, cudaStream_t, const CUtensorMap*);
 template cudaError_t launch_spread<double, double>(const Geom&, const KerSpec<double>&, int,
                                                    int64_t, const SortState&, const void*,
-                                                   void*, int, cudaStream_t);
+                                                   void*, int, cudaStream_t, const CUtensorMap*);
 
 
 template <typename TC, typename TD>
