@@ -52,6 +52,7 @@ struct Geom {
   int nb[3];
   int64_t nbins;
   int maxsub;
+  int stash;  // spread: a subproblem's strengths are staged in shared memory after the tile
 };
 
 // Shared-memory tile of one bin: bs + w - 1 cells per axis from the bin's
@@ -63,6 +64,18 @@ __host__ __device__ inline int64_t tile_cells(int dim, const int* bs, int w) {
   int64_t n = tile_x(bs[0], w);
   for (int d = 1; d < dim; ++d) n *= bs[d] + w - 1;
   return n;
+}
+
+// Shared memory of one shared-memory spread block: the accumulator tile (two
+// 4-byte integers per cell in FP32, two doubles in FP64) and, with g.stash,
+// the subproblem's strengths in the compute precision (16-byte aligned).
+__host__ __device__ inline size_t spread_tile_bytes(int dim, const int* bs, int w, bool single) {
+  return ((size_t)tile_cells(dim, bs, w) * 2 * (single ? 4 : 8) + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t spread_smem_bytes(int dim, const int* bs, int w, bool single,
+                                                    int maxsub, bool stash) {
+  return spread_tile_bytes(dim, bs, w, single) +
+         (stash ? (size_t)maxsub * 2 * (single ? 4 : 8) : 0);
 }
 
 // How points map onto the grid: mode 0 folds periodically (types 1/2),

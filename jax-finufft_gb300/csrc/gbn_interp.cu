@@ -126,11 +126,28 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
 
   cplx_t<TD>* ct = c + (int64_t)t * M;
   const bool lane_on = gl < w;
-  for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
+  constexpr int kStep = NWARP * PPW;
+  // each group's next point record and output index are loaded one
+  // iteration ahead, so their latency hides behind the current gather
+  PtRec<TC, DIM> rn;
+  int on_next = 0;
+  if (warp * PPW < cnt) {
+    const int pn = warp * PPW + grp;
+    const int jn = start + (pn < cnt ? pn : 0);
+    rn = recs[jn];
+    on_next = sa.perm ? sa.perm[jn] : jn;
+  }
+  for (int pb = warp * PPW; pb < cnt; pb += kStep) {
     const int pi = pb + grp;
     const bool valid = pi < cnt;
-    const int js = start + (valid ? pi : 0);
-    const PtRec<TC, DIM> r = recs[js];
+    const PtRec<TC, DIM> r = rn;
+    const int out_idx = on_next;
+    if (pb + kStep < cnt) {
+      const int pn = pb + kStep + grp;
+      const int jn = start + (pn < cnt ? pn : 0);
+      rn = recs[jn];
+      on_next = sa.perm ? sa.perm[jn] : jn;
+    }
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
     const int l0 = r.i[0] - org[0] + gl;
     TC ar = TC(0), ai = TC(0);
@@ -182,7 +199,7 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
       cplx_t<TD> o;
       o.x = (TD)ar;
       o.y = (TD)ai;
-      ct[sa.perm ? sa.perm[js] : js] = o;
+      ct[out_idx] = o;
     }
   }
 }

@@ -428,6 +428,9 @@ void setup_geom(gbn_plan_s* p) {
     g.nbins *= g.nb[d];
   }
   g.maxsub = p->opts.gpu_maxsubprobsize > 0 ? p->opts.gpu_maxsubprobsize : 1024;
+  // stage each subproblem's strengths in shared memory when it still fits
+  g.stash = method == 2 && spread_smem_bytes(p->dim, bs, p->w, p->comp_single, g.maxsub, true) <=
+                               smem_limit;
 }
 
 int upload_doubles_as(const std::vector<double>& v, bool single, DevBuf& buf, cudaStream_t s) {
@@ -1579,7 +1582,8 @@ int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, c
     if (p->method != 2 || !p->sorted) b->queue = false;
     b->comp_single = p->comp_single;
     if (p->w > 8) b->wide = true;
-    const size_t tb = tile_bytes(dim, p->geom.bs, p->w, p->comp_single);
+    const size_t tb = spread_smem_bytes(dim, p->geom.bs, p->w, p->comp_single,
+                                        p->geom.maxsub, p->geom.stash != 0);
     b->smem = std::max(b->smem, tb);
     if (M[k] < 0) return fail(GBN_ERR_ARGS, "negative number of points");
     b->M.push_back(M[k]);

@@ -7,6 +7,8 @@
 // once with coalesced accesses.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdint>
 
 #include "gbn_common.cuh"
@@ -259,38 +261,65 @@ __global__ void deconv1_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2
   }
 }
 
+// One block per item = up to 512 cells of one fine-grid row (x line): the
+// row's y/z mode indices are resolved once, each thread writes two cells with
+// one 16-byte store per transform (zero outside the mode region, so the
+// padding needs no memset).  Rows outside the mode region are pure zero
+// stores.
 template <typename TC, typename TD, int DIM>
-__global__ void deconv2_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
-                               const TC* __restrict__ p0, const TC* __restrict__ p1,
-                               const TC* __restrict__ p2, const cplx_t<TD>* __restrict__ in,
-                               cplx_t<TC>* __restrict__ fine, int ntr, int64_t nftot,
-                               int64_t Ntot) {
-  const int g0 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g0 >= nf0) return;
-  const int i0 = (int)fine_to_mode(g0, N0, nf0, modeord);
-  const TC f0 = i0 >= 0 ? p0[i0] : TC(0);
-  for (int g2 = blockIdx.z; g2 < nf2; g2 += gridDim.z) {
+__global__ void __launch_bounds__(256)
+    deconv2_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
+                   const TC* __restrict__ p0, const TC* __restrict__ p1,
+                   const TC* __restrict__ p2, const cplx_t<TD>* __restrict__ in,
+                   cplx_t<TC>* __restrict__ fine, int ntr, int64_t nftot, int64_t Ntot) {
+  const int nrows = nf1 * nf2;
+  const int npair = nf0 >> 1;  // nf0 is even
+  const int nchunk = (npair + blockDim.x - 1) / blockDim.x;  // blockDim.x pairs per item
+  for (int item = blockIdx.x; item < nrows * nchunk; item += gridDim.x) {
+    const int row = item / nchunk, chunk = item - row * nchunk;
+    const int g1 = DIM > 1 ? row % nf1 : 0;
+    const int g2 = DIM > 2 ? row / nf1 : 0;
+    const int i1 = DIM > 1 ? (int)fine_to_mode(g1, N1, nf1, modeord) : 0;
     const int i2 = DIM > 2 ? (int)fine_to_mode(g2, N2, nf2, modeord) : 0;
-    for (int g1 = blockIdx.y; g1 < nf1; g1 += gridDim.y) {
-      const int i1 = DIM > 1 ? (int)fine_to_mode(g1, N1, nf1, modeord) : 0;
-      const int dst = (g2 * nf1 + g1) * nf0 + g0;
-      cplx_t<TC> o;
-      o.x = TC(0);
-      o.y = TC(0);
-      if (i0 >= 0 && i1 >= 0 && i2 >= 0) {
-        TC f = f0;
-        if (DIM > 1) f *= p1[i1];
-        if (DIM > 2) f *= p2[i2];
-        const int src = (i2 * N1 + i1) * N0 + i0;
-        for (int t = 0; t < ntr; ++t) {
-          const cplx_t<TD> v = in[t * Ntot + src];
-          cplx_t<TC> r;
-          r.x = (TC)v.x * f;
-          r.y = (TC)v.y * f;
-          fine[t * nftot + dst] = r;
+    const bool live = i1 >= 0 && i2 >= 0;
+    TC f12 = TC(1);
+    if (live) {
+      if (DIM > 1) f12 *= p1[i1];
+      if (DIM > 2) f12 *= p2[i2];
+    }
+    const int64_t dst_row = (int64_t)row * nf0;
+    const int64_t src_row = live ? ((int64_t)i2 * N1 + i1) * N0 : 0;
+    const int q = chunk * blockDim.x + threadIdx.x;
+    if (q < npair) {
+      const int g0 = 2 * q;
+      int ia = -1, ib = -1;
+      TC fa = TC(0), fb = TC(0);
+      if (live) {
+        ia = (int)fine_to_mode(g0, N0, nf0, modeord);
+        ib = (int)fine_to_mode(g0 + 1, N0, nf0, modeord);
+        if (ia >= 0) fa = p0[ia] * f12;
+        if (ib >= 0) fb = p0[ib] * f12;
+      }
+      for (int t = 0; t < ntr; ++t) {
+        cplx_t<TC> a, b;
+        a.x = a.y = b.x = b.y = TC(0);
+        if (ia >= 0) {
+          const cplx_t<TD> v = in[t * Ntot + src_row + ia];
+          a.x = (TC)v.x * fa;
+          a.y = (TC)v.y * fa;
         }
-      } else {
-        for (int t = 0; t < ntr; ++t) fine[t * nftot + dst] = o;
+        if (ib >= 0) {
+          const cplx_t<TD> v = in[t * Ntot + src_row + ib];
+          b.x = (TC)v.x * fb;
+          b.y = (TC)v.y * fb;
+        }
+        cplx_t<TC>* d = fine + t * nftot + dst_row + g0;  // even cell: 16-byte aligned pair
+        if constexpr (sizeof(TC) == 4) {
+          *reinterpret_cast<float4*>(d) = make_float4(a.x, a.y, b.x, b.y);
+        } else {
+          d[0] = a;
+          d[1] = b;
+        }
       }
     }
   }
@@ -609,12 +638,15 @@ cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int mod
                            const TC* const* phi, const void* in, void* fine, int ntr,
                            cudaStream_t s) {
   const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
-  dim3 grid(grid1(nf[0], 128), (unsigned)(nf[1] < 65535 ? nf[1] : 65535),
-            (unsigned)(nf[2] < 65535 ? nf[2] : 65535));
+  const int64_t items = nf[1] * nf[2] * ((nf[0] / 2 + 255) / 256);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)std::min<int64_t>(items, (int64_t)nsm * 16);
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
   auto args = [&](auto kern) {
-    kern<<<grid, 128, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
+    kern<<<grid, 256, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
                               (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TD>*)in,
                               (cplx_t<TC>*)fine, ntr, nftot, Ntot);
   };

@@ -103,16 +103,28 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
   const cplx_t<TD>* ct = c + (int64_t)t * M;
 
-  // fixed-point scale from the subproblem's strengths
+  // one pass over the subproblem's strengths: stage them in shared memory
+  // (g.stash) and, in FP32, take the fixed-point scale from them
+  cplx_t<TC>* cst = reinterpret_cast<cplx_t<TC>*>(
+      smem_raw + spread_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4));
+  const bool stash = g.stash != 0;
   TC scale = TC(1), inv = TC(1);
-  if (kFixed) {
-    TC part = TC(0);
+  TC part = TC(0);
+  if (kFixed || stash) {
     for (int p = threadIdx.x; p < cnt; p += kThreads) {
       const int js = start + p;
       TC re, im;
       load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), re, im);
+      if (stash) {
+        cplx_t<TC> v;
+        v.x = re;
+        v.y = im;
+        cst[p] = v;
+      }
       part += fmax(fabs(re), fabs(im));
     }
+  }
+  if (kFixed) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if (lane == 0) s_red[warp] = part;
@@ -126,16 +138,35 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
   }
   TC co[NCO];
   load_coef<TC, NCO>(co, ks, gl, w);
-  __syncthreads();
+  __syncthreads();  // tile cleared, strengths staged
 
   const bool lane_on = gl < w;
-  for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
+  constexpr int kStep = NWARP * PPW;
+  // each group's next point record is loaded one iteration ahead
+  PtRec<TC, DIM> rn;
+  if (warp * PPW < cnt) {
+    const int pn = warp * PPW + grp;
+    rn = recs[start + (pn < cnt ? pn : 0)];
+  }
+  for (int pb = warp * PPW; pb < cnt; pb += kStep) {
     const int pi = pb + grp;
     const bool valid = pi < cnt;
     const int js = start + (valid ? pi : 0);
-    const PtRec<TC, DIM> r = recs[js];
+    const PtRec<TC, DIM> r = rn;
+    if (pb + kStep < cnt) {
+      const int pn = pb + kStep + grp;
+      rn = recs[start + (pn < cnt ? pn : 0)];
+    }
     TC cr = TC(0), ci = TC(0);
-    if (valid) load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), cr, ci);
+    if (valid) {
+      if (stash) {
+        const cplx_t<TC> v = cst[pi];
+        cr = v.x;
+        ci = v.y;
+      } else {
+        load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), cr, ci);
+      }
+    }
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w) * scale;
     const int l0 = r.i[0] - tl.org[0] + gl;
     const bool on = valid && lane_on;
@@ -352,8 +383,8 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     const cplx_t<TD>* ct = (const cplx_t<TD>*)c + (int64_t)t0 * M;
     cplx_t<TC>* ft = (cplx_t<TC>*)fine + (int64_t)t0 * nftot;
     if (method == 2 && sa.sorted) {
-      const int64_t ncell = tile_cells(DIM, g.bs, g.w);
-      const size_t smem = (size_t)ncell * 2 * sizeof(typename Acc<TC>::type);
+      const size_t smem =
+          spread_smem_bytes(DIM, g.bs, g.w, sizeof(TC) == 4, g.maxsub, g.stash != 0);
       auto kern = spread_sm_kernel<TC, TD, DIM, G>;
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
