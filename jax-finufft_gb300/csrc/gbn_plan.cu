@@ -328,6 +328,12 @@ struct gbn_plan_s {
 
   // cuFFT plans by batch count (fine grids per exec)
   std::vector<std::pair<int, cufftHandle>> ffts;
+  // pruned 3D FFT: 2D plans over the low and high planes of the mode region
+  // and one strided 1D plan along z, sharing one work area
+  cufftHandle fft_lo = 0, fft_hi = 0, fft_z = 0;
+  int64_t prune_lo = 0, prune_hi = 0;
+  int prune_state = 0;  // 0 not tried, 1 ready, -1 not applicable
+  DevBuf fft_work;
 
   // type 3
   std::unique_ptr<gbn_plan_s> inner;
@@ -351,6 +357,9 @@ struct gbn_plan_s {
     own.stream = stream;
     own.release();
     for (auto& h : ffts) cufftDestroy(h.second);
+    for (cufftHandle h : {fft_lo, fft_hi, fft_z})
+      if (h) cufftDestroy(h);
+    fft_work.release(stream);
     for (auto& e : ev_exec) cudaEventDestroy(e);
     for (auto& e : ev_setpts) cudaEventDestroy(e);
     cudaStreamSynchronize(stream);
@@ -480,8 +489,81 @@ int make_fft(gbn_plan_s* p, int nbatch, cufftHandle* h) {
   return GBN_OK;
 }
 
+// Pruned 3D FFT plans (see exec_fft).  The mode region along z holds the
+// planes [0, lo) and [nf2 - hi, nf2).
+int make_pruned_fft(gbn_plan_s* p) {
+  const int nf0 = (int)p->nf[0], nf1 = (int)p->nf[1], nf2 = (int)p->nf[2];
+  const int64_t N2 = p->N[2];
+  const int64_t lo = (N2 - 1) / 2 + 1, hi = N2 / 2;
+  if (p->dim != 3 || lo + hi >= nf2) return GBN_ERR_ARGS;
+  const cufftType ty = p->comp_single ? CUFFT_C2C : CUFFT_Z2Z;
+  const int plane = nf0 * nf1;
+  size_t ws[3] = {0, 0, 0};
+  cufftHandle* hs[3] = {&p->fft_lo, &p->fft_hi, &p->fft_z};
+  for (cufftHandle* h : hs) {
+    if (cufftCreate(h) != CUFFT_SUCCESS || cufftSetAutoAllocation(*h, 0) != CUFFT_SUCCESS)
+      return fail(GBN_ERR_CUFFT, "cufftCreate failed");
+  }
+  int n2[2] = {nf1, nf0};
+  cufftResult r = cufftMakePlanMany(p->fft_lo, 2, n2, nullptr, 1, plane, nullptr, 1, plane, ty,
+                                    (int)lo, &ws[0]);
+  if (r == CUFFT_SUCCESS && hi > 0)
+    r = cufftMakePlanMany(p->fft_hi, 2, n2, nullptr, 1, plane, nullptr, 1, plane, ty, (int)hi,
+                          &ws[1]);
+  int nz[1] = {nf2}, emb[1] = {nf2};
+  if (r == CUFFT_SUCCESS)
+    r = cufftMakePlanMany(p->fft_z, 1, nz, emb, plane, 1, emb, plane, 1, ty, plane, &ws[2]);
+  if (r != CUFFT_SUCCESS)
+    return fail(GBN_ERR_CUFFT, "pruned cufftMakePlanMany failed with code " + std::to_string((int)r));
+  const size_t work = std::max(ws[0], std::max(ws[1], ws[2]));
+  GBN_CUDA(p->fft_work.ensure(std::max<size_t>(work, 256), p->stream));
+  for (cufftHandle* h : hs)
+    if (cufftSetWorkArea(*h, p->fft_work.p) != CUFFT_SUCCESS)
+      return fail(GBN_ERR_CUFFT, "cufftSetWorkArea failed");
+  p->prune_lo = lo;
+  p->prune_hi = hi;
+  return GBN_OK;
+}
+
+int fft_exec(gbn_plan_s* p, cufftHandle h, void* data, int dir) {
+  cufftSetStream(h, p->stream);
+  const cufftResult r =
+      p->comp_single ? cufftExecC2C(h, (cufftComplex*)data, (cufftComplex*)data, dir)
+                     : cufftExecZ2Z(h, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, dir);
+  if (r != CUFFT_SUCCESS)
+    return fail(GBN_ERR_CUFFT, "cufftExec failed with code " + std::to_string((int)r));
+  return GBN_OK;
+}
+
 // In-place batched FFT of nb fine grids at buf with exponent sign `sign`.
-int exec_fft(gbn_plan_s* p, void* buf, int nb, int sign) {
+// kind 1: the input is zero outside the mode region (zero-padded modes);
+// kind 2: only the mode region of the output is read afterwards.  For a
+// large 3D grid either lets the FFT skip the planes outside the mode region
+// along z: kind 1 transforms (x, y) on the mode region's planes, then z on
+// every column; kind 2 transforms z first, then (x, y) on those planes only
+// (the other planes are left partially transformed).  1/sigma of the plane
+// work instead of all of it.  kind 0 (or GBN_DISABLE_FFT_PRUNING=1): the
+// full transform.
+int exec_fft(gbn_plan_s* p, void* buf, int nb, int sign, int kind = 0) {
+  const int dir = sign >= 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
+  const char* no_prune = std::getenv("GBN_DISABLE_FFT_PRUNING");
+  if (no_prune && no_prune[0] == '1') kind = 0;
+  if (kind != 0 && p->dim == 3 && nb <= 8 && p->nftot >= ((int64_t)1 << 21)) {
+    if (p->prune_state == 0) p->prune_state = make_pruned_fft(p) == GBN_OK ? 1 : -1;
+    if (p->prune_state == 1) {
+      const size_t csz = cplx_size(p->comp_single);
+      const size_t plane = (size_t)p->nf[0] * p->nf[1] * csz;
+      for (int t = 0; t < nb; ++t) {
+        char* g = (char*)buf + (size_t)t * p->nftot * csz;
+        char* g_hi = g + (size_t)(p->nf[2] - p->prune_hi) * plane;
+        if (kind == 2) GBN_TRY(fft_exec(p, p->fft_z, g, dir));
+        GBN_TRY(fft_exec(p, p->fft_lo, g, dir));
+        if (p->prune_hi > 0) GBN_TRY(fft_exec(p, p->fft_hi, g_hi, dir));
+        if (kind == 1) GBN_TRY(fft_exec(p, p->fft_z, g, dir));
+      }
+      return GBN_OK;
+    }
+  }
   cufftHandle h = 0;
   for (auto& e : p->ffts)
     if (e.first == nb) h = e.second;
@@ -493,15 +575,7 @@ int exec_fft(gbn_plan_s* p, void* buf, int nb, int sign) {
       p->ffts.erase(p->ffts.begin());
     }
   }
-  cufftSetStream(h, p->stream);
-  const int dir = sign >= 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
-  cufftResult r;
-  if (p->comp_single)
-    r = cufftExecC2C(h, (cufftComplex*)buf, (cufftComplex*)buf, dir);
-  else
-    r = cufftExecZ2Z(h, (cufftDoubleComplex*)buf, (cufftDoubleComplex*)buf, dir);
-  if (r != CUFFT_SUCCESS) return fail(GBN_ERR_CUFFT, "cufftExec failed with code " + std::to_string((int)r));
-  return GBN_OK;
+  return fft_exec(p, h, buf, dir);
 }
 
 // Resolve compute precision; returns an error for unsupported combinations.
@@ -904,7 +978,7 @@ int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int 
       GBN_CUDA(cudaMemsetAsync(p->fine.p, 0, (size_t)nb * p->nftot * csz, s));
       GBN_TRY(do_spread(p, ps, cb, nb, false, p->fine.p));
       ev_record(ev, 1, s);
-      GBN_TRY(exec_fft(p, p->fine.p, nb, sign));
+      GBN_TRY(exec_fft(p, p->fine.p, nb, sign, 2));
       ev_record(ev, 2, s);
       GBN_TRY(do_deconv(p, fb, nb, true, p->fine.p));
       ev_record(ev, 3, s);
@@ -914,7 +988,7 @@ int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int 
       ev_record(ev, 0, s);
       GBN_TRY(do_deconv(p, (void*)fb, nb, false, p->fine.p));
       ev_record(ev, 1, s);
-      GBN_TRY(exec_fft(p, p->fine.p, nb, sign));
+      GBN_TRY(exec_fft(p, p->fine.p, nb, sign, 1));
       ev_record(ev, 2, s);
       GBN_TRY(do_interp(p, ps, cb, nb, p->fine.p));
       ev_record(ev, 3, s);
@@ -1007,7 +1081,7 @@ int plan_grad(gbn_plan_s* p, gbn_points_s& ps, int ntr, const void* src, const v
                                           p->gfine.p, nb, E, base, dims, a_re, a_im, s);
     }
     GBN_CUDA(e);
-    GBN_TRY(exec_fft(p, p->gfine.p, nb * E, sign));
+    GBN_TRY(exec_fft(p, p->gfine.p, nb * E, sign, 1));
     if (p->comp_single) {
       e = p->data_single
               ? launch_interp_grad<float, float>(p->geom, ker_spec<float>(p), ps.M, ps.st,
