@@ -158,38 +158,42 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
         ai = v.y;
       }
     } else if (DIM == 2) {
+      // the group's y kernel values, fetched once per point
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      int idx = (r.i[1] - org[1]) * T[0] + l0;
-      for (int iy = 0; iy < w; ++iy) {
-        const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-        if (lane_on) {
-          const cplx_t<TC> v = tile[idx];
-          ar = fma(v.x, kyv, ar);
-          ai = fma(v.y, kyv, ai);
+      TC kyr[G];
+#pragma unroll
+      for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
+      const cplx_t<TC>* col = tile + (r.i[1] - org[1]) * T[0] + l0;
+#pragma unroll
+      for (int iy = 0; iy < G; ++iy) {
+        if (iy < w && lane_on) {
+          const cplx_t<TC> v = col[iy * T[0]];
+          ar = fma(v.x, kyr[iy], ar);
+          ai = fma(v.y, kyr[iy], ai);
         }
-        idx += T[0];
       }
     } else {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
+      TC kyr[G];
+#pragma unroll
+      for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
       const int plane = T[0] * T[1];
-      int zbase = ((r.i[2] - org[2]) * T[1] + (r.i[1] - org[1])) * T[0] + l0;
+      const cplx_t<TC>* zrow = tile + ((r.i[2] - org[2]) * T[1] + (r.i[1] - org[1])) * T[0] + l0;
       for (int iz = 0; iz < w; ++iz) {
         const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
         TC yr = TC(0), yi = TC(0);
-        int idx = zbase;
-        for (int iy = 0; iy < w; ++iy) {
-          const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-          if (lane_on) {
-            const cplx_t<TC> v = tile[idx];
-            yr = fma(v.x, kyv, yr);
-            yi = fma(v.y, kyv, yi);
+#pragma unroll
+        for (int iy = 0; iy < G; ++iy) {
+          if (iy < w && lane_on) {
+            const cplx_t<TC> v = zrow[iy * T[0]];
+            yr = fma(v.x, kyr[iy], yr);
+            yi = fma(v.y, kyr[iy], yi);
           }
-          idx += T[0];
         }
         ar = fma(yr, kzv, ar);
         ai = fma(yi, kzv, ai);
-        zbase += plane;
+        zrow += plane;
       }
     }
     ar *= kx;

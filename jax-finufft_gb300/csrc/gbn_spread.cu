@@ -177,34 +177,40 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
         acc_add(&sacc[2 * l0 + 1], vi);
       }
     } else if (DIM == 2) {
+      // the group's y kernel values, fetched once per point
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      int idx = 2 * ((r.i[1] - tl.org[1]) * tl.T[0] + l0);
-      for (int iy = 0; iy < w; ++iy) {
-        const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-        if (on) {
-          acc_add(&sacc[idx], vr * kyv);
-          acc_add(&sacc[idx + 1], vi * kyv);
+      TC kyr[G];
+#pragma unroll
+      for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
+      A* col = sacc + 2 * ((r.i[1] - tl.org[1]) * tl.T[0] + l0);
+      const int pitch = 2 * tl.T[0];
+#pragma unroll
+      for (int iy = 0; iy < G; ++iy) {
+        if (iy < w && on) {
+          acc_add(&col[iy * pitch], vr * kyr[iy]);
+          acc_add(&col[iy * pitch + 1], vi * kyr[iy]);
         }
-        idx += 2 * tl.T[0];
       }
     } else {
       const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
       const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
+      TC kyr[G];
+#pragma unroll
+      for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
       const int plane = 2 * tl.T[0] * tl.T[1];
-      int zbase = 2 * (((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0);
+      const int pitch = 2 * tl.T[0];
+      A* zrow = sacc + 2 * (((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0);
       for (int iz = 0; iz < w; ++iz) {
         const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
         const TC zr = vr * kzv, zi = vi * kzv;
-        int idx = zbase;
-        for (int iy = 0; iy < w; ++iy) {
-          const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-          if (on) {
-            acc_add(&sacc[idx], zr * kyv);
-            acc_add(&sacc[idx + 1], zi * kyv);
+#pragma unroll
+        for (int iy = 0; iy < G; ++iy) {
+          if (iy < w && on) {
+            acc_add(&zrow[iy * pitch], zr * kyr[iy]);
+            acc_add(&zrow[iy * pitch + 1], zi * kyr[iy]);
           }
-          idx += 2 * tl.T[0];
         }
-        zbase += plane;
+        zrow += plane;
       }
     }
   }
