@@ -7,10 +7,15 @@ namespace gbn {
 
 // Lanes per point: a group of G consecutive lanes handles one point, lane gl
 // owning piece gl of the kernel (x offset gl of the w-wide support).
-// G = 8 covers w <= 8, G = 16 covers w <= 16.  NCO is the number of Horner
+// G = 6 covers w <= 6, G = 8 covers w <= 8, G = 16 covers w <= 16; a warp
+// holds 32 / G groups (lanes past the last whole group stay idle).  NCO is the number of Horner
 // coefficients held in registers (degree w + 2, zero-padded).
 template <int G>
 struct GroupCfg;
+template <>
+struct GroupCfg<6> {
+  static constexpr int NCO = 9;  // w <= 6: five groups per warp, lanes 30-31 idle
+};
 template <>
 struct GroupCfg<8> {
   static constexpr int NCO = 11;

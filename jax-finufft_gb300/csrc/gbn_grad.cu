@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kThreads)
   const int dd[4] = {dims.x, dims.y, dims.z, dims.w};
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
-    const bool valid = pi < cnt;
+    const bool valid = pi < cnt && grp < PPW;
     const int js = start + (valid ? pi : 0);
     const PtRec<TC, DIM> r = recs[js];
     const int idx = sa.perm ? sa.perm[js] : js;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kThreads)
   TD* gxe = e >= base ? go.gx[dd[e]] : nullptr;
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
-    const bool valid = pi < cnt;
+    const bool valid = pi < cnt && grp < PPW;
     const int js = start + (valid ? pi : 0);
     const PtRec<TC, DIM> r = recs[js];
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);

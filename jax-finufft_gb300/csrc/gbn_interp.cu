@@ -57,10 +57,25 @@ __device__ __forceinline__ bool sub_range(const SubArgs& sa, const Geom& g, int6
 
 template <typename TC, int G>
 __device__ __forceinline__ void group_reduce(TC& a, TC& b) {
+  if constexpr ((G & (G - 1)) == 0) {
 #pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
+    for (int o = G / 2; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+  } else {
+    // tree towards the group's first lane, skipping partners past the group
+    constexpr int P = G > 8 ? 8 : G > 4 ? 4 : G > 2 ? 2 : 1;
+    const int gl = (threadIdx.x & 31) % G;
+#pragma unroll
+    for (int o = P; o > 0; o >>= 1) {
+      const TC ta = __shfl_down_sync(0xffffffffu, a, o);
+      const TC tb = __shfl_down_sync(0xffffffffu, b, o);
+      if (gl + o < G) {
+        a += ta;
+        b += tb;
+      }
+    }
   }
 }
 
@@ -139,7 +154,7 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
   }
   for (int pb = warp * PPW; pb < cnt; pb += kStep) {
     const int pi = pb + grp;
-    const bool valid = pi < cnt;
+    const bool valid = pi < cnt && grp < PPW;
     const PtRec<TC, DIM> r = rn;
     const int out_idx = on_next;
     if (pb + kStep < cnt) {
@@ -241,7 +256,7 @@ __global__ void __launch_bounds__(kThreads)
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
-    const bool valid = pi < cnt;
+    const bool valid = pi < cnt && grp < PPW;
     const int js = start + (valid ? pi : 0);
     const PtRec<TC, DIM> r = recs[js];
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
@@ -400,18 +415,21 @@ cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int6
                           const SortState& st, const void* fine, void* c, int ntr,
                           cudaStream_t s, const CUtensorMap* tmap) {
   if (M == 0) return cudaSuccess;
-  const bool wide = g.w > 8;
+  // lanes per point: the narrowest group that covers the kernel width
+  const int G = g.w > 8 ? 16 : g.w > 6 ? 8 : 6;
+#define GBN_DISPATCH(DIM, TM)                                        \
+  return G == 16 ? run_interp<TC, TD, DIM, 16>(g, ks, method, M, st, fine, c, ntr, s, TM)      \
+         : G == 8 ? run_interp<TC, TD, DIM, 8>(g, ks, method, M, st, fine, c, ntr, s, TM)      \
+                  : run_interp<TC, TD, DIM, 6>(g, ks, method, M, st, fine, c, ntr, s, TM);
   switch (g.dim) {
     case 1:
-      return wide ? run_interp<TC, TD, 1, 16>(g, ks, method, M, st, fine, c, ntr, s, nullptr)
-                  : run_interp<TC, TD, 1, 8>(g, ks, method, M, st, fine, c, ntr, s, nullptr);
+      GBN_DISPATCH(1, nullptr)
     case 2:
-      return wide ? run_interp<TC, TD, 2, 16>(g, ks, method, M, st, fine, c, ntr, s, tmap)
-                  : run_interp<TC, TD, 2, 8>(g, ks, method, M, st, fine, c, ntr, s, tmap);
+      GBN_DISPATCH(2, tmap)
     default:
-      return wide ? run_interp<TC, TD, 3, 16>(g, ks, method, M, st, fine, c, ntr, s, tmap)
-                  : run_interp<TC, TD, 3, 8>(g, ks, method, M, st, fine, c, ntr, s, tmap);
+      GBN_DISPATCH(3, tmap)
   }
+#undef GBN_DISPATCH
 }
 
 template cudaError_t launch_interp<float, float>(const Geom&, const KerSpec<float>&, int,

@@ -150,7 +150,7 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
   }
   for (int pb = warp * PPW; pb < cnt; pb += kStep) {
     const int pi = pb + grp;
-    const bool valid = pi < cnt;
+    const bool valid = pi < cnt && grp < PPW;
     const int js = start + (valid ? pi : 0);
     const PtRec<TC, DIM> r = rn;
     if (pb + kStep < cnt) {
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kThreads)
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
   for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
     const int pi = pb + grp;
-    const bool valid = pi < cnt;
+    const bool valid = pi < cnt && grp < PPW;
     const int js = start + (valid ? pi : 0);
     const PtRec<TC, DIM> r = recs[js];
     TC cr = TC(0), ci = TC(0);
@@ -419,18 +419,21 @@ cudaError_t launch_spread(const Geom& g, const KerSpec<TC>& ks, int method, int6
                           const SortState& st, const void* c, void* fine, int ntr,
                           cudaStream_t s, const CUtensorMap* tmap) {
   if (M == 0) return cudaSuccess;
-  const bool wide = g.w > 8;
+  // lanes per point: the narrowest group that covers the kernel width
+  const int G = g.w > 8 ? 16 : g.w > 6 ? 8 : 6;
+#define GBN_DISPATCH(DIM, TM)                                        \
+  return G == 16 ? run_spread<TC, TD, DIM, 16>(g, ks, method, M, st, c, fine, ntr, s, TM)      \
+         : G == 8 ? run_spread<TC, TD, DIM, 8>(g, ks, method, M, st, c, fine, ntr, s, TM)      \
+                  : run_spread<TC, TD, DIM, 6>(g, ks, method, M, st, c, fine, ntr, s, TM);
   switch (g.dim) {
     case 1:
-      return wide ? run_spread<TC, TD, 1, 16>(g, ks, method, M, st, c, fine, ntr, s, nullptr)
-                  : run_spread<TC, TD, 1, 8>(g, ks, method, M, st, c, fine, ntr, s, nullptr);
+      GBN_DISPATCH(1, nullptr)
     case 2:
-      return wide ? run_spread<TC, TD, 2, 16>(g, ks, method, M, st, c, fine, ntr, s, tmap)
-                  : run_spread<TC, TD, 2, 8>(g, ks, method, M, st, c, fine, ntr, s, tmap);
+      GBN_DISPATCH(2, tmap)
     default:
-      return wide ? run_spread<TC, TD, 3, 16>(g, ks, method, M, st, c, fine, ntr, s, tmap)
-                  : run_spread<TC, TD, 3, 8>(g, ks, method, M, st, c, fine, ntr, s, tmap);
+      GBN_DISPATCH(3, tmap)
   }
+#undef GBN_DISPATCH
 }
 
 template cudaError_t launch_spread<float, float>(const Geom&, const KerSpec<float>&, int,

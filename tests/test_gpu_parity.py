@@ -154,6 +154,9 @@ for _ndim, _ty in product([2, 3], [1, 2]):
         (_ndim, _ty, False, dict(modeord=1, gpu_method=2), "wide"),
         (_ndim, _ty, True, dict(gpu_binsizex=8, gpu_binsizey=8, gpu_binsizez=4), "cluster"),
     ]
+# narrow kernels (w = 3, 4): six-lane groups with idle lanes inside the group
+for _ndim, _ty in product([1, 2, 3], [1, 2]):
+    CASES.append((_ndim, _ty, True, dict(_eps=1e-2 if _ty == 1 else 1e-3), "cluster"))
 CASES += [(1, 1, True, dict(gpu_upsampfac=1.25), "cluster"),
           (1, 2, False, dict(gpu_method=1), "wide"),
           (3, 1, False, dict(gpu_method=2), "uniform"),
@@ -172,6 +175,8 @@ def test_against_oracle(jf, cn, ndim, ty, single, kw, kind):
     eps = 1e-5 if single else 1e-9
     if kw.get("gpu_precision") == 3:
         eps = 1e-6
+    kw = dict(kw)
+    eps = kw.pop("_eps", eps)
     rdt, cdt = (np.float32, np.complex64) if single else (np.float64, np.complex128)
     opts = _opts(**kw)
     mo = int(kw.get("modeord", 0))
