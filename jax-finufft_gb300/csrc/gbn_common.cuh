@@ -84,6 +84,8 @@ struct FoldSpec {
   int mode;
   double center[3];
   double scale[3];
+  double nf_d[3];  // (double)nf per axis, filled by launch_fold
+  double hw;       // w / 2, filled by launch_fold
 };
 
 // Kernel evaluation: piecewise Horner coefficients coef[piece*(deg+1)+n]

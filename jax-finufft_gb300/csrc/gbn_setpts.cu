@@ -25,17 +25,30 @@ constexpr double kInv2Pi = 0.159154943091895335768883763372514362;
 // s = fma(x - center, scale, nf/2 - w/2).  FP64 with one rounding per
 // operation, the order the CPU restatement uses (bit-identical results).
 // Non-finite coordinates are treated as 0 (mode 0) or as the centre (mode 1).
-__device__ __forceinline__ double grid_shift(double x, int mode, double center, double scale,
-                                             int64_t nf, int w) {
-  const double hw = 0.5 * (double)w;
+// nf_d = (double)nf and hw = w/2 come from the host (no per-point
+// conversions on the FP64 pipe); for 0 <= t < 1 the floor is 0 and for
+// -1 <= t < 0 it is -1, so f is t itself or the one rounded sum t + 1 --
+// the same operation t - (-1) -- and only other t take the general path.
+template <typename TX>
+__device__ __forceinline__ double grid_shift(TX xin, int mode, double center, double scale,
+                                             double nf_d, double hw) {
   if (mode == 0) {
-    if (!isfinite(x)) x = 0.0;
+    const double x = isfinite(xin) ? (double)xin : 0.0;
     const double t = __dmul_rn(x, kInv2Pi);
-    const double f = __dsub_rn(t, floor(t));
-    return __fma_rn(f, (double)nf, -hw);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    const bool neg = (b >> 63) != 0;
+    double f;
+    if (e < 0x3FFu && (!neg || (b << 1) == 0))
+      f = t;  // 0 <= t < 1 (or -0): t - 0
+    else if (neg && (e < 0x3FFu || b == 0xBFF0000000000000ull))
+      f = __dadd_rn(t, 1.0);  // -1 <= t < 0: t - (-1)
+    else
+      f = __dsub_rn(t, floor(t));
+    return __fma_rn(f, nf_d, -hw);
   }
-  const double d = isfinite(x) ? __dsub_rn(x, center) : 0.0;
-  return __fma_rn(d, scale, 0.5 * (double)nf - hw);
+  const double d = isfinite(xin) ? __dsub_rn((double)xin, center) : 0.0;
+  return __fma_rn(d, scale, __dmul_rn(0.5, nf_d) - hw);
 }
 
 // Fold, grid start and bin of every point.  The first grid index a point
@@ -59,8 +72,8 @@ __global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict
     const int h = g.w >> 1;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      const double sh = grid_shift((double)c[d][j], fs.mode, fs.center[d], fs.scale[d],
-                                   g.nf[d], g.w);
+      const double sh = grid_shift(c[d][j], fs.mode, fs.center[d], fs.scale[d], fs.nf_d[d],
+                                   fs.hw);
       const double cl = ceil(sh);
       int i0 = (int)cl;
       r.d[d] = (TC)__dsub_rn(cl, sh);
@@ -520,9 +533,12 @@ inline unsigned grid1(int64_t n, int threads) { return (unsigned)((n + threads -
 // =============================================================================
 
 template <typename TX, typename TC>
-cudaError_t launch_fold(const Geom& g, const FoldSpec& fs, int64_t M, const TX* x, const TX* y,
+cudaError_t launch_fold(const Geom& g, const FoldSpec& fs_in, int64_t M, const TX* x, const TX* y,
                         const TX* z, SortState& st, cudaStream_t s) {
   if (M == 0) return cudaSuccess;
+  FoldSpec fs = fs_in;
+  for (int d = 0; d < 3; ++d) fs.nf_d[d] = (double)g.nf[d];
+  fs.hw = 0.5 * (double)g.w;
   const unsigned nb = grid1(M, kThreads);
   const int count = st.bin_count != nullptr;
   switch (g.dim) {
