@@ -37,8 +37,10 @@ template <typename T>
 using cplx_t = typename Cplx<T>::type;
 
 // One nonuniform point after folding: offsets and grid starts per axis.
+// Aligned to 16 bytes when its natural size is a multiple of 16, else to 8,
+// so records move with 8/16-byte accesses instead of 4-byte ones.
 template <typename T, int DIM>
-struct PtRec {
+struct alignas((sizeof(T) * DIM + 4 * DIM) % 16 == 0 ? 16 : 8) PtRec {
   T d[DIM];
   int i[DIM];
 };
