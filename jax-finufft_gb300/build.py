@@ -90,6 +90,8 @@ def build(verbose=False, force=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s%s" % (name, r.stdout, r.stderr))
+        if r.stderr.strip():
+            print(r.stderr, file=sys.stderr, flush=True)  # warnings
         return obj
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kThreads)
   const int t = te / E, e = te - t * E;
   const int w = g.w;
   const Tile<DIM> tl(g, bin);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
   const cplx_t<TC>* ft = grids + (int64_t)te * nftot;
   {

@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kThreads)
     interp_queue_kernel(const BatchProb<TC>* __restrict__ probs, int K,
                         const int64_t* __restrict__ item_start, int* counter, int T,
                         const cplx_t<TC>* __restrict__ arena, cplx_t<TD>* __restrict__ c) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ int s_item;
   const int64_t total = item_start[K];
   for (;;) {
