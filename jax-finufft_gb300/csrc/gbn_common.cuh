@@ -68,11 +68,13 @@ __host__ __device__ inline int64_t tile_cells(int dim, const int* bs, int w) {
   return n;
 }
 
-// Shared memory of one shared-memory spread block: the accumulator tile (two
-// 4-byte integers per cell in FP32, two doubles in FP64) and, with g.stash,
-// the subproblem's strengths in the compute precision (16-byte aligned).
+// Shared memory of one shared-memory spread block: per transform an
+// accumulator tile (two 4-byte integers per cell in FP32, two doubles in
+// FP64) padded to 128 bytes -- the alignment a bulk tensor copy needs for its
+// shared-memory side -- and, with g.stash, the subproblem's strengths in the
+// compute precision.
 __host__ __device__ inline size_t spread_tile_bytes(int dim, const int* bs, int w, bool single) {
-  return ((size_t)tile_cells(dim, bs, w) * 2 * (single ? 4 : 8) + 15) & ~(size_t)15;
+  return ((size_t)tile_cells(dim, bs, w) * 2 * (single ? 4 : 8) + 127) & ~(size_t)127;
 }
 __host__ __device__ inline size_t spread_smem_bytes(int dim, const int* bs, int w, bool single,
                                                     int maxsub, bool stash) {
@@ -248,19 +250,23 @@ struct BatchProb {
   int64_t nftot;
 };
 
-// item_start[k] = T * sum_{i<k} n_sub_i for k = 0..K (device, one block).
+// item_start[k] = T * sum_{i<k} n_sub_i for k = 0..K (device, one block);
+// T here is the number of items per subproblem.
 template <typename TC>
 cudaError_t launch_item_prefix(const BatchProb<TC>* probs, int K, int T, int64_t* item_start,
                                cudaStream_t s);
 
 // Persistent spread/interp over every (problem, subproblem, transform) item
 // of a batch, pulled from one atomic counter (reset by the caller).
+// group = lanes per point (6, 8 or 16, covering the widest kernel); the
+// spread takes tb transforms per item (item_start counted in groups of tb)
+// and smem1 = one transform's shared memory.
 template <typename TC, typename TD>
-cudaError_t launch_spread_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+cudaError_t launch_spread_queue(int dim, int group, int tb, const BatchProb<TC>* probs, int K,
                                 const int64_t* item_start, int* counter, int T, const void* c,
-                                void* arena, size_t smem, cudaStream_t s);
+                                void* arena, size_t smem1, cudaStream_t s);
 template <typename TC, typename TD>
-cudaError_t launch_interp_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+cudaError_t launch_interp_queue(int dim, int group, const BatchProb<TC>* probs, int K,
                                 const int64_t* item_start, int* counter, int T,
                                 const void* arena, void* c, size_t smem, cudaStream_t s);
 

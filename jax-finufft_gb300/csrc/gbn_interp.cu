@@ -103,7 +103,7 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
   const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
   bool staged = false;
   if constexpr (sizeof(TC) == 4 && DIM > 1) {
-    if (tmap != nullptr && tl.interior(g)) {
+    if (tmap != nullptr && tl.interior(g) && (smem_addr(tile) & 127u) == 0) {
       __shared__ alignas(8) uint64_t s_bar;
       if (threadIdx.x == 0) {
         mbar_init(&s_bar, 1);
@@ -511,25 +511,30 @@ cudaError_t read_wait_timeouts(unsigned* out, bool reset) {
 }
 
 template <typename TC, typename TD>
-cudaError_t launch_interp_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+cudaError_t launch_interp_queue(int dim, int group, const BatchProb<TC>* probs, int K,
                                 const int64_t* item_start, int* counter, int T,
                                 const void* arena, void* c, size_t smem, cudaStream_t s) {
   if (K == 0) return cudaSuccess;
+#define GBN_QDISPATCH(DIM)                                                                     \
+  return group == 16 ? run_interp_queue<TC, TD, DIM, 16>(probs, K, item_start, counter, T,     \
+                                                         arena, c, smem, s)                    \
+         : group == 8 ? run_interp_queue<TC, TD, DIM, 8>(probs, K, item_start, counter, T,     \
+                                                         arena, c, smem, s)                    \
+                      : run_interp_queue<TC, TD, DIM, 6>(probs, K, item_start, counter, T,     \
+                                                         arena, c, smem, s);
   switch (dim) {
     case 1:
-      return wide ? run_interp_queue<TC, TD, 1, 16>(probs, K, item_start, counter, T, arena, c, smem, s)
-                  : run_interp_queue<TC, TD, 1, 8>(probs, K, item_start, counter, T, arena, c, smem, s);
+      GBN_QDISPATCH(1)
     case 2:
-      return wide ? run_interp_queue<TC, TD, 2, 16>(probs, K, item_start, counter, T, arena, c, smem, s)
-                  : run_interp_queue<TC, TD, 2, 8>(probs, K, item_start, counter, T, arena, c, smem, s);
+      GBN_QDISPATCH(2)
     default:
-      return wide ? run_interp_queue<TC, TD, 3, 16>(probs, K, item_start, counter, T, arena, c, smem, s)
-                  : run_interp_queue<TC, TD, 3, 8>(probs, K, item_start, counter, T, arena, c, smem, s);
+      GBN_QDISPATCH(3)
   }
+#undef GBN_QDISPATCH
 }
 
 #define GBN_INST_IQ(TC, TD)                                                                  \
-  template cudaError_t launch_interp_queue<TC, TD>(int, bool, const BatchProb<TC>*, int,     \
+  template cudaError_t launch_interp_queue<TC, TD>(int, int, const BatchProb<TC>*, int,     \
                                                    const int64_t*, int*, int, const void*,   \
                                                    void*, size_t, cudaStream_t);
 GBN_INST_IQ(float, float)

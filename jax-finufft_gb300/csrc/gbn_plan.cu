@@ -1585,8 +1585,10 @@ struct gbn_batch_s {
   std::vector<Group> groups;
   DevBuf arena, probs, item_start, counter;
   std::vector<unsigned char> probs_host;  // last uploaded table (stays alive for the copy)
-  bool queue = true, wide = false;
-  size_t smem = 0;
+  bool queue = true;
+  int group = 6;  // lanes per point of the queue kernels: 6, 8 or 16 (widest kernel)
+  int tb = 1;     // transforms per spread item
+  size_t smem = 0;  // one transform's shared memory (largest problem)
   cudaGraphExec_t gexec = nullptr;
   const void* gkey[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
@@ -1655,7 +1657,7 @@ int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, c
     b->sub.emplace_back(p);
     if (p->method != 2 || !p->sorted) b->queue = false;
     b->comp_single = p->comp_single;
-    if (p->w > 8) b->wide = true;
+    b->group = std::max(b->group, p->w > 8 ? 16 : p->w > 6 ? 8 : 6);
     const size_t tb = spread_smem_bytes(dim, p->geom.bs, p->w, p->comp_single,
                                         p->geom.maxsub, p->geom.stash != 0);
     b->smem = std::max(b->smem, tb);
@@ -1685,6 +1687,14 @@ int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, c
       ++g.count;
     }
     b->groups.push_back(g);
+  }
+  // stacked type-1 transforms share each point's kernel values in the queue
+  // kernel (FP32, up to 100 KB of shared memory per block)
+  if (type == 1 && b->comp_single && b->group <= 8) {
+    if (T >= 4 && 4 * b->smem <= 100 * 1024)
+      b->tb = 4;
+    else if (T >= 2 && 2 * b->smem <= 100 * 1024)
+      b->tb = 2;
   }
   const size_t csz = cplx_size(b->comp_single);
   cudaStream_t s = b->stream;
@@ -1745,11 +1755,12 @@ int batch_setpts(gbn_batch_s* b, const TX* x, const TX* y, const TX* z) {
     GBN_CUDA(cudaMemcpyAsync(b->probs.p, b->probs_host.data(), b->probs_host.size(),
                              cudaMemcpyHostToDevice, s));
   }
+  const int per_sub = b->type == 1 ? (b->T + b->tb - 1) / b->tb : b->T;  // items per subproblem
   cudaError_t e = b->comp_single
                       ? launch_item_prefix<float>((const BatchProb<float>*)b->probs.p, b->K,
-                                                  b->T, b->item_start.as<int64_t>(), s)
+                                                  per_sub, b->item_start.as<int64_t>(), s)
                       : launch_item_prefix<double>((const BatchProb<double>*)b->probs.p, b->K,
-                                                   b->T, b->item_start.as<int64_t>(), s);
+                                                   per_sub, b->item_start.as<int64_t>(), s);
   GBN_CUDA(e);
   return GBN_OK;
 }
@@ -1776,17 +1787,17 @@ int batch_execute(gbn_batch_s* b, void* c, void* f) {
     cudaError_t e;
     if (b->comp_single)
       e = b->data_single
-              ? launch_interp_queue<float, float>(b->dim, b->wide,
+              ? launch_interp_queue<float, float>(b->dim, b->group,
                                                   (const BatchProb<float>*)b->probs.p, b->K,
                                                   b->item_start.as<int64_t>(),
                                                   b->counter.as<int>(), b->T, arena, c, b->smem, s)
-              : launch_interp_queue<float, double>(b->dim, b->wide,
+              : launch_interp_queue<float, double>(b->dim, b->group,
                                                    (const BatchProb<float>*)b->probs.p, b->K,
                                                    b->item_start.as<int64_t>(),
                                                    b->counter.as<int>(), b->T, arena, c, b->smem,
                                                    s);
     else
-      e = launch_interp_queue<double, double>(b->dim, b->wide,
+      e = launch_interp_queue<double, double>(b->dim, b->group,
                                               (const BatchProb<double>*)b->probs.p, b->K,
                                               b->item_start.as<int64_t>(), b->counter.as<int>(),
                                               b->T, arena, c, b->smem, s);
@@ -1797,17 +1808,17 @@ int batch_execute(gbn_batch_s* b, void* c, void* f) {
     cudaError_t e;
     if (b->comp_single)
       e = b->data_single
-              ? launch_spread_queue<float, float>(b->dim, b->wide,
+              ? launch_spread_queue<float, float>(b->dim, b->group, b->tb,
                                                   (const BatchProb<float>*)b->probs.p, b->K,
                                                   b->item_start.as<int64_t>(),
                                                   b->counter.as<int>(), b->T, c, arena, b->smem, s)
-              : launch_spread_queue<float, double>(b->dim, b->wide,
+              : launch_spread_queue<float, double>(b->dim, b->group, b->tb,
                                                    (const BatchProb<float>*)b->probs.p, b->K,
                                                    b->item_start.as<int64_t>(),
                                                    b->counter.as<int>(), b->T, c, arena, b->smem,
                                                    s);
     else
-      e = launch_spread_queue<double, double>(b->dim, b->wide,
+      e = launch_spread_queue<double, double>(b->dim, b->group, b->tb,
                                               (const BatchProb<double>*)b->probs.p, b->K,
                                               b->item_start.as<int64_t>(), b->counter.as<int>(),
                                               b->T, c, arena, b->smem, s);

@@ -25,6 +25,7 @@
 //     not fit or when points are not sorted.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "gbn_common.cuh"
@@ -76,13 +77,17 @@ struct Acc<float> {
 __device__ __forceinline__ void acc_add(int* p, float v) { atomicAdd(p, __float2int_rn(v)); }
 __device__ __forceinline__ void acc_add(double* p, double v) { atomicAdd(p, v); }
 
-// One subproblem of one transform, executed by the whole block (shared by
-// the per-subproblem kernel and the work-queue kernel of batched plans).
-// tmap (or null): TMA map of the grids; t_map = this transform's index in it.
-template <typename TC, typename TD, int DIM, int G>
+// One subproblem of ntb <= TB transforms t, t+1, ..., executed by the whole
+// block (shared by the per-subproblem kernel and the work-queue kernel of
+// batched plans).  Each transform has its own tile; a point's record, kernel
+// values and shuffles are computed once and applied to every transform.
+// Shared memory: TB tiles of spread_tile_bytes, then (g.stash) TB x maxsub
+// strengths.  tmap (or null): TMA map of the grids; t_map = transform t's
+// index in it.
+template <typename TC, typename TD, int DIM, int G, int TB = 1>
 __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                                 const PtRec<TC, DIM>* __restrict__ recs,
-                                                const SubArgs& sa, int sub, int t,
+                                                const SubArgs& sa, int sub, int t, int ntb,
                                                 const cplx_t<TD>* __restrict__ c,
                                                 cplx_t<TC>* __restrict__ fine, int64_t nftot,
                                                 unsigned char* smem_raw,
@@ -93,52 +98,65 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
   constexpr int NCO = GroupCfg<G>::NCO;
   constexpr int PPW = 32 / G;
   constexpr int NWARP = kThreads / 32;
-  __shared__ TC s_red[NWARP];
+  __shared__ TC s_red[TB][NWARP];
   int start, cnt, bin;
   if (!sub_range(sa, g, M, sub, start, cnt, bin)) return;
   const int w = g.w;
   const Tile<DIM> tl(g, bin);
-  A* sacc = reinterpret_cast<A*>(smem_raw);  // cell i: [2i] real, [2i+1] imaginary
-  for (int i = threadIdx.x; i < 2 * tl.ncell; i += kThreads) sacc[i] = A(0);
+  const size_t tile_b = spread_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4);
+  const int tile_w = (int)(tile_b / sizeof(A));  // accumulator words per tile
+  A* sacc = reinterpret_cast<A*>(smem_raw);  // tile k at sacc + k*tile_w; cell i: [2i] re, [2i+1] im
+  for (int i = threadIdx.x; i < tile_w * ntb; i += kThreads) sacc[i] = A(0);
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
-  const cplx_t<TD>* ct = c + (int64_t)t * M;
 
   // one pass over the subproblem's strengths: stage them in shared memory
-  // (g.stash) and, in FP32, take the fixed-point scale from them
-  cplx_t<TC>* cst = reinterpret_cast<cplx_t<TC>*>(
-      smem_raw + spread_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4));
+  // (g.stash) and, in FP32, take each transform's fixed-point scale from them
+  cplx_t<TC>* cst = reinterpret_cast<cplx_t<TC>*>(smem_raw + TB * tile_b);
   const bool stash = g.stash != 0;
-  TC scale = TC(1), inv = TC(1);
-  TC part = TC(0);
-  if (kFixed || stash) {
-    for (int p = threadIdx.x; p < cnt; p += kThreads) {
-      const int js = start + p;
-      TC re, im;
-      load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), re, im);
-      if (stash) {
-        cplx_t<TC> v;
-        v.x = re;
-        v.y = im;
-        cst[p] = v;
+  TC scale[TB], inv[TB];
+#pragma unroll
+  for (int k = 0; k < TB; ++k) {
+    scale[k] = TC(1);
+    inv[k] = TC(1);
+    if (k >= ntb) continue;
+    const cplx_t<TD>* ct = c + (int64_t)(t + k) * M;
+    TC part = TC(0);
+    if (kFixed || stash) {
+      for (int p = threadIdx.x; p < cnt; p += kThreads) {
+        const int js = start + p;
+        TC re, im;
+        load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), re, im);
+        if (stash) {
+          cplx_t<TC> v;
+          v.x = re;
+          v.y = im;
+          cst[k * g.maxsub + p] = v;
+        }
+        part += fmax(fabs(re), fabs(im));
       }
-      part += fmax(fabs(re), fabs(im));
+    }
+    if (kFixed) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      if (lane == 0) s_red[k][warp] = part;
     }
   }
   if (kFixed) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if (lane == 0) s_red[warp] = part;
     __syncthreads();
-    TC B = TC(0);
 #pragma unroll
-    for (int i = 0; i < NWARP; ++i) B += s_red[i];
-    // B == 0 (or denormal): nothing to spread; the tile stays zero
-    scale = B > TC(1e-30) ? TC(1073741824.0) / B : TC(0);
-    inv = B > TC(1e-30) ? B / TC(1073741824.0) : TC(0);
+    for (int k = 0; k < TB; ++k) {
+      if (k >= ntb) continue;
+      TC B = TC(0);
+#pragma unroll
+      for (int i = 0; i < NWARP; ++i) B += s_red[k][i];
+      // B == 0 (or denormal): nothing to spread; the tile stays zero
+      scale[k] = B > TC(1e-30) ? TC(1073741824.0) / B : TC(0);
+      inv[k] = B > TC(1e-30) ? B / TC(1073741824.0) : TC(0);
+    }
   }
   TC co[NCO];
   load_coef<TC, NCO>(co, ks, gl, w);
-  __syncthreads();  // tile cleared, strengths staged
+  __syncthreads();  // tiles cleared, strengths staged
 
   const bool lane_on = gl < w;
   constexpr int kStep = NWARP * PPW;
@@ -157,60 +175,66 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
       const int pn = pb + kStep + grp;
       rn = recs[start + (pn < cnt ? pn : 0)];
     }
-    TC cr = TC(0), ci = TC(0);
-    if (valid) {
-      if (stash) {
-        const cplx_t<TC> v = cst[pi];
-        cr = v.x;
-        ci = v.y;
-      } else {
-        load_c<TD, TC>(ct + (sa.perm ? sa.perm[js] : js), cr, ci);
-      }
-    }
-    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w) * scale;
+    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
     const int l0 = r.i[0] - tl.org[0] + gl;
     const bool on = valid && lane_on;
-    const TC vr = cr * kx, vi = ci * kx;
-    if (DIM == 1) {
-      if (on) {
-        acc_add(&sacc[2 * l0], vr);
-        acc_add(&sacc[2 * l0 + 1], vi);
-      }
-    } else if (DIM == 2) {
-      // the group's y kernel values, fetched once per point
-      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      TC kyr[G];
+    // the group's y (and z) kernel values, fetched once per point
+    TC ky = TC(0), kz = TC(0);
+    TC kyr[G];
+    if (DIM > 1) {
+      ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
 #pragma unroll
       for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
-      A* col = sacc + 2 * ((r.i[1] - tl.org[1]) * tl.T[0] + l0);
-      const int pitch = 2 * tl.T[0];
+    }
+    if (DIM > 2) kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
+    const int pitch = 2 * tl.T[0];
+    const int plane = pitch * tl.T[1];
+    const int cell0 = DIM == 1 ? 2 * l0
+                      : DIM == 2
+                          ? pitch * (r.i[1] - tl.org[1]) + 2 * l0
+                          : plane * (r.i[2] - tl.org[2]) + pitch * (r.i[1] - tl.org[1]) + 2 * l0;
 #pragma unroll
-      for (int iy = 0; iy < G; ++iy) {
-        if (iy < w && on) {
-          acc_add(&col[iy * pitch], vr * kyr[iy]);
-          acc_add(&col[iy * pitch + 1], vi * kyr[iy]);
+    for (int k = 0; k < TB; ++k) {
+      if (k >= ntb) break;
+      TC cr = TC(0), ci = TC(0);
+      if (valid) {
+        if (stash) {
+          const cplx_t<TC> v = cst[k * g.maxsub + pi];
+          cr = v.x;
+          ci = v.y;
+        } else {
+          load_c<TD, TC>(c + (int64_t)(t + k) * M + (sa.perm ? sa.perm[js] : js), cr, ci);
         }
       }
-    } else {
-      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
-      TC kyr[G];
-#pragma unroll
-      for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
-      const int plane = 2 * tl.T[0] * tl.T[1];
-      const int pitch = 2 * tl.T[0];
-      A* zrow = sacc + 2 * (((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0);
-      for (int iz = 0; iz < w; ++iz) {
-        const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
-        const TC zr = vr * kzv, zi = vi * kzv;
+      const TC kxs = kx * scale[k];
+      const TC vr = cr * kxs, vi = ci * kxs;
+      A* acc = sacc + k * tile_w + cell0;
+      if (DIM == 1) {
+        if (on) {
+          acc_add(&acc[0], vr);
+          acc_add(&acc[1], vi);
+        }
+      } else if (DIM == 2) {
 #pragma unroll
         for (int iy = 0; iy < G; ++iy) {
           if (iy < w && on) {
-            acc_add(&zrow[iy * pitch], zr * kyr[iy]);
-            acc_add(&zrow[iy * pitch + 1], zi * kyr[iy]);
+            acc_add(&acc[iy * pitch], vr * kyr[iy]);
+            acc_add(&acc[iy * pitch + 1], vi * kyr[iy]);
           }
         }
-        zrow += plane;
+      } else {
+        for (int iz = 0; iz < w; ++iz) {
+          const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
+          const TC zr = vr * kzv, zi = vi * kzv;
+#pragma unroll
+          for (int iy = 0; iy < G; ++iy) {
+            if (iy < w && on) {
+              acc_add(&acc[iy * pitch], zr * kyr[iy]);
+              acc_add(&acc[iy * pitch + 1], zi * kyr[iy]);
+            }
+          }
+          acc += plane;
+        }
       }
     }
   }
@@ -218,45 +242,58 @@ __device__ __forceinline__ void spread_sm_block(const Geom& g, const KerSpec<TC>
 
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
   if constexpr (kFixed && DIM > 1) {
-    if (tmap != nullptr && tl.interior(g)) {
-      // fixed point -> float in place, then one bulk reduce-add of the box
-      for (int i = threadIdx.x; i < 2 * tl.ncell; i += kThreads)
-        sacc[i] = __float_as_int((TC)sacc[i] * inv);
+    // every tile must start on a 128-byte boundary of shared memory
+    if (tmap != nullptr && tl.interior(g) && (smem_addr(sacc) & 127u) == 0 &&
+        (tile_b & 127u) == 0) {
+      // fixed point -> float in place, then one bulk reduce-add per tile
+      for (int k = 0; k < ntb; ++k) {
+        A* tk = sacc + k * tile_w;
+        for (int i = threadIdx.x; i < 2 * tl.ncell; i += kThreads)
+          tk[i] = __float_as_int((TC)tk[i] * inv[k]);
+      }
       fence_async_smem();
       __syncthreads();
       if (threadIdx.x == 0) {
-        if (DIM == 2)
-          tma_reduce_add_2d(tmap, sacc, 2 * tl.org[0], tl.org[1] + t_map * nf1);
-        else
-          tma_reduce_add_3d(tmap, sacc, 2 * tl.org[0], tl.org[1], tl.org[2] + t_map * nf2);
+        for (int k = 0; k < ntb; ++k) {
+          const A* tk = sacc + k * tile_w;
+          if (DIM == 2)
+            tma_reduce_add_2d(tmap, tk, 2 * tl.org[0], tl.org[1] + (t_map + k) * nf1);
+          else
+            tma_reduce_add_3d(tmap, tk, 2 * tl.org[0], tl.org[1], tl.org[2] + (t_map + k) * nf2);
+        }
         bulk_commit();
-        bulk_wait_read();  // the tile stays allocated until the copy has read it
+        bulk_wait_read();  // the tiles stay allocated until the copies have read them
       }
       return;
     }
   }
-  cplx_t<TC>* ft = fine + (int64_t)t * nftot;
-  CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
-  for (int i = threadIdx.x; i < tl.ncell; i += kThreads, cw.next()) {
-    const A ar = sacc[2 * i], ai = sacc[2 * i + 1];
-    if (ar == A(0) && ai == A(0)) continue;
-    const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
-    const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
-    const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
-    atomic_add_c(&ft[(g2 * nf1 + g1) * nf0 + g0], (TC)ar * inv, (TC)ai * inv);
+  for (int k = 0; k < ntb; ++k) {
+    const A* tk = sacc + k * tile_w;
+    cplx_t<TC>* ft = fine + (int64_t)(t + k) * nftot;
+    CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
+    for (int i = threadIdx.x; i < tl.ncell; i += kThreads, cw.next()) {
+      const A ar = tk[2 * i], ai = tk[2 * i + 1];
+      if (ar == A(0) && ai == A(0)) continue;
+      const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
+      const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
+      const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
+      atomic_add_c(&ft[(g2 * nf1 + g1) * nf0 + g0], (TC)ar * inv[k], (TC)ai * inv[k]);
+    }
   }
 }
 
-template <typename TC, typename TD, int DIM, int G>
+// grid (subproblems, ceil(ntr / TB)); block y handles transforms TB*y ...
+template <typename TC, typename TD, int DIM, int G, int TB>
 __global__ void __launch_bounds__(kThreads)
     spread_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
                      SubArgs sa, const cplx_t<TD>* __restrict__ c, cplx_t<TC>* __restrict__ fine,
-                     int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
-                     int t_base) {
+                     int64_t nftot, int ntr, const __grid_constant__ CUtensorMap tmap,
+                     int use_tma, int t_base) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  spread_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, c, fine, nftot,
-                                  smem_raw, use_tma ? &tmap : nullptr,
-                                  t_base + (int)blockIdx.y);
+  const int t = TB * (int)blockIdx.y;
+  const int ntb = min(TB, ntr - t);
+  spread_sm_block<TC, TD, DIM, G, TB>(g, ks, M, recs, sa, blockIdx.x, t, ntb, c, fine, nftot,
+                                      smem_raw, use_tma ? &tmap : nullptr, t_base + t);
 }
 
 template <typename TC, typename TD, int DIM, int G>
@@ -316,7 +353,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 
-template <typename TC, typename TD, int DIM, int G>
+template <typename TC, typename TD, int DIM, int G, int TB>
 __global__ void __launch_bounds__(kThreads)
     spread_queue_kernel(const BatchProb<TC>* __restrict__ probs, int K,
                         const int64_t* __restrict__ item_start, int* counter, int T,
@@ -340,18 +377,21 @@ __global__ void __launch_bounds__(kThreads)
     }
     const BatchProb<TC> P = probs[lo];
     const int64_t local = item - item_start[lo];
-    const int sub = (int)(local / T), t = (int)(local - (int64_t)sub * T);
+    const int Tg = (T + TB - 1) / TB;  // items per subproblem
+    const int sub = (int)(local / Tg), tg = (int)(local - (int64_t)sub * Tg);
+    const int t = tg * TB;
     SubArgs sa{P.sub_bin, P.sub_off, P.n_sub, P.bin_start, P.bin_count, P.perm, 1};
-    spread_sm_block<TC, TD, DIM, G>(P.g, P.ks, P.M, (const PtRec<TC, DIM>*)P.recs, sa, sub, t,
-                                    c + P.c_off, arena + P.grid_off, P.nftot, smem_raw);
+    spread_sm_block<TC, TD, DIM, G, TB>(P.g, P.ks, P.M, (const PtRec<TC, DIM>*)P.recs, sa, sub,
+                                        t, min(TB, T - t), c + P.c_off, arena + P.grid_off,
+                                        P.nftot, smem_raw);
   }
 }
 
-template <typename TC, typename TD, int DIM, int G>
+template <typename TC, typename TD, int DIM, int G, int TB>
 cudaError_t run_spread_queue(const BatchProb<TC>* probs, int K, const int64_t* item_start,
                              int* counter, int T, const void* c, void* arena, size_t smem,
                              cudaStream_t s) {
-  auto kern = spread_queue_kernel<TC, TD, DIM, G>;
+  auto kern = spread_queue_kernel<TC, TD, DIM, G, TB>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
@@ -383,24 +423,46 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
   int64_t nftot = 1;
   for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
   const PtRec<TC, DIM>* recs = (const PtRec<TC, DIM>*)(sa.sorted ? st.recs : st.recs_in);
-  for (int t0 = 0; t0 < ntr; t0 += 65535) {
-    const int nt = ntr - t0 < 65535 ? ntr - t0 : 65535;
-    dim3 grid((unsigned)nblk, (unsigned)nt);
+  // transforms per block: several stacked transforms share each point's
+  // record, kernel values and shuffles (FP32 with staged strengths, while
+  // the block's shared memory stays within 100 KB)
+  const bool sm = method == 2 && sa.sorted;
+  const size_t smem1 = spread_smem_bytes(DIM, g.bs, g.w, sizeof(TC) == 4, g.maxsub, g.stash != 0);
+  int TB = 1;
+  if (sm && sizeof(TC) == 4 && G <= 8 && g.stash) {
+    if (ntr >= 4 && 4 * smem1 <= 100 * 1024)
+      TB = 4;
+    else if (ntr >= 2 && 2 * smem1 <= 100 * 1024)
+      TB = 2;
+  }
+  for (int t0 = 0; t0 < ntr; t0 += 65535 * TB) {
+    const int nt = std::min(ntr - t0, 65535 * TB);
+    dim3 grid((unsigned)nblk, (unsigned)((nt + TB - 1) / TB));
     const cplx_t<TD>* ct = (const cplx_t<TD>*)c + (int64_t)t0 * M;
     cplx_t<TC>* ft = (cplx_t<TC>*)fine + (int64_t)t0 * nftot;
-    if (method == 2 && sa.sorted) {
-      const size_t smem =
-          spread_smem_bytes(DIM, g.bs, g.w, sizeof(TC) == 4, g.maxsub, g.stash != 0);
-      auto kern = spread_sm_kernel<TC, TD, DIM, G>;
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
-      if (e != cudaSuccess) return e;
+    if (sm) {
       CUtensorMap m;
       memset(&m, 0, sizeof(m));
       const int use = tmap != nullptr && sizeof(TC) == 4;
       if (use) m = *tmap;
-      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ct, ft, nftot, m, use, t0);
-      note_launch();
+      auto go = [&](auto kern, int tb) -> cudaError_t {
+        const size_t smem = smem1 * tb;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ct, ft, nftot, nt, m, use, t0);
+        note_launch();
+        return cudaSuccess;
+      };
+      cudaError_t e;
+      if constexpr (sizeof(TC) == 4 && G <= 8) {
+        e = TB == 4   ? go(spread_sm_kernel<TC, TD, DIM, G, 4>, 4)
+            : TB == 2 ? go(spread_sm_kernel<TC, TD, DIM, G, 2>, 2)
+                      : go(spread_sm_kernel<TC, TD, DIM, G, 1>, 1);
+      } else {
+        e = go(spread_sm_kernel<TC, TD, DIM, G, 1>, 1);
+      }
+      if (e != cudaSuccess) return e;
     } else {
       spread_gm_kernel<TC, TD, DIM, G><<<grid, kThreads, 0, s>>>(g, ks, M, recs, sa, ct, ft,
                                                                   nftot);
@@ -447,27 +509,52 @@ template cudaError_t launch_spread<double, double>(const Geom&, const KerSpec<do
                                                    void*, int, cudaStream_t, const CUtensorMap*);
 
 
+template <typename TC, typename TD, int DIM>
+cudaError_t spread_queue_dim(int group, int tb, const BatchProb<TC>* probs, int K,
+                             const int64_t* item_start, int* counter, int T, const void* c,
+                             void* arena, size_t smem1, cudaStream_t s) {
+  if (group == 16)
+    return run_spread_queue<TC, TD, DIM, 16, 1>(probs, K, item_start, counter, T, c, arena,
+                                                smem1, s);
+  if constexpr (sizeof(TC) == 4) {
+    if (tb == 4)
+      return group == 8 ? run_spread_queue<TC, TD, DIM, 8, 4>(probs, K, item_start, counter, T,
+                                                              c, arena, 4 * smem1, s)
+                        : run_spread_queue<TC, TD, DIM, 6, 4>(probs, K, item_start, counter, T,
+                                                              c, arena, 4 * smem1, s);
+    if (tb == 2)
+      return group == 8 ? run_spread_queue<TC, TD, DIM, 8, 2>(probs, K, item_start, counter, T,
+                                                              c, arena, 2 * smem1, s)
+                        : run_spread_queue<TC, TD, DIM, 6, 2>(probs, K, item_start, counter, T,
+                                                              c, arena, 2 * smem1, s);
+  }
+  return group == 8 ? run_spread_queue<TC, TD, DIM, 8, 1>(probs, K, item_start, counter, T, c,
+                                                          arena, smem1, s)
+                    : run_spread_queue<TC, TD, DIM, 6, 1>(probs, K, item_start, counter, T, c,
+                                                          arena, smem1, s);
+}
+
 template <typename TC, typename TD>
-cudaError_t launch_spread_queue(int dim, bool wide, const BatchProb<TC>* probs, int K,
+cudaError_t launch_spread_queue(int dim, int group, int tb, const BatchProb<TC>* probs, int K,
                                 const int64_t* item_start, int* counter, int T, const void* c,
-                                void* arena, size_t smem, cudaStream_t s) {
+                                void* arena, size_t smem1, cudaStream_t s) {
   if (K == 0) return cudaSuccess;
   switch (dim) {
     case 1:
-      return wide ? run_spread_queue<TC, TD, 1, 16>(probs, K, item_start, counter, T, c, arena, smem, s)
-                  : run_spread_queue<TC, TD, 1, 8>(probs, K, item_start, counter, T, c, arena, smem, s);
+      return spread_queue_dim<TC, TD, 1>(group, tb, probs, K, item_start, counter, T, c, arena,
+                                         smem1, s);
     case 2:
-      return wide ? run_spread_queue<TC, TD, 2, 16>(probs, K, item_start, counter, T, c, arena, smem, s)
-                  : run_spread_queue<TC, TD, 2, 8>(probs, K, item_start, counter, T, c, arena, smem, s);
+      return spread_queue_dim<TC, TD, 2>(group, tb, probs, K, item_start, counter, T, c, arena,
+                                         smem1, s);
     default:
-      return wide ? run_spread_queue<TC, TD, 3, 16>(probs, K, item_start, counter, T, c, arena, smem, s)
-                  : run_spread_queue<TC, TD, 3, 8>(probs, K, item_start, counter, T, c, arena, smem, s);
+      return spread_queue_dim<TC, TD, 3>(group, tb, probs, K, item_start, counter, T, c, arena,
+                                         smem1, s);
   }
 }
 
-#define GBN_INST_SQ(TC, TD)                                                                  \
-  template cudaError_t launch_spread_queue<TC, TD>(int, bool, const BatchProb<TC>*, int,     \
-                                                   const int64_t*, int*, int, const void*,   \
+#define GBN_INST_SQ(TC, TD)                                                                   \
+  template cudaError_t launch_spread_queue<TC, TD>(int, int, int, const BatchProb<TC>*, int,  \
+                                                   const int64_t*, int*, int, const void*,    \
                                                    void*, size_t, cudaStream_t);
 GBN_INST_SQ(float, float)
 GBN_INST_SQ(float, double)
