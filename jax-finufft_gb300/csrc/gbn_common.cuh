@@ -159,6 +159,23 @@ cudaError_t launch_spread(const Geom& g, const KerSpec<TC>& ks, int method, int6
                           const SortState& st, const void* c, void* fine, int ntr,
                           cudaStream_t s, const CUtensorMap* tmap = nullptr);
 
+// Outputs of the fused gradient gather.
+template <typename TD>
+struct GradOut {
+  const cplx_t<TD>* w;  // mode 0: strengths c (ntr, M); mode 1: cotangent g (ntr, M)
+  cplx_t<TD>* out_c;    // mode 0 with base: gathered grid 0 (ntr, M), or null
+  TD* gx[3];            // coordinate gradients per axis (M), or null
+};
+
+// Shared-memory fused gradient gather over ntr*E grids (the interp kernel's
+// block with a gradient epilogue); tmap as for launch_interp over the grids.
+template <typename TC, typename TD>
+cudaError_t launch_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                                  const SortState& st, const void* grids, int ntr, int E,
+                                  int mode, int iflag, int base, const int* dims,
+                                  const GradOut<TD>& go, const CUtensorMap* tmap,
+                                  cudaStream_t s);
+
 // Encode a TMA map over nb float2 fine grids of geometry g (rank = dim:
 // x as 2*nf0 floats, the last axis stacked over the nb grids) whose box is
 // one bin tile.  False (and no map) when TMA does not apply: 1D, a box
@@ -223,12 +240,14 @@ cudaError_t launch_deconv2w(int dim, const int64_t* N, const int64_t* nf, int mo
 // weights and combine them into gradients (see gbn_grad.cu): mode 0 = the
 // type-1 gradient (w = strengths; grid 0 -> out_c when base = 1), mode 1 =
 // the type-2 coordinate gradient (w = output cotangent).  gx[d] (M reals,
-// may be null) is accumulated.
+// may be null, zeroed by the caller) receives the gradient.  tmap: a TMA map
+// of the ntr*E grids for the shared-memory gather (or null).
 template <typename TC, typename TD>
 cudaError_t launch_interp_grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                const SortState& st, const void* grids, int ntr, int E, int mode,
                                int iflag, int base, const int* dims, const void* w, void* out_c,
-                               void* const* gx, bool shared, cudaStream_t s);
+                               void* const* gx, bool shared, cudaStream_t s,
+                               const CUtensorMap* tmap = nullptr);
 
 // One problem of a batched plan, as the work-queue kernels see it: its
 // geometry, kernel, sorted points, and where its strengths/values (T, M)

@@ -40,55 +40,86 @@ __device__ __forceinline__ int64_t fine_to_mode_d(int64_t g, int64_t N, int64_t 
 // For every fine cell: the mode it holds (or zero padding), divided by the
 // kernel's Fourier transform, times E weights: grid e gets factor 1 when
 // e < base, else a * k_{dims[e]} (k the integer frequency along that axis,
-// a = 1 or i*iflag).  Output grids are (t*E + e)*nftot + cell.
+// a = 1 or i*iflag).  Output grids are (t*E + e)*nftot + cell.  One block
+// per item = up to 512 cells of one fine-grid row; each thread writes two
+// neighbouring cells of every grid (16-byte stores in FP32).
 template <typename TC, typename TD, int DIM, int E>
-__global__ void deconv2w_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
-                                const TC* __restrict__ p0, const TC* __restrict__ p1,
-                                const TC* __restrict__ p2, const cplx_t<TD>* __restrict__ in,
-                                cplx_t<TC>* __restrict__ grids, int ntr, int64_t nftot,
-                                int64_t Ntot, int base, int4 dims, TC a_re, TC a_im) {
-  const int g0 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g0 >= nf0) return;
-  const int i0 = (int)fine_to_mode_d(g0, N0, nf0, modeord);
+__global__ void __launch_bounds__(256)
+    deconv2w_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
+                    const TC* __restrict__ p0, const TC* __restrict__ p1,
+                    const TC* __restrict__ p2, const cplx_t<TD>* __restrict__ in,
+                    cplx_t<TC>* __restrict__ grids, int ntr, int64_t nftot, int64_t Ntot,
+                    int base, int4 dims, TC a_re, TC a_im) {
   const int dd[4] = {dims.x, dims.y, dims.z, dims.w};
-  for (int g2 = blockIdx.z; g2 < nf2; g2 += gridDim.z) {
+  const int nrows = nf1 * nf2;
+  const int npair = nf0 >> 1;  // nf0 is even
+  const int nchunk = (npair + blockDim.x - 1) / blockDim.x;
+  for (int item = blockIdx.x; item < nrows * nchunk; item += gridDim.x) {
+    const int row = item / nchunk, chunk = item - row * nchunk;
+    const int g1 = DIM > 1 ? row % nf1 : 0;
+    const int g2 = DIM > 2 ? row / nf1 : 0;
+    const int i1 = DIM > 1 ? (int)fine_to_mode_d(g1, N1, nf1, modeord) : 0;
     const int i2 = DIM > 2 ? (int)fine_to_mode_d(g2, N2, nf2, modeord) : 0;
-    for (int g1 = blockIdx.y; g1 < nf1; g1 += gridDim.y) {
-      const int i1 = DIM > 1 ? (int)fine_to_mode_d(g1, N1, nf1, modeord) : 0;
-      const int cell = (g2 * nf1 + g1) * nf0 + g0;
-      const bool mode = i0 >= 0 && i1 >= 0 && i2 >= 0;
-      TC f = TC(0);
-      TC k[3] = {TC(0), TC(0), TC(0)};
-      int src = 0;
-      if (mode) {
-        f = p0[i0];
-        if (DIM > 1) f *= p1[i1];
-        if (DIM > 2) f *= p2[i2];
-        k[0] = (TC)mode_freq_d(i0, N0, modeord);
-        if (DIM > 1) k[1] = (TC)mode_freq_d(i1, N1, modeord);
-        if (DIM > 2) k[2] = (TC)mode_freq_d(i2, N2, modeord);
-        src = (i2 * N1 + i1) * N0 + i0;
+    const bool live = i1 >= 0 && i2 >= 0;
+    TC f12 = TC(1), k1 = TC(0), k2 = TC(0);
+    if (live) {
+      if (DIM > 1) {
+        f12 *= p1[i1];
+        k1 = (TC)mode_freq_d(i1, N1, modeord);
       }
-      for (int t = 0; t < ntr; ++t) {
-        TC vr = TC(0), vi = TC(0);
-        if (mode) {
-          const cplx_t<TD> v = in[t * Ntot + src];
-          vr = (TC)v.x * f;
-          vi = (TC)v.y * f;
-        }
+      if (DIM > 2) {
+        f12 *= p2[i2];
+        k2 = (TC)mode_freq_d(i2, N2, modeord);
+      }
+    }
+    const int q = chunk * blockDim.x + threadIdx.x;
+    if (q >= npair) continue;
+    const int g0 = 2 * q;
+    int ia[2] = {-1, -1};
+    TC fa[2] = {TC(0), TC(0)}, k0[2] = {TC(0), TC(0)};
+    if (live) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-          cplx_t<TC> o;
+      for (int h = 0; h < 2; ++h) {
+        ia[h] = (int)fine_to_mode_d(g0 + h, N0, nf0, modeord);
+        if (ia[h] >= 0) {
+          fa[h] = p0[ia[h]] * f12;
+          k0[h] = (TC)mode_freq_d(ia[h], N0, modeord);
+        }
+      }
+    }
+    const int64_t src_row = live ? ((int64_t)i2 * N1 + i1) * N0 : 0;
+    const int64_t dst = (int64_t)row * nf0 + g0;
+    for (int t = 0; t < ntr; ++t) {
+      TC vr[2] = {TC(0), TC(0)}, vi[2] = {TC(0), TC(0)};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (ia[h] >= 0) {
+          const cplx_t<TD> v = in[t * Ntot + src_row + ia[h]];
+          vr[h] = (TC)v.x * fa[h];
+          vi[h] = (TC)v.y * fa[h];
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        cplx_t<TC> o[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
           if (e < base) {
-            o.x = vr;
-            o.y = vi;
+            o[h].x = vr[h];
+            o[h].y = vi[h];
           } else {
-            const TC kk = k[dd[e]];
+            const TC kk = dd[e] == 0 ? k0[h] : dd[e] == 1 ? k1 : k2;
             const TC wr = a_re * kk, wi = a_im * kk;
-            o.x = vr * wr - vi * wi;
-            o.y = vr * wi + vi * wr;
+            o[h].x = vr[h] * wr - vi[h] * wi;
+            o[h].y = vr[h] * wi + vi[h] * wr;
           }
-          grids[(int64_t)(t * E + e) * nftot + cell] = o;
+        }
+        cplx_t<TC>* d = grids + (int64_t)(t * E + e) * nftot + dst;
+        if constexpr (sizeof(TC) == 4) {
+          *reinterpret_cast<float4*>(d) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+        } else {
+          d[0] = o[0];
+          d[1] = o[1];
         }
       }
     }
@@ -122,12 +153,6 @@ __device__ __forceinline__ bool sub_range(const SubArgs& sa, const Geom& g, int6
   return cnt > 0;
 }
 
-template <typename TD>
-struct GradOut {
-  const cplx_t<TD>* w;  // mode 0: strengths c (ntr, M); mode 1: cotangent g (ntr, M)
-  cplx_t<TD>* out_c;    // mode 0 with base: gathered grid 0 (ntr, M), or null
-  TD* gx[3];            // coordinate gradients per axis (M), or null
-};
 
 // One pass over the points gathering E grids per transform with shared
 // kernel weights.  mode 0 (type-1 gradient): grid 0 (when base) is the
@@ -228,161 +253,6 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Shared-memory variant: one launch over (subproblem, transform x grid).
-// Each block stages its bin's tile of one grid (t, e), gathers it at the
-// bin's points with the lane-per-x-offset groups of the interp kernel and
-// adds each point's term to the gradients (out_c written, gx accumulated
-// with one atomic per point and grid).  Kernel weights are recomputed per
-// block from the sorted records.
-__device__ __forceinline__ void atomic_add_r(float* p, float v) { atomicAdd(p, v); }
-__device__ __forceinline__ void atomic_add_r(double* p, double v) { atomicAdd(p, v); }
-
-template <typename TC, typename TD, int DIM, int G>
-__global__ void __launch_bounds__(kThreads)
-    interp_grad_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M,
-                          const PtRec<TC, DIM>* __restrict__ recs, SubArgs sa,
-                          const cplx_t<TC>* __restrict__ grids, int E, int64_t nftot, int mode,
-                          int iflag, int base, int4 dims, GradOut<TD> go) {
-  constexpr int NCO = GroupCfg<G>::NCO;
-  constexpr int PPW = 32 / G;
-  constexpr int NWARP = kThreads / 32;
-  int start, cnt;
-  if (!sub_range(sa, g, M, blockIdx.x, start, cnt)) return;
-  const int bin = sa.sub_bin[blockIdx.x];
-  const int te = blockIdx.y;
-  const int t = te / E, e = te - t * E;
-  const int w = g.w;
-  const Tile<DIM> tl(g, bin);
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
-  const cplx_t<TC>* ft = grids + (int64_t)te * nftot;
-  {
-    const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
-    CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
-    for (int i = threadIdx.x; i < tl.ncell; i += kThreads, cw.next()) {
-      const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
-      const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
-      const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
-      tile[i] = ft[(g2 * nf1 + g1) * nf0 + g0];
-    }
-  }
-  const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
-  TC co[NCO];
-  load_coef<TC, NCO>(co, ks, gl, w);
-  __syncthreads();
-  const bool lane_on = gl < w;
-  const int dd[4] = {dims.x, dims.y, dims.z, dims.w};
-  TD* gxe = e >= base ? go.gx[dd[e]] : nullptr;
-  for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
-    const int pi = pb + grp;
-    const bool valid = pi < cnt && grp < PPW;
-    const int js = start + (valid ? pi : 0);
-    const PtRec<TC, DIM> r = recs[js];
-    const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
-    const int l0 = r.i[0] - tl.org[0] + gl;
-    TC ar = TC(0), ai = TC(0);
-    if (DIM == 1) {
-      if (lane_on) {
-        const cplx_t<TC> v = tile[l0];
-        ar = v.x;
-        ai = v.y;
-      }
-    } else if (DIM == 2) {
-      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      int idx = (r.i[1] - tl.org[1]) * tl.T[0] + l0;
-      for (int iy = 0; iy < w; ++iy) {
-        const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-        if (lane_on) {
-          const cplx_t<TC> v = tile[idx];
-          ar = fma(v.x, kyv, ar);
-          ai = fma(v.y, kyv, ai);
-        }
-        idx += tl.T[0];
-      }
-    } else {
-      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
-      const int plane = tl.T[0] * tl.T[1];
-      int zbase = ((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * tl.T[0] + l0;
-      for (int iz = 0; iz < w; ++iz) {
-        const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
-        TC yr = TC(0), yi = TC(0);
-        int idx = zbase;
-        for (int iy = 0; iy < w; ++iy) {
-          const TC kyv = __shfl_sync(0xffffffffu, ky, grp * G + iy);
-          if (lane_on) {
-            const cplx_t<TC> v = tile[idx];
-            yr = fma(v.x, kyv, yr);
-            yi = fma(v.y, kyv, yi);
-          }
-          idx += tl.T[0];
-        }
-        ar = fma(yr, kzv, ar);
-        ai = fma(yi, kzv, ai);
-        zbase += plane;
-      }
-    }
-    ar *= kx;
-    ai *= kx;
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-      ar += __shfl_xor_sync(0xffffffffu, ar, o);
-      ai += __shfl_xor_sync(0xffffffffu, ai, o);
-    }
-    if (valid && gl == 0) {
-      const int pidx = sa.perm[js];
-      if (e < base) {
-        if (go.out_c) {
-          cplx_t<TD> o;
-          o.x = (TD)ar;
-          o.y = (TD)ai;
-          go.out_c[(int64_t)t * M + pidx] = o;
-        }
-      } else if (gxe) {
-        const cplx_t<TD> wv = go.w[(int64_t)t * M + pidx];
-        const TC wr = (TC)wv.x, wi = (TC)wv.y;
-        const TC v = mode == 0 ? (TC)iflag * (wr * ai - wi * ar) : wr * ar + wi * ai;
-        atomic_add_r(&gxe[pidx], (TD)v);
-      }
-    }
-  }
-}
-
-inline unsigned grid1(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
-
-template <typename TC, typename TD, int DIM, int G>
-cudaError_t run_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t M,
-                               const SortState& st, const void* grids, int ntr, int E, int mode,
-                               int iflag, int base, const int* dims, const void* w, void* out_c,
-                               void* const* gx, cudaStream_t s) {
-  SubArgs sa;
-  sa.sub_bin = st.sub_bin;
-  sa.sub_off = st.sub_off;
-  sa.n_sub = st.n_sub;
-  sa.bin_start = st.bin_start;
-  sa.bin_count = st.bin_count;
-  sa.perm = st.perm;
-  sa.sorted = 1;
-  if (st.max_sub == 0) return cudaSuccess;
-  int64_t nftot = 1;
-  for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
-  const int64_t ncell = tile_cells(DIM, g.bs, g.w);
-  GradOut<TD> go;
-  go.w = (const cplx_t<TD>*)w;
-  go.out_c = (cplx_t<TD>*)out_c;
-  for (int d = 0; d < 3; ++d) go.gx[d] = gx ? (TD*)gx[d] : nullptr;
-  const size_t smem = (size_t)ncell * sizeof(cplx_t<TC>);
-  auto kern = interp_grad_sm_kernel<TC, TD, DIM, G>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  const int nte = ntr * E;
-  kern<<<dim3((unsigned)st.max_sub, (unsigned)nte), kThreads, smem, s>>>(
-      g, ks, M, (const PtRec<TC, DIM>*)st.recs, sa, (const cplx_t<TC>*)grids, E, nftot, mode,
-      iflag, base, make_int4(dims[0], dims[1], dims[2], dims[3]), go);
-  return cudaGetLastError();
-}
-
 template <typename TC, typename TD, int DIM, int G, int E>
 cudaError_t run_interp_grad_s(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                               const SortState& st, const void* grids, int ntr, int mode,
@@ -419,13 +289,16 @@ cudaError_t launch_deconv2w(int dim, const int64_t* N, const int64_t* nf, int mo
                             int base, const int* dims, double a_re, double a_im,
                             cudaStream_t s) {
   const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
-  dim3 grid(grid1(nf[0], 128), (unsigned)(nf[1] < 65535 ? nf[1] : 65535),
-            (unsigned)(nf[2] < 65535 ? nf[2] : 65535));
+  const int64_t items = nf[1] * nf[2] * ((nf[0] / 2 + 255) / 256);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)(items < (int64_t)nsm * 16 ? items : (int64_t)nsm * 16);
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
   const int4 dv = make_int4(dims[0], dims[1], dims[2], dims[3]);
   auto go = [&](auto kern) {
-    kern<<<grid, 128, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
+    kern<<<grid, 256, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
                               (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TD>*)in,
                               (cplx_t<TC>*)grids, ntr, nftot, Ntot, base, dv, (TC)a_re, (TC)a_im);
   };
@@ -456,27 +329,18 @@ template <typename TC, typename TD>
 cudaError_t launch_interp_grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                const SortState& st, const void* grids, int ntr, int E, int mode,
                                int iflag, int base, const int* dims, const void* w, void* out_c,
-                               void* const* gx, bool shared, cudaStream_t s) {
+                               void* const* gx, bool shared, cudaStream_t s,
+                               const CUtensorMap* tmap) {
   if (M == 0) return cudaSuccess;
   const bool wide = g.w > 8;
   cudaError_t e = cudaSuccess;
   if (shared && st.perm != nullptr && (int64_t)ntr * E <= 65535) {
-    switch (g.dim) {
-      case 1:
-        e = wide ? run_interp_grad_sm<TC, TD, 1, 16>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims, w, out_c, gx, s)
-                 : run_interp_grad_sm<TC, TD, 1, 8>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims, w, out_c, gx, s);
-        break;
-      case 2:
-        e = wide ? run_interp_grad_sm<TC, TD, 2, 16>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims, w, out_c, gx, s)
-                 : run_interp_grad_sm<TC, TD, 2, 8>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims, w, out_c, gx, s);
-        break;
-      default:
-        e = wide ? run_interp_grad_sm<TC, TD, 3, 16>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims, w, out_c, gx, s)
-                 : run_interp_grad_sm<TC, TD, 3, 8>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims, w, out_c, gx, s);
-        break;
-    }
-    note_launch();
-    return e;
+    GradOut<TD> go;
+    go.w = (const cplx_t<TD>*)w;
+    go.out_c = (cplx_t<TD>*)out_c;
+    for (int d = 0; d < 3; ++d) go.gx[d] = gx ? (TD*)gx[d] : nullptr;
+    return launch_interp_grad_sm<TC, TD>(g, ks, M, st, grids, ntr, E, mode, iflag, base, dims,
+                                         go, tmap, s);
   }
 #define GBN_IG(D, GG)                                                                          \
   switch (E) {                                                                                 \
@@ -508,7 +372,8 @@ cudaError_t launch_interp_grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
   template cudaError_t launch_interp_grad<TC, TD>(const Geom&, const KerSpec<TC>&, int64_t,    \
                                                   const SortState&, const void*, int, int, int, \
                                                   int, int, const int*, const void*, void*,     \
-                                                  void* const*, bool, cudaStream_t);
+                                                  void* const*, bool, cudaStream_t,             \
+                                                  const CUtensorMap*);
 GBN_INST_GRAD(float, float)
 GBN_INST_GRAD(float, double)
 GBN_INST_GRAD(double, double)

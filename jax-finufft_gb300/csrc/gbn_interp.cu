@@ -79,15 +79,63 @@ __device__ __forceinline__ void group_reduce(TC& a, TC& b) {
   }
 }
 
-// One subproblem of one transform, executed by the whole block (shared by
-// the per-subproblem kernel and the work-queue kernel of batched plans).
-// tmap (or null): TMA map of the grids; t_map = this transform's index in it.
-template <typename TC, typename TD, int DIM, int G>
+// Epilogue of the gather: the interpolated value of a point (input index
+// idx) goes to the output array.
+template <typename TC, typename TD>
+struct StoreOut {
+  cplx_t<TD>* ct;
+  __device__ __forceinline__ void operator()(int idx, TC ar, TC ai) const {
+    cplx_t<TD> o;
+    o.x = (TD)ar;
+    o.y = (TD)ai;
+    ct[idx] = o;
+  }
+};
+
+// Epilogue of the fused gradient gather for grid e of transform t: e < base
+// stores the value as the strength gradient; otherwise the coordinate
+// gradient of axis dims[e] gets Re(conj-weighted) terms against the weights
+// w (mode 0, type-1 plan: iflag * (w_re*v_im - w_im*v_re); mode 1, type-2
+// plan: w_re*v_re + w_im*v_im), added atomically when several transforms
+// share the gradient, else stored.
+template <typename TC, typename TD>
+struct GradEpi {
+  cplx_t<TD>* out_c;
+  TD* gx;
+  const cplx_t<TD>* w;
+  int strength, mode, iflag, atomic;
+  __device__ __forceinline__ void operator()(int idx, TC ar, TC ai) const {
+    if (strength) {
+      if (out_c) {
+        cplx_t<TD> o;
+        o.x = (TD)ar;
+        o.y = (TD)ai;
+        out_c[idx] = o;
+      }
+      return;
+    }
+    if (!gx) return;
+    const cplx_t<TD> wv = w[idx];
+    const TC wr = (TC)wv.x, wi = (TC)wv.y;
+    const TC v = mode == 0 ? (TC)iflag * (wr * ai - wi * ar) : wr * ar + wi * ai;
+    if (atomic)
+      atomicAdd(&gx[idx], (TD)v);
+    else
+      gx[idx] = (TD)v;
+  }
+};
+
+// One subproblem of one grid, executed by the whole block (shared by the
+// per-subproblem kernel, the work-queue kernel of batched plans and the
+// fused gradient kernel).  Grid t is fine + t*nftot; each point's value goes
+// through epi(input index, re, im).  tmap (or null): TMA map of the grids;
+// t_map = this grid's index in it.
+template <typename TC, typename TD, int DIM, int G, typename Epi>
 __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                                 const PtRec<TC, DIM>* __restrict__ recs,
                                                 const SubArgs& sa, int sub, int t,
                                                 const cplx_t<TC>* __restrict__ fine,
-                                                cplx_t<TD>* __restrict__ c, int64_t nftot,
+                                                const Epi& epi, int64_t nftot,
                                                 unsigned char* smem_raw,
                                                 const CUtensorMap* tmap = nullptr,
                                                 int t_map = 0) {
@@ -139,7 +187,6 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
   load_coef<TC, NCO>(co, ks, gl, w);
   __syncthreads();
 
-  cplx_t<TD>* ct = c + (int64_t)t * M;
   const bool lane_on = gl < w;
   constexpr int kStep = NWARP * PPW;
   // each group's next point record and output index are loaded one
@@ -214,12 +261,7 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
     ar *= kx;
     ai *= kx;
     group_reduce<TC, G>(ar, ai);
-    if (valid && gl == 0) {
-      cplx_t<TD> o;
-      o.x = (TD)ar;
-      o.y = (TD)ai;
-      ct[out_idx] = o;
-    }
+    if (valid && gl == 0) epi(out_idx, ar, ai);
   }
 }
 
@@ -230,9 +272,35 @@ __global__ void __launch_bounds__(kThreads)
                      int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
                      int t_base) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  interp_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, fine, c, nftot,
+  const StoreOut<TC, TD> epi{c + (int64_t)blockIdx.y * M};
+  interp_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, fine, epi, nftot,
                                   smem_raw, use_tma ? &tmap : nullptr,
                                   t_base + (int)blockIdx.y);
+}
+
+// Fused gradient gather: block (subproblem, t*E + e) gathers grid t*E + e at
+// the subproblem's points into the strength or coordinate gradient.
+template <typename TC, typename TD, int DIM, int G>
+__global__ void __launch_bounds__(kThreads)
+    interp_grad_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M,
+                          const PtRec<TC, DIM>* __restrict__ recs, SubArgs sa,
+                          const cplx_t<TC>* __restrict__ grids, int E, int64_t nftot, int mode,
+                          int iflag, int base, int4 dims, GradOut<TD> go, int atomic,
+                          const __grid_constant__ CUtensorMap tmap, int use_tma) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int te = blockIdx.y;
+  const int t = te / E, e = te - t * E;
+  const int dd[4] = {dims.x, dims.y, dims.z, dims.w};
+  GradEpi<TC, TD> epi;
+  epi.strength = e < base;
+  epi.out_c = go.out_c ? go.out_c + (int64_t)t * M : nullptr;
+  epi.gx = e >= base ? go.gx[dd[e]] : nullptr;
+  epi.w = go.w + (int64_t)t * M;
+  epi.mode = mode;
+  epi.iflag = iflag;
+  epi.atomic = atomic;
+  interp_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, te, grids, epi, nftot,
+                                  smem_raw, use_tma ? &tmap : nullptr, te);
 }
 
 template <typename TC, typename TD, int DIM, int G>
@@ -338,8 +406,9 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t local = item - item_start[lo];
     const int sub = (int)(local / T), t = (int)(local - (int64_t)sub * T);
     SubArgs sa{P.sub_bin, P.sub_off, P.n_sub, P.bin_start, P.bin_count, P.perm, 1};
+    const StoreOut<TC, TD> epi{c + P.c_off + (int64_t)t * P.M};
     interp_sm_block<TC, TD, DIM, G>(P.g, P.ks, P.M, (const PtRec<TC, DIM>*)P.recs, sa, sub, t,
-                                    arena + P.grid_off, c + P.c_off, P.nftot, smem_raw);
+                                    arena + P.grid_off, epi, P.nftot, smem_raw);
   }
 }
 
@@ -500,6 +569,76 @@ bool tile_tensor_map(const Geom& g, const void* grid, int nb, CUtensorMap* out) 
                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
+
+namespace {
+
+template <typename TC, typename TD, int DIM, int G>
+cudaError_t run_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                               const SortState& st, const void* grids, int ntr, int E, int mode,
+                               int iflag, int base, const int* dims, const GradOut<TD>& go,
+                               const CUtensorMap* tmap, cudaStream_t s) {
+  SubArgs sa;
+  sa.sub_bin = st.sub_bin;
+  sa.sub_off = st.sub_off;
+  sa.n_sub = st.n_sub;
+  sa.bin_start = st.bin_start;
+  sa.bin_count = st.bin_count;
+  sa.perm = st.perm;
+  sa.sorted = 1;
+  if (st.max_sub == 0) return cudaSuccess;
+  int64_t nftot = 1;
+  for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
+  const size_t smem = (size_t)tile_cells(DIM, g.bs, g.w) * sizeof(cplx_t<TC>);
+  auto kern = interp_grad_sm_kernel<TC, TD, DIM, G>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  CUtensorMap m;
+  memset(&m, 0, sizeof(m));
+  const int use = tmap != nullptr && sizeof(TC) == 4;
+  if (use) m = *tmap;
+  kern<<<dim3((unsigned)st.max_sub, (unsigned)(ntr * E)), kThreads, smem, s>>>(
+      g, ks, M, (const PtRec<TC, DIM>*)st.recs, sa, (const cplx_t<TC>*)grids, E, nftot, mode,
+      iflag, base, make_int4(dims[0], dims[1], dims[2], dims[3]), go, ntr > 1 ? 1 : 0, m, use);
+  note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+template <typename TC, typename TD>
+cudaError_t launch_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                                  const SortState& st, const void* grids, int ntr, int E,
+                                  int mode, int iflag, int base, const int* dims,
+                                  const GradOut<TD>& go, const CUtensorMap* tmap,
+                                  cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  const int G = g.w > 8 ? 16 : g.w > 6 ? 8 : 6;
+#define GBN_GDISPATCH(DIM, TM)                                                                 \
+  return G == 16 ? run_interp_grad_sm<TC, TD, DIM, 16>(g, ks, M, st, grids, ntr, E, mode,     \
+                                                       iflag, base, dims, go, TM, s)          \
+         : G == 8 ? run_interp_grad_sm<TC, TD, DIM, 8>(g, ks, M, st, grids, ntr, E, mode,     \
+                                                       iflag, base, dims, go, TM, s)          \
+                  : run_interp_grad_sm<TC, TD, DIM, 6>(g, ks, M, st, grids, ntr, E, mode,     \
+                                                       iflag, base, dims, go, TM, s);
+  switch (g.dim) {
+    case 1:
+      GBN_GDISPATCH(1, nullptr)
+    case 2:
+      GBN_GDISPATCH(2, tmap)
+    default:
+      GBN_GDISPATCH(3, tmap)
+  }
+#undef GBN_GDISPATCH
+}
+
+#define GBN_INST_IGS(TC, TD)                                                                   \
+  template cudaError_t launch_interp_grad_sm<TC, TD>(                                          \
+      const Geom&, const KerSpec<TC>&, int64_t, const SortState&, const void*, int, int, int,  \
+      int, int, const int*, const GradOut<TD>&, const CUtensorMap*, cudaStream_t);
+GBN_INST_IGS(float, float)
+GBN_INST_IGS(float, double)
+GBN_INST_IGS(double, double)
 
 cudaError_t read_wait_timeouts(unsigned* out, bool reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_wait_timeouts, sizeof(unsigned));

@@ -1083,13 +1083,15 @@ int plan_grad(gbn_plan_s* p, gbn_points_s& ps, int ntr, const void* src, const v
     GBN_CUDA(e);
     GBN_TRY(exec_fft(p, p->gfine.p, nb * E, sign, 1));
     if (p->comp_single) {
+      CUtensorMap map;
+      const CUtensorMap* tm = grid_map(p, ps, p->gfine.p, nb * E, &map);
       e = p->data_single
               ? launch_interp_grad<float, float>(p->geom, ker_spec<float>(p), ps.M, ps.st,
                                                  p->gfine.p, nb, E, mode, p->iflag, base, dims,
-                                                 win, outc, gxx, p->method == 2, s)
+                                                 win, outc, gxx, p->method == 2, s, tm)
               : launch_interp_grad<float, double>(p->geom, ker_spec<float>(p), ps.M, ps.st,
                                                   p->gfine.p, nb, E, mode, p->iflag, base, dims,
-                                                  win, outc, gxx, p->method == 2, s);
+                                                  win, outc, gxx, p->method == 2, s, tm);
     } else {
       e = launch_interp_grad<double, double>(p->geom, ker_spec<double>(p), ps.M, ps.st,
                                              p->gfine.p, nb, E, mode, p->iflag, base, dims, win,
