@@ -82,6 +82,12 @@ __host__ __device__ inline size_t spread_smem_bytes(int dim, const int* bs, int 
          (stash ? (size_t)maxsub * 2 * (single ? 4 : 8) : 0);
 }
 
+// Shared memory of one interpolation tile (a complex per cell), padded to 128
+// bytes so that consecutive tiles of a multi-grid block stay TMA-aligned.
+__host__ __device__ inline size_t interp_tile_bytes(int dim, const int* bs, int w, bool single) {
+  return ((size_t)tile_cells(dim, bs, w) * 2 * (single ? 4 : 8) + 127) & ~(size_t)127;
+}
+
 // How points map onto the grid: mode 0 folds periodically (types 1/2),
 // mode 1 rescales (type-3 sources): X = (x - center)*scale + nf/2.
 struct FoldSpec {

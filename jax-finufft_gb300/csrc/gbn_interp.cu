@@ -13,6 +13,7 @@
 //   method 1 (GM): gathers straight from the fine grid through L1/L2.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -26,6 +27,17 @@ namespace {
 // Bounded waits that gave up (see read_wait_timeouts).
 __device__ unsigned g_wait_timeouts;
 constexpr int kWaitPolls = 1 << 20;
+
+// Grids per shared-memory interpolation block: up to four stacked grids share
+// each point's record and kernel values (FP32, groups of at most 8 lanes,
+// while the block's tiles stay within 100 KB of shared memory).
+template <typename TC, int G>
+int grids_per_block(int ngrid, size_t tile_bytes) {
+  if (sizeof(TC) != 4 || G > 8) return 1;
+  if (ngrid >= 3 && 4 * tile_bytes <= 100 * 1024) return 4;
+  if (ngrid >= 2 && 2 * tile_bytes <= 100 * 1024) return 2;
+  return 1;
+}
 
 struct SubArgs {
   const int* sub_bin;
@@ -80,60 +92,62 @@ __device__ __forceinline__ void group_reduce(TC& a, TC& b) {
 }
 
 // Epilogue of the gather: the interpolated value of a point (input index
-// idx) goes to the output array.
+// idx) from the block's grid slot k goes to transform t0 + k of the output.
 template <typename TC, typename TD>
 struct StoreOut {
-  cplx_t<TD>* ct;
-  __device__ __forceinline__ void operator()(int idx, TC ar, TC ai) const {
+  cplx_t<TD>* c;
+  int64_t M;
+  int t0;
+  __device__ __forceinline__ void operator()(int k, int idx, TC ar, TC ai) const {
     cplx_t<TD> o;
     o.x = (TD)ar;
     o.y = (TD)ai;
-    ct[idx] = o;
+    c[(int64_t)(t0 + k) * M + idx] = o;
   }
 };
 
-// Epilogue of the fused gradient gather for grid e of transform t: e < base
-// stores the value as the strength gradient; otherwise the coordinate
-// gradient of axis dims[e] gets Re(conj-weighted) terms against the weights
-// w (mode 0, type-1 plan: iflag * (w_re*v_im - w_im*v_re); mode 1, type-2
-// plan: w_re*v_re + w_im*v_im), added atomically when several transforms
-// share the gradient, else stored.
+// Epilogue of the fused gradient gather for grid g0 + k = t*E + e (grid e of
+// transform t): e < base stores the value as the strength gradient;
+// otherwise the coordinate gradient of axis dims[e] gets Re(conj-weighted)
+// terms against the weights w (mode 0, type-1 plan: iflag * (w_re*v_im -
+// w_im*v_re); mode 1, type-2 plan: w_re*v_re + w_im*v_im), added atomically
+// when several transforms share the gradient, else stored.
 template <typename TC, typename TD>
 struct GradEpi {
-  cplx_t<TD>* out_c;
-  TD* gx;
-  const cplx_t<TD>* w;
-  int strength, mode, iflag, atomic;
-  __device__ __forceinline__ void operator()(int idx, TC ar, TC ai) const {
-    if (strength) {
-      if (out_c) {
-        cplx_t<TD> o;
-        o.x = (TD)ar;
-        o.y = (TD)ai;
-        out_c[idx] = o;
-      }
+  cplx_t<TD>* out[4];      // slot k: strength gradient of its transform, or null
+  TD* gx[4];               // slot k: coordinate gradient of its axis, or null
+  const cplx_t<TD>* w[4];  // slot k: weights of its transform
+  int mode, iflag, atomic;
+  __device__ __forceinline__ void operator()(int k, int idx, TC ar, TC ai) const {
+    if (out[k]) {
+      cplx_t<TD> o;
+      o.x = (TD)ar;
+      o.y = (TD)ai;
+      out[k][idx] = o;
       return;
     }
-    if (!gx) return;
-    const cplx_t<TD> wv = w[idx];
+    if (!gx[k]) return;
+    const cplx_t<TD> wv = w[k][idx];
     const TC wr = (TC)wv.x, wi = (TC)wv.y;
     const TC v = mode == 0 ? (TC)iflag * (wr * ai - wi * ar) : wr * ar + wi * ai;
     if (atomic)
-      atomicAdd(&gx[idx], (TD)v);
+      atomicAdd(&gx[k][idx], (TD)v);
     else
-      gx[idx] = (TD)v;
+      gx[k][idx] = (TD)v;
   }
 };
 
-// One subproblem of one grid, executed by the whole block (shared by the
-// per-subproblem kernel, the work-queue kernel of batched plans and the
-// fused gradient kernel).  Grid t is fine + t*nftot; each point's value goes
-// through epi(input index, re, im).  tmap (or null): TMA map of the grids;
-// t_map = this grid's index in it.
-template <typename TC, typename TD, int DIM, int G, typename Epi>
+// One subproblem of ntb <= TB grids t, t+1, ..., executed by the whole block
+// (shared by the per-subproblem kernel, the work-queue kernel of batched
+// plans and the fused gradient kernel).  Grid t+k is fine + (t+k)*nftot and
+// is staged in tile k (shared memory, each tile padded to 128 bytes); a
+// point's record and kernel values are computed once for all its grids, and
+// its value from grid slot k goes through epi(k, input index, re, im).
+// tmap (or null): TMA map of the grids; t_map = grid t's index in it.
+template <typename TC, typename TD, int DIM, int G, int TB, typename Epi>
 __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
                                                 const PtRec<TC, DIM>* __restrict__ recs,
-                                                const SubArgs& sa, int sub, int t,
+                                                const SubArgs& sa, int sub, int t, int ntb,
                                                 const cplx_t<TC>* __restrict__ fine,
                                                 const Epi& epi, int64_t nftot,
                                                 unsigned char* smem_raw,
@@ -147,41 +161,47 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
   const int w = g.w;
   const Tile<DIM> tl(g, bin);
   const int ncell = tl.ncell;
-  cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
-  const cplx_t<TC>* ft = fine + (int64_t)t * nftot;
+  const int tile_c = (int)(interp_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4) / sizeof(cplx_t<TC>));
+  cplx_t<TC>* tiles = reinterpret_cast<cplx_t<TC>*>(smem_raw);  // tile k at tiles + k*tile_c
   bool staged = false;
   if constexpr (sizeof(TC) == 4 && DIM > 1) {
-    if (tmap != nullptr && tl.interior(g) && (smem_addr(tile) & 127u) == 0) {
+    if (tmap != nullptr && tl.interior(g) && (smem_addr(tiles) & 127u) == 0 &&
+        ((size_t)tile_c * sizeof(cplx_t<TC>)) % 128 == 0) {
       __shared__ alignas(8) uint64_t s_bar;
       if (threadIdx.x == 0) {
         mbar_init(&s_bar, 1);
-        mbar_expect_tx(&s_bar, (uint32_t)(ncell * sizeof(cplx_t<TC>)));
-        if (DIM == 2)
-          tma_load_2d(tile, tmap, &s_bar, 2 * tl.org[0], tl.org[1] + t_map * (int)g.nf[1]);
-        else
-          tma_load_3d(tile, tmap, &s_bar, 2 * tl.org[0], tl.org[1],
-                      tl.org[2] + t_map * (int)g.nf[2]);
+        mbar_expect_tx(&s_bar, (uint32_t)(ntb * ncell * sizeof(cplx_t<TC>)));
+        for (int k = 0; k < ntb; ++k) {
+          if (DIM == 2)
+            tma_load_2d(tiles + k * tile_c, tmap, &s_bar, 2 * tl.org[0],
+                        tl.org[1] + (t_map + k) * (int)g.nf[1]);
+          else
+            tma_load_3d(tiles + k * tile_c, tmap, &s_bar, 2 * tl.org[0], tl.org[1],
+                        tl.org[2] + (t_map + k) * (int)g.nf[2]);
+        }
       }
       __syncthreads();  // the barrier is initialised before anyone polls it
       if (!mbar_wait_bounded(&s_bar, 0, kWaitPolls)) {
         if (threadIdx.x == 0) atomicAdd(&g_wait_timeouts, 1u);
-        mbar_wait_bounded(&s_bar, 0, kWaitPolls);  // the copy in flight, bounded again
+        mbar_wait_bounded(&s_bar, 0, kWaitPolls);  // the copies in flight, bounded again
       }
       staged = true;
     }
   }
   if (!staged) {
     const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
-    CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
-    for (int i = threadIdx.x; i < ncell; i += kThreads, cw.next()) {
-      const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
-      const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
-      const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
-      tile[i] = ft[(g2 * nf1 + g1) * nf0 + g0];
+    for (int k = 0; k < ntb; ++k) {
+      const cplx_t<TC>* ft = fine + (int64_t)(t + k) * nftot;
+      cplx_t<TC>* tile = tiles + k * tile_c;
+      CellWalk cw(threadIdx.x, kThreads, tl.T[0], tl.T[1]);
+      for (int i = threadIdx.x; i < ncell; i += kThreads, cw.next()) {
+        const int g0 = wrap_i32(tl.org[0] + cw.c0, nf0);
+        const int g1 = DIM > 1 ? wrap_i32(tl.org[1] + cw.c1, nf1) : 0;
+        const int g2 = DIM > 2 ? wrap_i32(tl.org[2] + cw.c2, nf2) : 0;
+        tile[i] = ft[(g2 * nf1 + g1) * nf0 + g0];
+      }
     }
   }
-  const int org[3] = {tl.org[0], tl.org[1], tl.org[2]};
-  const int T[3] = {tl.T[0], tl.T[1], tl.T[2]};
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
   TC co[NCO];
   load_coef<TC, NCO>(co, ks, gl, w);
@@ -199,6 +219,8 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
     rn = recs[jn];
     on_next = sa.perm ? sa.perm[jn] : jn;
   }
+  const int T0 = tl.T[0];
+  const int plane = T0 * tl.T[1];
   for (int pb = warp * PPW; pb < cnt; pb += kStep) {
     const int pi = pb + grp;
     const bool valid = pi < cnt && grp < PPW;
@@ -211,96 +233,108 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
       on_next = sa.perm ? sa.perm[jn] : jn;
     }
     const TC kx = kerval<TC, NCO>(co, ks, r.d[0], gl, w);
-    const int l0 = r.i[0] - org[0] + gl;
-    TC ar = TC(0), ai = TC(0);
-    if (DIM == 1) {
-      if (lane_on) {
-        const cplx_t<TC> v = tile[l0];
-        ar = v.x;
-        ai = v.y;
-      }
-    } else if (DIM == 2) {
-      // the group's y kernel values, fetched once per point
-      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      TC kyr[G];
+    const int l0 = r.i[0] - tl.org[0] + gl;
+    // the group's y (and z) kernel values, fetched once per point
+    TC ky = TC(0), kz = TC(0);
+    TC kyr[G];
+    if (DIM > 1) {
+      ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
 #pragma unroll
       for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
-      const cplx_t<TC>* col = tile + (r.i[1] - org[1]) * T[0] + l0;
+    }
+    if (DIM > 2) kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
+    const int cell0 = DIM == 1 ? l0
+                      : DIM == 2 ? (r.i[1] - tl.org[1]) * T0 + l0
+                                 : ((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * T0 +
+                                       l0;
 #pragma unroll
-      for (int iy = 0; iy < G; ++iy) {
-        if (iy < w && lane_on) {
-          const cplx_t<TC> v = col[iy * T[0]];
-          ar = fma(v.x, kyr[iy], ar);
-          ai = fma(v.y, kyr[iy], ai);
+    for (int k = 0; k < TB; ++k) {
+      if (k >= ntb) break;
+      const cplx_t<TC>* tk = tiles + k * tile_c + cell0;
+      TC ar = TC(0), ai = TC(0);
+      if (DIM == 1) {
+        if (lane_on) {
+          const cplx_t<TC> v = tk[0];
+          ar = v.x;
+          ai = v.y;
         }
-      }
-    } else {
-      const TC ky = kerval<TC, NCO>(co, ks, r.d[1], gl, w);
-      const TC kz = kerval<TC, NCO>(co, ks, r.d[2], gl, w);
-      TC kyr[G];
-#pragma unroll
-      for (int i = 0; i < G; ++i) kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
-      const int plane = T[0] * T[1];
-      const cplx_t<TC>* zrow = tile + ((r.i[2] - org[2]) * T[1] + (r.i[1] - org[1])) * T[0] + l0;
-      for (int iz = 0; iz < w; ++iz) {
-        const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
-        TC yr = TC(0), yi = TC(0);
+      } else if (DIM == 2) {
 #pragma unroll
         for (int iy = 0; iy < G; ++iy) {
           if (iy < w && lane_on) {
-            const cplx_t<TC> v = zrow[iy * T[0]];
-            yr = fma(v.x, kyr[iy], yr);
-            yi = fma(v.y, kyr[iy], yi);
+            const cplx_t<TC> v = tk[iy * T0];
+            ar = fma(v.x, kyr[iy], ar);
+            ai = fma(v.y, kyr[iy], ai);
           }
         }
-        ar = fma(yr, kzv, ar);
-        ai = fma(yi, kzv, ai);
-        zrow += plane;
+      } else {
+        const cplx_t<TC>* zrow = tk;
+        for (int iz = 0; iz < w; ++iz) {
+          const TC kzv = __shfl_sync(0xffffffffu, kz, grp * G + iz);
+          TC yr = TC(0), yi = TC(0);
+#pragma unroll
+          for (int iy = 0; iy < G; ++iy) {
+            if (iy < w && lane_on) {
+              const cplx_t<TC> v = zrow[iy * T0];
+              yr = fma(v.x, kyr[iy], yr);
+              yi = fma(v.y, kyr[iy], yi);
+            }
+          }
+          ar = fma(yr, kzv, ar);
+          ai = fma(yi, kzv, ai);
+          zrow += plane;
+        }
       }
+      ar *= kx;
+      ai *= kx;
+      group_reduce<TC, G>(ar, ai);
+      if (valid && gl == 0) epi(k, out_idx, ar, ai);
     }
-    ar *= kx;
-    ai *= kx;
-    group_reduce<TC, G>(ar, ai);
-    if (valid && gl == 0) epi(out_idx, ar, ai);
   }
 }
 
-template <typename TC, typename TD, int DIM, int G>
+// grid (subproblems, ceil(ntr / TB)); block y handles transforms TB*y ...
+template <typename TC, typename TD, int DIM, int G, int TB>
 __global__ void __launch_bounds__(kThreads)
     interp_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
                      SubArgs sa, const cplx_t<TC>* __restrict__ fine, cplx_t<TD>* __restrict__ c,
-                     int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
-                     int t_base) {
+                     int64_t nftot, int ntr, const __grid_constant__ CUtensorMap tmap,
+                     int use_tma, int t_base) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const StoreOut<TC, TD> epi{c + (int64_t)blockIdx.y * M};
-  interp_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, blockIdx.y, fine, epi, nftot,
-                                  smem_raw, use_tma ? &tmap : nullptr,
-                                  t_base + (int)blockIdx.y);
+  const int t = TB * (int)blockIdx.y;
+  const StoreOut<TC, TD> epi{c, M, t};
+  interp_sm_block<TC, TD, DIM, G, TB>(g, ks, M, recs, sa, blockIdx.x, t, min(TB, ntr - t), fine,
+                                      epi, nftot, smem_raw, use_tma ? &tmap : nullptr,
+                                      t_base + t);
 }
 
-// Fused gradient gather: block (subproblem, t*E + e) gathers grid t*E + e at
-// the subproblem's points into the strength or coordinate gradient.
-template <typename TC, typename TD, int DIM, int G>
+// Fused gradient gather: block (subproblem, y) gathers grids TB*y ... of
+// the ntr*E grids (grid t*E + e) at the subproblem's points into the
+// strength or coordinate gradients, with each point's kernel values shared
+// by the block's grids.
+template <typename TC, typename TD, int DIM, int G, int TB>
 __global__ void __launch_bounds__(kThreads)
     interp_grad_sm_kernel(Geom g, KerSpec<TC> ks, int64_t M,
                           const PtRec<TC, DIM>* __restrict__ recs, SubArgs sa,
-                          const cplx_t<TC>* __restrict__ grids, int E, int64_t nftot, int mode,
-                          int iflag, int base, int4 dims, GradOut<TD> go, int atomic,
+                          const cplx_t<TC>* __restrict__ grids, int ngrid, int E, int64_t nftot,
+                          int mode, int iflag, int base, int4 dims, GradOut<TD> go, int atomic,
                           const __grid_constant__ CUtensorMap tmap, int use_tma) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const int te = blockIdx.y;
-  const int t = te / E, e = te - t * E;
-  const int dd[4] = {dims.x, dims.y, dims.z, dims.w};
+  const int g0 = TB * (int)blockIdx.y;
   GradEpi<TC, TD> epi;
-  epi.strength = e < base;
-  epi.out_c = go.out_c ? go.out_c + (int64_t)t * M : nullptr;
-  epi.gx = e >= base ? go.gx[dd[e]] : nullptr;
-  epi.w = go.w + (int64_t)t * M;
+  const int dd[4] = {dims.x, dims.y, dims.z, dims.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int gi = g0 + (k < TB ? k : 0), t = gi / E, e = gi - t * E;
+    epi.out[k] = e < base && go.out_c ? go.out_c + (int64_t)t * M : nullptr;
+    epi.gx[k] = e >= base ? go.gx[dd[e]] : nullptr;
+    epi.w[k] = go.w + (int64_t)t * M;
+  }
   epi.mode = mode;
   epi.iflag = iflag;
   epi.atomic = atomic;
-  interp_sm_block<TC, TD, DIM, G>(g, ks, M, recs, sa, blockIdx.x, te, grids, epi, nftot,
-                                  smem_raw, use_tma ? &tmap : nullptr, te);
+  interp_sm_block<TC, TD, DIM, G, TB>(g, ks, M, recs, sa, blockIdx.x, g0, min(TB, ngrid - g0),
+                                      grids, epi, nftot, smem_raw, use_tma ? &tmap : nullptr, g0);
 }
 
 template <typename TC, typename TD, int DIM, int G>
@@ -406,9 +440,9 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t local = item - item_start[lo];
     const int sub = (int)(local / T), t = (int)(local - (int64_t)sub * T);
     SubArgs sa{P.sub_bin, P.sub_off, P.n_sub, P.bin_start, P.bin_count, P.perm, 1};
-    const StoreOut<TC, TD> epi{c + P.c_off + (int64_t)t * P.M};
-    interp_sm_block<TC, TD, DIM, G>(P.g, P.ks, P.M, (const PtRec<TC, DIM>*)P.recs, sa, sub, t,
-                                    arena + P.grid_off, epi, P.nftot, smem_raw);
+    const StoreOut<TC, TD> epi{c + P.c_off, P.M, t};
+    interp_sm_block<TC, TD, DIM, G, 1>(P.g, P.ks, P.M, (const PtRec<TC, DIM>*)P.recs, sa, sub, t,
+                                       1, arena + P.grid_off, epi, P.nftot, smem_raw);
   }
 }
 
@@ -448,24 +482,37 @@ cudaError_t run_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
   int64_t nftot = 1;
   for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
   const PtRec<TC, DIM>* recs = (const PtRec<TC, DIM>*)(sa.sorted ? st.recs : st.recs_in);
-  for (int t0 = 0; t0 < ntr; t0 += 65535) {
-    const int nt = ntr - t0 < 65535 ? ntr - t0 : 65535;
-    dim3 grid((unsigned)nblk, (unsigned)nt);
+  const bool sm = method == 2 && sa.sorted;
+  const size_t tile1 = interp_tile_bytes(DIM, g.bs, g.w, sizeof(TC) == 4);
+  const int TB = sm ? grids_per_block<TC, G>(ntr, tile1) : 1;
+  for (int t0 = 0; t0 < ntr; t0 += 65535 * TB) {
+    const int nt = std::min(ntr - t0, 65535 * TB);
+    dim3 grid((unsigned)nblk, (unsigned)((nt + TB - 1) / TB));
     const cplx_t<TC>* ft = (const cplx_t<TC>*)fine + (int64_t)t0 * nftot;
     cplx_t<TD>* ct = (cplx_t<TD>*)c + (int64_t)t0 * M;
-    if (method == 2 && sa.sorted) {
-      const int64_t ncell = tile_cells(DIM, g.bs, g.w);
-      const size_t smem = (size_t)ncell * sizeof(cplx_t<TC>);
-      auto kern = interp_sm_kernel<TC, TD, DIM, G>;
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
-      if (e != cudaSuccess) return e;
+    if (sm) {
       CUtensorMap m;
       memset(&m, 0, sizeof(m));
       const int use = tmap != nullptr && sizeof(TC) == 4;
       if (use) m = *tmap;
-      kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ft, ct, nftot, m, use, t0);
-      note_launch();
+      auto go = [&](auto kern, int tb) -> cudaError_t {
+        const size_t smem = tile1 * tb;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, kThreads, smem, s>>>(g, ks, M, recs, sa, ft, ct, nftot, nt, m, use, t0);
+        note_launch();
+        return cudaSuccess;
+      };
+      cudaError_t e;
+      if constexpr (sizeof(TC) == 4 && G <= 8) {
+        e = TB == 4   ? go(interp_sm_kernel<TC, TD, DIM, G, 4>, 4)
+            : TB == 2 ? go(interp_sm_kernel<TC, TD, DIM, G, 2>, 2)
+                      : go(interp_sm_kernel<TC, TD, DIM, G, 1>, 1);
+      } else {
+        e = go(interp_sm_kernel<TC, TD, DIM, G, 1>, 1);
+      }
+      if (e != cudaSuccess) return e;
     } else {
       interp_gm_kernel<TC, TD, DIM, G><<<grid, kThreads, 0, s>>>(g, ks, M, recs, sa, ft, ct,
                                                                   nftot);
@@ -588,20 +635,30 @@ cudaError_t run_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t M,
   if (st.max_sub == 0) return cudaSuccess;
   int64_t nftot = 1;
   for (int d = 0; d < DIM; ++d) nftot *= g.nf[d];
-  const size_t smem = (size_t)tile_cells(DIM, g.bs, g.w) * sizeof(cplx_t<TC>);
-  auto kern = interp_grad_sm_kernel<TC, TD, DIM, G>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
+  const int ngrid = ntr * E;
+  const size_t tile1 = interp_tile_bytes(DIM, g.bs, g.w, sizeof(TC) == 4);
+  const int TB = grids_per_block<TC, G>(ngrid, tile1);
   CUtensorMap m;
   memset(&m, 0, sizeof(m));
   const int use = tmap != nullptr && sizeof(TC) == 4;
   if (use) m = *tmap;
-  kern<<<dim3((unsigned)st.max_sub, (unsigned)(ntr * E)), kThreads, smem, s>>>(
-      g, ks, M, (const PtRec<TC, DIM>*)st.recs, sa, (const cplx_t<TC>*)grids, E, nftot, mode,
-      iflag, base, make_int4(dims[0], dims[1], dims[2], dims[3]), go, ntr > 1 ? 1 : 0, m, use);
-  note_launch();
-  return cudaGetLastError();
+  auto launch = [&](auto kern, int tb) -> cudaError_t {
+    const size_t smem = tile1 * tb;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<dim3((unsigned)st.max_sub, (unsigned)((ngrid + tb - 1) / tb)), kThreads, smem, s>>>(
+        g, ks, M, (const PtRec<TC, DIM>*)st.recs, sa, (const cplx_t<TC>*)grids, ngrid, E, nftot,
+        mode, iflag, base, make_int4(dims[0], dims[1], dims[2], dims[3]), go, ntr > 1 ? 1 : 0, m,
+        use);
+    note_launch();
+    return cudaGetLastError();
+  };
+  if constexpr (sizeof(TC) == 4 && G <= 8) {
+    if (TB == 4) return launch(interp_grad_sm_kernel<TC, TD, DIM, G, 4>, 4);
+    if (TB == 2) return launch(interp_grad_sm_kernel<TC, TD, DIM, G, 2>, 2);
+  }
+  return launch(interp_grad_sm_kernel<TC, TD, DIM, G, 1>, 1);
 }
 
 }  // namespace
