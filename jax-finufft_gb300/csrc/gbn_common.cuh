@@ -228,10 +228,13 @@ cudaError_t launch_t3_prephase_factors(int dim, int64_t M, const TX* const* x, c
                                        const double* cs, int iflag, void* fac, cudaStream_t s);
 
 // Type 3: per-target post factor exp(iflag*i*sum_d cx_d*s_d) / prod_d psihat(tau_d).
+// With tau_max > 0 (a bound on |tau|), psihat comes from a piecewise
+// Chebyshev fit checked on the host against the quadrature (relative 1e-14
+// in FP64, 1e-9 in FP32), else from the quadrature per target.
 template <typename TX, typename TC>
 cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
                                    const double* const* tau, int iflag, int w, double beta,
-                                   void* fac, cudaStream_t s);
+                                   void* fac, cudaStream_t s, double tau_max = 0.0);
 
 // Gradient grids: for every transform, E fine grids from its modes `in`
 // (ntr, N): grid e < base holds mode/psihat, grid e >= base holds

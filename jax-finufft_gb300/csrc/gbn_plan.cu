@@ -796,6 +796,14 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
       nmodes_inner[d] = p->nf[d];
     }
     for (int d = p->dim; d < 3; ++d) p->nf[d] = 1;
+    // bound on |tau| = |s - cs| / scale over the targets (for the psihat fit)
+    double tau_max = 0.0;
+    for (int d = 0; d < p->dim && N > 0; ++d) {
+      const double smin = h[2 * (p->dim + d)], smax = h[2 * (p->dim + d) + 1];
+      const double r = std::max(std::fabs(smin - p->t3_cs[d]), std::fabs(smax - p->t3_cs[d]));
+      tau_max = std::max(tau_max, r / p->t3_scale[d]);
+    }
+    tau_max = tau_max * (1.0 + 1e-9) + 1e-300;
     p->nftot = p->nf[0] * p->nf[1] * p->nf[2];
     if (p->nftot > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "type-3 grid too large (> 2^31 cells)");
     p->Nt = N;
@@ -848,14 +856,14 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
       GBN_CUDA((launch_t3_prephase_factors<TX, float>(p->dim, M, xs, p->t3_cx, p->t3_cs,
                                                        p->iflag, p->t3_pre.p, st)));
       GBN_CUDA((launch_t3_post_factors<TX, float>(p->dim, N, ss, p->t3_cx, ctaus, p->iflag,
-                                                   p->w, p->beta, p->t3_post.p, st)));
+                                                   p->w, p->beta, p->t3_post.p, st, tau_max)));
     } else {
       GBN_CUDA((launch_t3_prephase_factors<double, double>(p->dim, M, (const double* const*)xs,
                                                            p->t3_cx, p->t3_cs, p->iflag,
                                                            p->t3_pre.p, st)));
       GBN_CUDA((launch_t3_post_factors<double, double>(p->dim, N, (const double* const*)ss,
                                                        p->t3_cx, ctaus, p->iflag, p->w,
-                                                       p->beta, p->t3_post.p, st)));
+                                                       p->beta, p->t3_post.p, st, tau_max)));
     }
   }
   if (sev) GBN_CUDA(cudaEventRecord(sev[1], st));

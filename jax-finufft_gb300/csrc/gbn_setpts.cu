@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <vector>
 
 #include <cstdint>
 
@@ -467,6 +469,44 @@ __global__ void t3_post_kernel(int dim, int64_t N, Ptrs3 s, double cx0, double c
   fac[k] = o;
 }
 
+// The same factors with psihat from a piecewise Chebyshev table: piece
+// p = min(|tau| / h, P - 1), coefficients tab[p*(D+1) .. ] (the first one
+// halved), evaluated by Clenshaw's recurrence.
+template <typename TX, typename TC>
+__global__ void t3_post_table_kernel(int dim, int64_t N, Ptrs3 s, double cx0, double cx1,
+                                     double cx2, CDPtrs3 tau, int iflag,
+                                     const double* __restrict__ tab, double h, int P, int D,
+                                     cplx_t<TC>* __restrict__ fac) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double cx[3] = {cx0, cx1, cx2};
+  const double inv_h = 1.0 / h;
+  double ph = 0.0, den = 1.0;
+  for (int d = 0; d < dim; ++d) {
+    double v = (double)((const TX*)s.p[d])[k];
+    if (!isfinite(v)) v = 0.0;
+    ph += cx[d] * v;
+    const double u = fabs(tau.p[d][k]);
+    int piece = (int)(u * inv_h);
+    piece = piece < 0 ? 0 : (piece >= P ? P - 1 : piece);
+    const double x = 2.0 * (u - piece * h) * inv_h - 1.0;
+    const double* c = tab + (int64_t)piece * (D + 1);
+    double b1 = 0.0, b2 = 0.0;
+    for (int n = D; n >= 1; --n) {
+      const double b0 = fma(2.0 * x, b1, c[n] - b2);
+      b2 = b1;
+      b1 = b0;
+    }
+    den *= fma(x, b1, c[0] - b2);
+  }
+  double sn, cn;
+  sincos((double)iflag * ph, &sn, &cn);
+  cplx_t<TC> o;
+  o.x = (TC)(cn / den);
+  o.y = (TC)(sn / den);
+  fac[k] = o;
+}
+
 template <typename TI, typename TO, typename TF>
 __global__ void cmul_kernel(int64_t n, int ntr, const cplx_t<TI>* __restrict__ in,
                             const cplx_t<TF>* __restrict__ fac, cplx_t<TO>* __restrict__ out) {
@@ -766,10 +806,69 @@ static void gauss_legendre(int q, double* x, double* wt) {
   }
 }
 
+// psihat(tau) = sum_i f_i cos(tau t_i) by the quadrature (FP64, host).
+double psihat_quad(const Quad& qd, double tau) {
+  double acc = 0.0;
+  for (int i = 0; i < qd.q; ++i) acc += qd.f[i] * std::cos(tau * qd.t[i]);
+  return acc;
+}
+
+// Piecewise Chebyshev fit of psihat on [0, tau_max] (degree D per piece,
+// pieces of width h halved until every check point of every piece -- nodes
+// off the interpolation nodes, piece ends included -- is within rel_tol of
+// the quadrature).  False when 4096 pieces do not reach it.
+bool fit_psihat(const Quad& qd, double tau_max, double rel_tol, int D, std::vector<double>& tab,
+                double& h, int& P) {
+  const double pi = 3.141592653589793238462643383279502884;
+  const double t_max = qd.t[qd.q - 1] > qd.t[0] ? qd.t[qd.q - 1] : qd.t[0];
+  double hh = t_max > 0.0 ? 2.0 / t_max : tau_max;
+  for (int attempt = 0; attempt < 12; ++attempt, hh *= 0.5) {
+    const int np = (int)std::ceil(tau_max * (1.0 + 1e-12) / hh) + 1;
+    if (np > 4096) return false;
+    std::vector<double> c((size_t)np * (D + 1));
+    std::vector<double> fv(D + 1);
+    for (int p = 0; p < np; ++p) {
+      const double a = p * hh;
+      for (int j = 0; j <= D; ++j) {
+        const double xj = std::cos(pi * (j + 0.5) / (D + 1));
+        fv[j] = psihat_quad(qd, a + 0.5 * (xj + 1.0) * hh);
+      }
+      for (int n = 0; n <= D; ++n) {
+        double acc = 0.0;
+        for (int j = 0; j <= D; ++j) acc += fv[j] * std::cos(pi * n * (j + 0.5) / (D + 1));
+        c[(size_t)p * (D + 1) + n] = (n == 0 ? 1.0 : 2.0) * acc / (D + 1);
+      }
+    }
+    bool ok = true;
+    for (int p = 0; p < np && ok; ++p) {
+      const double* cp = c.data() + (size_t)p * (D + 1);
+      for (int m = 0; m <= 16 && ok; ++m) {
+        const double x = -1.0 + 2.0 * m / 16.0;
+        double b1 = 0.0, b2 = 0.0;
+        for (int n = D; n >= 1; --n) {
+          const double b0 = 2.0 * x * b1 - b2 + cp[n];
+          b2 = b1;
+          b1 = b0;
+        }
+        const double approx = x * b1 - b2 + cp[0];
+        const double exact = psihat_quad(qd, p * hh + 0.5 * (x + 1.0) * hh);
+        if (!(std::fabs(approx - exact) <= rel_tol * std::fabs(exact))) ok = false;
+      }
+    }
+    if (ok) {
+      tab.swap(c);
+      h = hh;
+      P = np;
+      return true;
+    }
+  }
+  return false;
+}
+
 template <typename TX, typename TC>
 cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
                                    const double* const* tau, int iflag, int w, double beta,
-                                   void* fac, cudaStream_t s) {
+                                   void* fac, cudaStream_t s, double tau_max) {
   if (N == 0) return cudaSuccess;
   const double pi = 3.141592653589793238462643383279502884;
   Quad qd;
@@ -789,6 +888,24 @@ cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, cons
     sp.p[d] = sx[d];
     tp.p[d] = tau[d];
     c[d] = cx[d];
+  }
+  std::vector<double> tab;
+  double h = 0.0;
+  int P = 0;
+  constexpr int D = 20;
+  if (tau_max > 0.0 && fit_psihat(qd, tau_max, sizeof(TC) == 4 ? 1e-9 : 1e-14, D, tab, h, P)) {
+    double* dtab = nullptr;
+    cudaError_t e = cudaMallocAsync(&dtab, tab.size() * sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    // pageable source: the call returns once the host buffer has been consumed
+    e = cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    t3_post_table_kernel<TX, TC><<<grid1(N, 128), 128, 0, s>>>(
+        dim, N, sp, c[0], c[1], c[2], tp, iflag, dtab, h, P, D, (cplx_t<TC>*)fac);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaFreeAsync(dtab, s);
   }
   t3_post_kernel<TX, TC><<<grid1(N, 128), 128, 0, s>>>(dim, N, sp, c[0], c[1], c[2], tp, iflag,
                                                        qd, (cplx_t<TC>*)fac);
@@ -855,7 +972,8 @@ template cudaError_t launch_t3_targets<double>(int, int64_t, const double* const
                                                           void*, cudaStream_t);                \
   template cudaError_t launch_t3_post_factors<TX, TC>(int, int64_t, const TX* const*,          \
                                                       const double*, const double* const*,     \
-                                                      int, int, double, void*, cudaStream_t);
+                                                      int, int, double, void*, cudaStream_t,   \
+                                                      double);
 GBN_INST_T3(float, float)
 GBN_INST_T3(double, float)
 GBN_INST_T3(double, double)
