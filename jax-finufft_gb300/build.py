@@ -111,5 +111,35 @@ def build(verbose=False, force=False):
     return library_path()
 
 
+def build_xla_ffi(verbose=False):
+    """Compile xla/gbn_xla_ffi.cc into the module jax_finufft_gpu (the XLA
+    FFI handlers jax-finufft's lowering registers) next to libgbnufft.so.
+    Needs jax (for the FFI headers) and pybind11; returns the module path,
+    or None when either is missing."""
+    try:
+        import jax.ffi  # noqa: F401
+        import pybind11
+        import sysconfig
+    except ImportError:
+        return None
+    import jax
+
+    lib = build(verbose=verbose)
+    ext = sysconfig.get_config_var("EXT_SUFFIX") or ".so"
+    out = os.path.join(OUT_DIR, "jax_finufft_gpu" + ext)
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+    cmd = ["c++", "-O2", "-std=c++17", "-shared", "-fPIC",
+           "-I", jax.ffi.include_dir(), "-I", pybind11.get_include(),
+           "-I", sysconfig.get_paths()["include"], "-I", INCLUDE, "-I", cuda_inc,
+           os.path.join(HERE, "xla", "gbn_xla_ffi.cc"), "-L", OUT_DIR, "-lgbnufft",
+           "-Wl,-rpath," + OUT_DIR, "-o", out]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("XLA FFI module build failed:\n%s%s" % (r.stdout, r.stderr))
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, force="--force" in sys.argv))

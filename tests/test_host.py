@@ -224,3 +224,26 @@ def test_ctypes_arity_matches_header():
     assert len(arity) == len(declared_symbols())
     for name, n in arity.items():
         assert len(_native.SIGNATURES[name][1]) == n, (name, n, len(_native.SIGNATURES[name][1]))
+
+
+def test_xla_ffi_handlers_cover_the_targets():
+    """The XLA FFI handler source defines one handler per one-shot entry point
+    (the 18 targets of lib/jax_finufft_gpu.cc) and binds the attributes in
+    the one-shot ABI's order."""
+    import re
+
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = open(os.path.join(repo, "jax-finufft_gb300", "xla", "gbn_xla_ffi.cc")).read()
+    header = open(os.path.join(repo, "include", "gbnufft.h")).read()
+    targets = re.findall(r"GBN_TARGET\((nufft\dd\df?),\s*(\d),\s*(\d),\s*(float|double)\)", src)
+    names = {t[0] for t in targets}
+    oneshot = set(re.findall(r"gbn_(nufft\dd\df?)\(", header))
+    assert names == oneshot and len(names) == 18
+    for name, dim, ty, eps in targets:
+        assert name == "nufft%sd%s%s" % (dim, ty, "f" if eps == "float" else "")
+    regs = set(re.findall(r"GBN_REG\((nufft\dd\df?)\)", src))
+    assert regs == names
+    attrs = re.findall(r'Attr<[^>]+>\("(\w+)"\)', src)
+    assert attrs == ["eps", "iflag", "n_tot", "n_transf", "n_j", "n_k_1", "n_k_2", "n_k_3",
+                     "modeord", "upsampfac", "gpu_method", "gpu_sort", "gpu_kerevalmeth",
+                     "gpu_maxbatchsize", "debug"]
