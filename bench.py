@@ -152,6 +152,25 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(v, ws, device):
+    """The largest per-rank value of the job (one all-reduce; v itself on one
+    rank).  Replicas time the same work, so the slowest rank sets the step."""
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(points_per_rank, ms_max, ws):
+    """Whole-job throughput of ws replicas: all ranks' points over the
+    slowest rank's time (weak scaling)."""
+    return ws * points_per_rank / (ms_max * 1e-3)
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (oracle port)
 # ---------------------------------------------------------------------------
@@ -255,12 +274,8 @@ def run_ours(args):
         if ws > 1:
             torch.distributed.barrier()
 
-    def max_over_ranks(v):
-        if ws == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    def job_max(v):
+        return max_over_ranks(v, ws, dev)
 
     for _ in range(args.warmup):
         step()
@@ -296,8 +311,8 @@ def run_ours(args):
     lib.gbn_plan_info(p1, ctypes.byref(w), nf3, None, None)
     nf_total = nf3[0] * nf3[1] * nf3[2]
 
-    ms_step = max_over_ranks(ms_step)
-    value = ws * 2 * M / (ms_step * 1e-3)
+    ms_step = job_max(ms_step)
+    value = job_value(2 * M, ms_step, ws)
 
     # ---- e2e through the reference-facing C-ABI entry points, host buffers
     e2e_value = e2e_ms = None
@@ -305,7 +320,7 @@ def run_ours(args):
     d2h = N * N * N * 8
     if not args.no_e2e:
         e2e_value, e2e_ms = run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws,
-                                    barrier, max_over_ranks)
+                                    barrier, job_max)
     accuracy = round_trip_errors(dev, pts_h, f, c, g, N)
     rate = ctypes.c_double()
     _native.check(lib.gbn_probe_smem_atomics(sp, min(w.value, 8), ctypes.byref(rate)), "probe")
@@ -364,7 +379,7 @@ def run_ours(args):
     return finish(args, result, rank, ws)
 
 
-def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, max_over_ranks):
+def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, job_max):
     """Same round trip through gbn_nufft3d2f/gbn_nufft3d1f with host buffers."""
     import torch
 
@@ -402,8 +417,8 @@ def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, max_over_
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    return ws * 2 * M / (e2e_ms * 1e-3), e2e_ms
+    e2e_ms = job_max(e0.elapsed_time(e1) / args.steps)
+    return job_value(2 * M, e2e_ms, ws), e2e_ms
 
 
 def _freqs(n, like):
