@@ -22,7 +22,7 @@ from . import _native
 from .options import Opts, to_native, unpack_opts
 
 _lock = threading.Lock()
-_plans = OrderedDict()  # key -> plan handle (most recent last)
+_plans = OrderedDict()  # key -> (plan handle, lock serialising its calls), most recent last
 _MAX_PLANS = 8
 
 
@@ -31,7 +31,9 @@ def _opts_key(n):
 
 
 def get_plan(key):
-    """Plan handle for a cache key (created on first use)."""
+    """(plan handle, lock) for a cache key (created on first use).  Threads
+    that share a key share the plan; they hold its lock around every call
+    on it (a plan's cuFFT handles and buffers serve one call at a time)."""
     lib = _native.load()
     with _lock:
         h = _plans.get(key)
@@ -45,14 +47,19 @@ def get_plan(key):
     mk = lib.gbnf_makeplan if single else lib.gbn_makeplan
     _native.check(mk(nufft_type, dim, nm, iflag, ntr, eps, ctypes.byref(plan),
                      ctypes.byref(native), ctypes.c_void_p(stream or None)), "makeplan")
+    entry = (plan, threading.Lock())
     evict = []
     with _lock:
-        _plans[key] = plan
+        if key in _plans:  # another thread made it meanwhile
+            lib.gbn_destroy(plan)
+            return _plans[key]
+        _plans[key] = entry
         while len(_plans) > _MAX_PLANS:
             evict.append(_plans.popitem(last=False)[1])
-    for p in evict:
-        lib.gbn_destroy(p)
-    return plan
+    for p, plock in evict:
+        with plock:  # wait for a call in flight on it
+            lib.gbn_destroy(p)
+    return entry
 
 
 def to_native_from_key(nopts):
@@ -107,7 +114,7 @@ def forward(nufft_type, source, points, output_shape, iflag, eps, opts, out, sin
     stream = torch.cuda.current_stream(dev).cuda_stream
     key = plan_key(nufft_type, dim, single, nk_b, iflag, n_transf, eps_v, opts, dev, stream,
                    n_j)
-    plan = get_plan(key)
+    plan, plock = get_plan(key)
     src = source.contiguous()
     pts = [p.contiguous() for p in points][::-1]  # backend order
     esz = src.element_size()
@@ -115,6 +122,7 @@ def forward(nufft_type, source, points, output_shape, iflag, eps, opts, out, sin
     n_k_total = int(np.prod(nk))
     handles = []
     try:
+        plock.acquire()
         for idx in range(n_tot):
             h = ctypes.c_void_p()
             xs = [ctypes.c_void_p(p.data_ptr() + idx * n_j * psz) for p in pts] + [None] * (3 - dim)
@@ -133,13 +141,15 @@ def forward(nufft_type, source, points, output_shape, iflag, eps, opts, out, sin
         for h in handles:
             lib.gbn_points_destroy(h)
         raise
+    finally:
+        plock.release()
     return FusedState(key, handles)
 
 
 def backward(state, nufft_type, source, points, g, need_src, need_pts):
     """Fused gradients: (grad_source or None, [grad per point array or None])."""
     lib = _native.load()
-    plan = get_plan(state.key)
+    plan, plock = get_plan(state.key)
     dim = len(points)
     n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
     n_j = int(points[0].shape[1])
@@ -152,6 +162,14 @@ def backward(state, nufft_type, source, points, g, need_src, need_pts):
     psz = points[0].element_size()
     per_src = src[0].numel() * esz  # bytes per n_tot index of the source
     per_g = g[0].numel() * esz
+    with plock:
+        _backward_calls(lib, plan, state, n_tot, n_transf, n_j, dim, src, g, grad_src, grads,
+                        psz, per_src, per_g)
+    return grad_src, grads
+
+
+def _backward_calls(lib, plan, state, n_tot, n_transf, n_j, dim, src, g, grad_src, grads, psz,
+                    per_src, per_g):
     for idx in range(n_tot):
         gx = (ctypes.c_void_p * 3)()
         for u in range(dim):
@@ -163,4 +181,3 @@ def backward(state, nufft_type, source, points, g, need_src, need_pts):
                                    ctypes.c_void_p(src.data_ptr() + idx * per_src),
                                    ctypes.c_void_p(g.data_ptr() + idx * per_g),
                                    ctypes.c_void_p(gs) if gs else None, gx), "grad")
-    return grad_src, grads
