@@ -276,8 +276,9 @@ __global__ void deconv1_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2
   }
 }
 
-// One block per item = up to 512 cells of one fine-grid row (x line): the
-// row's y/z mode indices are resolved once, each thread writes two cells with
+// Items = up to 512 cells of one fine-grid row (x line), a contiguous range
+// of them per block: the row's y/z mode indices are resolved once per item
+// (rows advanced incrementally, no division), each thread writes two cells with
 // one 16-byte store per transform (zero outside the mode region, so the
 // padding needs no memset).  Rows outside the mode region are pure zero
 // stores.
@@ -290,10 +291,23 @@ __global__ void __launch_bounds__(256)
   const int nrows = nf1 * nf2;
   const int npair = nf0 >> 1;  // nf0 is even
   const int nchunk = (npair + blockDim.x - 1) / blockDim.x;  // blockDim.x pairs per item
-  for (int item = blockIdx.x; item < nrows * nchunk; item += gridDim.x) {
-    const int row = item / nchunk, chunk = item - row * nchunk;
-    const int g1 = DIM > 1 ? row % nf1 : 0;
-    const int g2 = DIM > 2 ? row / nf1 : 0;
+  // each block walks a contiguous range of items, decoding only the first
+  const int nitem = nrows * nchunk;
+  const int per = (nitem + gridDim.x - 1) / gridDim.x;
+  const int it0 = blockIdx.x * per, it1 = min(it0 + per, nitem);
+  if (it0 >= it1) return;
+  int row = it0 / nchunk, chunk = it0 - row * nchunk;
+  int g1 = DIM > 1 ? row % nf1 : 0;
+  int g2 = DIM > 2 ? row / nf1 : 0;
+  for (int item = it0; item < it1; ++item) {
+    if (item > it0 && ++chunk == nchunk) {
+      chunk = 0;
+      ++row;
+      if (++g1 == nf1) {
+        g1 = 0;
+        ++g2;
+      }
+    }
     const int i1 = DIM > 1 ? (int)fine_to_mode(g1, N1, nf1, modeord) : 0;
     const int i2 = DIM > 2 ? (int)fine_to_mode(g2, N2, nf2, modeord) : 0;
     const bool live = i1 >= 0 && i2 >= 0;
@@ -698,7 +712,7 @@ cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int mod
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned grid = (unsigned)std::min<int64_t>(items, (int64_t)nsm * 16);
+  const unsigned grid = (unsigned)std::min<int64_t>(items, (int64_t)nsm * 32);
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
   auto args = [&](auto kern) {
