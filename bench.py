@@ -520,18 +520,24 @@ def measure_plain2d(dev, steps, warmup, cpu=True):
     ch = rng.standard_normal(M) + 1j * rng.standard_normal(M)
     xt, yt = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
     ct = torch.from_numpy(ch).to(dev)
-    fn = lambda: jf.nufft1((N, N), ct, xt, yt, eps=1e-6, iflag=1)
-    for _ in range(warmup):
-        fn()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        out = fn()
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
+    from jax_finufft_gb300.options import Opts
+
+    def timed(opts):
+        fn = lambda: jf.nufft1((N, N), ct, xt, yt, eps=1e-6, iflag=1, opts=opts)
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, out
+
+    ms, out = timed(None)
+    ms3, out3 = timed(Opts(gpu_precision=3))
     kk = _freqs(N, xt)
     Ex = torch.exp(1j * torch.outer(kk, xt))
     Ey = torch.exp(1j * torch.outer(kk, yt))
@@ -539,7 +545,12 @@ def measure_plain2d(dev, steps, warmup, cpu=True):
     res = {"workload": "2D type-1, M=1e5 uniform points, complex128, 256^2 modes, eps=1e-6 "
                        "(nufft1, one transform per call)",
            "ms_per_call": ms, "pts_per_s": M / (ms * 1e-3),
-           "rel_l2_vs_fp64_direct": rel_err(out, truth)}
+           "rel_l2_vs_fp64_direct": rel_err(out, truth),
+           "precision_split": {
+               "opts": "gpu_precision=3 (FP32 kernel evaluation and accumulation for "
+                       "eps >= 1e-6; fold and bins FP64)",
+               "ms_per_call": ms3, "pts_per_s": M / (ms3 * 1e-3),
+               "rel_l2_vs_fp64_direct": rel_err(out3, truth)}}
     if cpu:
         from oracle import cpu_nufft
 
