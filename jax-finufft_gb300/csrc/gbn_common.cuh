@@ -96,6 +96,11 @@ struct FoldSpec {
   double scale[3];
   double nf_d[3];  // (double)nf per axis, filled by launch_fold
   double hw;       // w / 2, filled by launch_fold
+  // integer fast path of mode 0 (FP32 coordinates), filled by launch_fold:
+  // 1/(2 pi) in FP64 as kmant * 2^kexp, and ceil(log2 nf) per axis
+  unsigned long long kmant;
+  int kexp;
+  int lnf[3];
 };
 
 // Kernel evaluation: piecewise Horner coefficients coef[piece*(deg+1)+n]

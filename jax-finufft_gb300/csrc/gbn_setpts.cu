@@ -12,8 +12,10 @@
 #include <vector>
 
 #include <cstdint>
+#include <cstring>
 
 #include "gbn_common.cuh"
+#include "gbn_fold.cuh"
 
 namespace gbn {
 
@@ -57,7 +59,9 @@ __device__ __forceinline__ double grid_shift(TX xin, int mode, double center, do
 // touches is i0 = ceil(s); its offset is delta = i0 - s in [0, 1).  The bin is
 // (i0 + w/2) / bs per axis after wrapping i0 + w/2 into [0, nf), so every
 // point's support starts inside its bin's tile, which therefore needs only
-// bs + w - 1 cells per axis.
+// bs + w - 1 cells per axis.  FP32 coordinates with FP32 offsets take the
+// integer fast path of the periodic fold (fold_fast_f32, same results), and
+// the FP64 chain only for the points it declines.
 template <typename TX, typename TC, int DIM>
 __global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict__ x,
                             const TX* __restrict__ y, const TX* __restrict__ z,
@@ -74,12 +78,23 @@ __global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict
     const int h = g.w >> 1;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      const double sh = grid_shift(c[d][j], fs.mode, fs.center[d], fs.scale[d], fs.nf_d[d],
-                                   fs.hw);
-      const double cl = ceil(sh);
-      int i0 = (int)cl;
-      r.d[d] = (TC)__dsub_rn(cl, sh);
       const int nf = (int)g.nf[d];
+      int i0;
+      bool done = false;
+      if constexpr (sizeof(TX) == 4 && sizeof(TC) == 4) {
+        if (fs.mode == 0) {
+          float dl;
+          done = fold_fast_f32((float)c[d][j], nf, g.w, fs.lnf[d], fs.kmant, fs.kexp, i0, dl);
+          if (done) r.d[d] = (TC)dl;
+        }
+      }
+      if (!done) {
+        const double sh = grid_shift(c[d][j], fs.mode, fs.center[d], fs.scale[d], fs.nf_d[d],
+                                     fs.hw);
+        const double cl = ceil(sh);
+        i0 = (int)cl;
+        r.d[d] = (TC)__dsub_rn(cl, sh);
+      }
       int tb = i0 + h;
       if (tb < 0) {
         tb += nf;
@@ -593,6 +608,15 @@ cudaError_t launch_fold(const Geom& g, const FoldSpec& fs_in, int64_t M, const T
   FoldSpec fs = fs_in;
   for (int d = 0; d < 3; ++d) fs.nf_d[d] = (double)g.nf[d];
   fs.hw = 0.5 * (double)g.w;
+  uint64_t kb;
+  std::memcpy(&kb, &kInv2Pi, 8);
+  fs.kmant = (kb & ((1ull << 52) - 1)) | (1ull << 52);
+  fs.kexp = (int)((kb >> 52) & 0x7FF) - 1075;
+  for (int d = 0; d < 3; ++d) {
+    int l = 0;
+    while (l < 62 && ((int64_t)1 << l) < g.nf[d]) ++l;
+    fs.lnf[d] = l;
+  }
   const unsigned nb = grid1(M, kThreads);
   const int count = st.bin_count != nullptr;
   switch (g.dim) {

@@ -219,16 +219,35 @@ def _plan(native, ty, ndim, nmodes, single, opts, stream=None):
     return plan
 
 
+def _boundary_points(rng, nf, M, rdt):
+    """Coordinates on and next to fine-grid cells and half cells (where the
+    fold's ceiling and the FP32 rounding of the offset are closest to a
+    decision), their float neighbours, and special values (+-pi, 0, tiny,
+    large) -- the points the FP32 fold's integer fast path hands to the FP64
+    chain, mixed into warps with points it keeps."""
+    out = []
+    for n in nf:
+        j = rng.integers(-n, n, M).astype(np.float64)
+        off = rng.choice([0.0, 0.5], M)
+        tiny = (rng.random(M) - 0.5) * np.ldexp(1.0, -rng.integers(0, 45, M))
+        v = (2 * np.pi * (j + off + tiny) / n).astype(rdt)
+        k = M // 8
+        steps = rng.integers(-40, 41, k)
+        v[k:2 * k] = v[k:2 * k] + steps * np.spacing(v[k:2 * k])
+        v[:k] = rng.choice(np.array([np.pi, -np.pi, 0.0, 1e-30, -1e-30, 2 * np.pi, 1e4, -3e5]), k)
+        out.append(v.astype(rdt))
+    return out
+
+
 @pytest.mark.parametrize("ndim, single, kind", list(product([1, 2, 3], [True, False],
-                                                            ["uniform", "cluster", "wide"])))
+                                                            ["uniform", "cluster", "wide",
+                                                             "boundary"])))
 def test_fold_and_bins_bit_exact(native, cn, ndim, single, kind):
     from jax_finufft_gb300 import _native
 
     rng = np.random.default_rng(7 + ndim)
     M = 20000
     rdt = np.float32 if single else np.float64
-    x = [v.astype(rdt) for v in _points(rng, ndim, M, kind)]
-    x[0][:4] = np.array([np.pi, -np.pi, 0.0, 2 * np.pi], dtype=rdt)
     nmodes = {1: (1000,), 2: (200, 130), 3: (40, 50, 36)}[ndim]
     opts = _native.default_opts()
     bs = {1: (128, 1, 1), 2: (16, 32, 1), 3: (8, 16, 4)}[ndim]
@@ -236,14 +255,19 @@ def test_fold_and_bins_bit_exact(native, cn, ndim, single, kind):
     opts.gpu_method = 2
     plan = _plan(native, 1, ndim, nmodes, single, opts)
     try:
+        w = ctypes.c_int()
+        nf = (ctypes.c_int64 * 3)()
+        _native.check(native.gbn_plan_info(plan, ctypes.byref(w), nf, None, None))
+        if kind == "boundary":
+            x = _boundary_points(rng, [nf[d] for d in range(ndim)], M, rdt)
+        else:
+            x = [v.astype(rdt) for v in _points(rng, ndim, M, kind)]
+            x[0][:4] = np.array([np.pi, -np.pi, 0.0, 2 * np.pi], dtype=rdt)
         xt = [T(v) for v in x] + [None] * (3 - ndim)
         ptr = [ctypes.c_void_p(t.data_ptr()) if t is not None else None for t in xt]
         setpts = native.gbnf_setpts if single else native.gbn_setpts
         torch.cuda.synchronize()
         _native.check(setpts(plan, M, ptr[0], ptr[1], ptr[2], 0, None, None, None))
-        w = ctypes.c_int()
-        nf = (ctypes.c_int64 * 3)()
-        _native.check(native.gbn_plan_info(plan, ctypes.byref(w), nf, None, None))
         nbins = ctypes.c_int64()
         native.gbn_debug_bins(plan, None, None, ctypes.byref(nbins))
         bins = np.empty(M, dtype=np.int64)
