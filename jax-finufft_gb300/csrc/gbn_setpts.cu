@@ -62,20 +62,41 @@ __device__ __forceinline__ double grid_shift(TX xin, int mode, double center, do
 // bs + w - 1 cells per axis.  FP32 coordinates with FP32 offsets take the
 // integer fast path of the periodic fold (fold_fast_f32, same results), and
 // the FP64 chain only for the points it declines.
+// Bin counting is aggregated per block: the block's kFoldPts * kThreads
+// points enter their bins into a shared-memory hash table (one slot per
+// distinct bin, ranks from shared-memory atomics), and each slot then makes a
+// single global atomic for its count.  Clustered points otherwise send one
+// global atomic per warp to the same few bins, which serialise in L2.
+constexpr int kFoldPts = 4;        // points per thread
+constexpr int kFoldSlots = 2048;   // hash slots (twice the block's points)
+
 template <typename TX, typename TC, int DIM>
-__global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict__ x,
-                            const TX* __restrict__ y, const TX* __restrict__ z,
-                            int* __restrict__ pt_bin, int* __restrict__ pt_rank,
-                            int* __restrict__ bin_count, PtRec<TC, DIM>* __restrict__ recs_in,
-                            int count_bins) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = j < M;
-  int bin = 0;
-  if (valid) {
-    const TX* c[3] = {x, y, z};
+__global__ void __launch_bounds__(kThreads)
+    fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict__ x,
+                const TX* __restrict__ y, const TX* __restrict__ z, int* __restrict__ pt_bin,
+                int* __restrict__ pt_rank, int* __restrict__ bin_count,
+                PtRec<TC, DIM>* __restrict__ recs_in, int count_bins) {
+  static_assert(kFoldSlots >= 2 * kFoldPts * kThreads, "hash table at most half full");
+  __shared__ int s_key[kFoldSlots];
+  __shared__ int s_cnt[kFoldSlots];
+  if (count_bins) {
+    for (int i = threadIdx.x; i < kFoldSlots; i += kThreads) {
+      s_key[i] = -1;
+      s_cnt[i] = 0;
+    }
+    __syncthreads();
+  }
+  const int64_t j0 = (int64_t)blockIdx.x * (kFoldPts * kThreads) + threadIdx.x;
+  int slot[kFoldPts], lrank[kFoldPts], binv[kFoldPts];
+  const TX* c[3] = {x, y, z};
+  const int h = g.w >> 1;
+#pragma unroll
+  for (int k = 0; k < kFoldPts; ++k) {
+    const int64_t j = j0 + (int64_t)k * kThreads;
+    slot[k] = -1;
+    if (j >= M) continue;
     PtRec<TC, DIM> r;
-    int stride = 1;
-    const int h = g.w >> 1;
+    int bin = 0, stride = 1;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const int nf = (int)g.nf[d];
@@ -109,19 +130,43 @@ __global__ void fold_kernel(Geom g, FoldSpec fs, int64_t M, const TX* __restrict
       stride *= g.nb[d];
     }
     recs_in[j] = r;
+    binv[k] = bin;
+    if (count_bins) {
+      // linear probing; at most kFoldPts * kThreads distinct keys, so a free
+      // or matching slot turns up within kFoldSlots probes
+      unsigned hs = ((unsigned)bin * 2654435761u) >> 21;
+      int sl = -1;
+      for (int probe = 0; probe < kFoldSlots; ++probe) {
+        const int prev = atomicCAS(&s_key[hs], -1, bin);
+        if (prev == -1 || prev == bin) {
+          sl = (int)hs;
+          break;
+        }
+        hs = (hs + 1) & (kFoldSlots - 1);
+      }
+      if (sl >= 0) {
+        slot[k] = sl;
+        lrank[k] = atomicAdd(&s_cnt[sl], 1);
+      } else {  // not reached (the table cannot fill); a direct global rank
+        slot[k] = -2;
+        lrank[k] = atomicAdd(&bin_count[bin], 1);
+      }
+    }
   }
   if (!count_bins) return;
-  // Warp-aggregated bin counting: lanes that share a bin make one atomic.
-  const unsigned active = __ballot_sync(0xffffffffu, valid);
-  if (valid) {
-    const unsigned peers = __match_any_sync(active, bin);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&bin_count[bin], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    pt_bin[j] = bin;
-    pt_rank[j] = base + __popc(peers & ((1u << lane) - 1u));
+  __syncthreads();
+  // one global atomic per distinct bin of the block; s_cnt becomes its base
+  for (int i = threadIdx.x; i < kFoldSlots; i += kThreads) {
+    const int key = s_key[i];
+    if (key >= 0) s_cnt[i] = atomicAdd(&bin_count[key], s_cnt[i]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kFoldPts; ++k) {
+    const int64_t j = j0 + (int64_t)k * kThreads;
+    if (j >= M) continue;
+    pt_bin[j] = binv[k];
+    pt_rank[j] = slot[k] >= 0 ? s_cnt[slot[k]] + lrank[k] : lrank[k];
   }
 }
 
@@ -617,7 +662,7 @@ cudaError_t launch_fold(const Geom& g, const FoldSpec& fs_in, int64_t M, const T
     while (l < 62 && ((int64_t)1 << l) < g.nf[d]) ++l;
     fs.lnf[d] = l;
   }
-  const unsigned nb = grid1(M, kThreads);
+  const unsigned nb = grid1(M, kThreads * kFoldPts);
   const int count = st.bin_count != nullptr;
   switch (g.dim) {
     case 1:
