@@ -37,10 +37,15 @@ template <typename T>
 using cplx_t = typename Cplx<T>::type;
 
 // One nonuniform point after folding: offsets and grid starts per axis.
-// Aligned to 16 bytes when its natural size is a multiple of 16, else to 8,
-// so records move with 8/16-byte accesses instead of 4-byte ones.
+// Aligned to 16 bytes when its natural size is a multiple of 16, or when it
+// is 24 bytes (FP32 in 3D, padded to one 32-byte sector: the bin-order
+// scatter's random stores then write whole sectors with two 16-byte
+// accesses), else to 8, so records move with 8/16-byte accesses instead of
+// 4-byte ones.
 template <typename T, int DIM>
-struct alignas((sizeof(T) * DIM + 4 * DIM) % 16 == 0 ? 16 : 8) PtRec {
+struct alignas((sizeof(T) * DIM + 4 * DIM) % 16 == 0 || (sizeof(T) * DIM + 4 * DIM) == 24
+                   ? 16
+                   : 8) PtRec {
   T d[DIM];
   int i[DIM];
 };
