@@ -60,6 +60,7 @@ struct Geom {
   int64_t nbins;
   int maxsub;
   int stash;  // spread: a subproblem's strengths are staged in shared memory after the tile
+  int rows;   // sort keys per bin: > 1 orders a bin's points by tile row (y, z), 0/1 by bin
 };
 
 // Shared-memory tile of one bin: bs + w - 1 cells per axis from the bin's
@@ -120,7 +121,9 @@ struct KerSpec {
 
 // Device-side sort state produced by setpts.
 struct SortState {
-  int* pt_bin;     // [M] bin of each input point
+  int* pt_bin;     // [M] sort key of each input point: bin * rows + row in bin (rows > 1), or bin
+  int* key_count;  // [nbins * rows] points per key (the bin counts themselves when rows <= 1)
+  int* key_start;  // [nbins * rows] exclusive scan of key_count
   int* pt_rank;    // [M] rank inside its bin
   int* bin_count;  // [nbins]
   int* bin_start;  // [nbins] exclusive scan of bin_count

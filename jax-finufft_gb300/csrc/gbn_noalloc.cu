@@ -77,6 +77,7 @@ cudaError_t binsort(const Geom& g, int64_t M, const TX* x, const TX* y, const TX
   SortState st{};
   st.pt_bin = bins;
   st.bin_count = counts;
+  st.key_count = counts;  // plain bin order
   st.pt_rank = reinterpret_cast<int*>(scratch);
   st.recs_in = scratch + kRankBytes;
   int* bin_start = reinterpret_cast<int*>(scratch + kRankBytes + kRecBytes);

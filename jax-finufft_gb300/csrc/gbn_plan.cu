@@ -288,7 +288,8 @@ size_t rec_size(int dim, bool single) {
 // execute, so a gradient can reuse the forward's sort.
 struct gbn_points_s {
   DevBuf pt_bin, pt_rank, bin_count, bin_start, perm, sub_count, sub_start, sub_bin, sub_off,
-      n_sub, recs, recs_in, scan_tmp;
+      n_sub, recs, recs_in, scan_tmp, key_count, key_start;
+  int rows = 1;  // sort keys per bin of the last sort
   SortState st{};
   int64_t M = 0;
   bool set = false;
@@ -300,8 +301,9 @@ struct gbn_points_s {
   cudaStream_t stream = nullptr;
 
   void release() {
-    DevBuf* bufs[] = {&pt_bin,  &pt_rank, &bin_count, &bin_start, &perm,   &sub_count, &sub_start,
-                      &sub_bin, &sub_off, &n_sub,     &recs,      &recs_in, &scan_tmp};
+    DevBuf* bufs[] = {&pt_bin,  &pt_rank, &bin_count, &bin_start, &perm,    &sub_count,
+                      &sub_start, &sub_bin, &sub_off, &n_sub,   &recs,      &recs_in,
+                      &scan_tmp, &key_count, &key_start};
     for (DevBuf* b : bufs) b->release(stream);
   }
   ~gbn_points_s() { release(); }
@@ -437,6 +439,15 @@ void setup_geom(gbn_plan_s* p) {
     g.nbins *= g.nb[d];
   }
   g.maxsub = p->opts.gpu_maxsubprobsize > 0 ? p->opts.gpu_maxsubprobsize : 1024;
+  // type-2 plans order a bin's points by tile row, so that the points a warp
+  // gathers together read the same or neighbouring rows of the tile
+  // (GBN_DISABLE_ROW_ORDER=1: bin order only)
+  static const bool no_rows = std::getenv("GBN_DISABLE_ROW_ORDER") != nullptr;
+  g.rows = 1;
+  if (!no_rows && p->type == 2 && method == 2 && p->sorted && p->dim >= 2) {
+    const int64_t r = p->dim == 2 ? bs[1] : (int64_t)bs[1] * bs[2];
+    if (r > 1 && g.nbins * r < ((int64_t)1 << 30)) g.rows = (int)r;
+  }
   // stage each subproblem's strengths in shared memory when it still fits
   g.stash = method == 2 && spread_smem_bytes(p->dim, bs, p->w, p->comp_single, g.maxsub, true) <=
                                smem_limit;
@@ -683,6 +694,8 @@ void fill_sort_state(gbn_points_s& ps, bool sorted) {
   st.pt_rank = ps.pt_rank.as<int>();
   st.bin_count = sorted ? ps.bin_count.as<int>() : nullptr;
   st.bin_start = ps.bin_start.as<int>();
+  st.key_count = !sorted ? nullptr : ps.rows > 1 ? ps.key_count.as<int>() : st.bin_count;
+  st.key_start = ps.rows > 1 ? ps.key_start.as<int>() : st.bin_start;
   st.perm = sorted ? ps.perm.as<int>() : nullptr;
   st.sub_count = ps.sub_count.as<int>();
   st.sub_start = ps.sub_start.as<int>();
@@ -710,9 +723,15 @@ int sort_points(gbn_plan_s* p, gbn_points_s& ps, int64_t M, const TX* x, const T
   GBN_CUDA(ps.recs_in.ensure(m * rs, s));
   GBN_CUDA(ps.pt_bin.ensure(m * 4, s));
   GBN_CUDA(ps.pt_rank.ensure(m * 4, s));
+  ps.rows = g.rows > 1 ? g.rows : 1;
+  const int64_t nkeys = g.nbins * ps.rows;
   if (p->sorted) {
     const int64_t nb = g.nbins;
     ps.st.max_sub = nb + (M + g.maxsub - 1) / g.maxsub;
+    if (ps.rows > 1) {
+      GBN_CUDA(ps.key_count.ensure((size_t)nkeys * 4, s));
+      GBN_CUDA(ps.key_start.ensure((size_t)nkeys * 4, s));
+    }
     GBN_CUDA(ps.recs.ensure(m * rs, s));
     GBN_CUDA(ps.perm.ensure(m * 4, s));
     GBN_CUDA(ps.bin_count.ensure((size_t)nb * 4, s));
@@ -722,10 +741,10 @@ int sort_points(gbn_plan_s* p, gbn_points_s& ps, int64_t M, const TX* x, const T
     GBN_CUDA(ps.sub_bin.ensure((size_t)ps.st.max_sub * 4, s));
     GBN_CUDA(ps.sub_off.ensure((size_t)ps.st.max_sub * 4, s));
     GBN_CUDA(ps.n_sub.ensure(4, s));
-    GBN_CUDA(ps.scan_tmp.ensure((size_t)scan_tmp_ints(nb) * 4, s));
+    GBN_CUDA(ps.scan_tmp.ensure((size_t)scan_tmp_ints(nkeys) * 4, s));
   }
   fill_sort_state(ps, p->sorted);
-  if (p->sorted) GBN_CUDA(cudaMemsetAsync(ps.bin_count.p, 0, (size_t)g.nbins * 4, s));
+  if (p->sorted) GBN_CUDA(cudaMemsetAsync(ps.st.key_count, 0, (size_t)nkeys * 4, s));
   if (p->comp_single) {
     GBN_CUDA((launch_fold<TX, float>(g, fs, M, x, y, z, ps.st, s)));
     GBN_CUDA(launch_sort_finish<float>(g, M, ps.st, p->sorted, s));
@@ -1371,7 +1390,8 @@ int gbn_debug_bins(gbn_plan plan, int64_t* bins_out, int64_t* counts_out, int64_
   if (bins_out && plan->own.M > 0) {
     std::vector<int> b((size_t)plan->own.M);
     GBN_CUDA(cudaMemcpy(b.data(), plan->own.pt_bin.p, b.size() * 4, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < b.size(); ++i) bins_out[i] = b[i];
+    const int rows = plan->own.rows > 1 ? plan->own.rows : 1;  // sort key -> bin
+    for (size_t i = 0; i < b.size(); ++i) bins_out[i] = b[i] / rows;
   }
   if (counts_out) {
     std::vector<int> b((size_t)plan->geom.nbins);

@@ -59,7 +59,11 @@ __device__ __forceinline__ double grid_shift(TX xin, int mode, double center, do
 // touches is i0 = ceil(s); its offset is delta = i0 - s in [0, 1).  The bin is
 // (i0 + w/2) / bs per axis after wrapping i0 + w/2 into [0, nf), so every
 // point's support starts inside its bin's tile, which therefore needs only
-// bs + w - 1 cells per axis.  FP32 coordinates with FP32 offsets take the
+// bs + w - 1 cells per axis.  With g.rows > 1 the sort key is
+// bin * rows + (tile row of the point in its bin: y, or y + z * bs_y), so a
+// bin's points come out ordered by row: an interpolation warp then gathers
+// for points of the same or neighbouring rows, whose shared-memory reads
+// collide on fewer banks.  FP32 coordinates with FP32 offsets take the
 // integer fast path of the periodic fold (fold_fast_f32, same results), and
 // the FP64 chain only for the points it declines.
 // Bin counting is aggregated per block: the block's kFoldPts * kThreads
@@ -96,7 +100,7 @@ __global__ void __launch_bounds__(kThreads)
     slot[k] = -1;
     if (j >= M) continue;
     PtRec<TC, DIM> r;
-    int bin = 0, stride = 1;
+    int bin = 0, stride = 1, row = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const int nf = (int)g.nf[d];
@@ -126,9 +130,13 @@ __global__ void __launch_bounds__(kThreads)
         i0 -= nf;
       }
       r.i[d] = i0;
-      bin += (tb / g.bs[d]) * stride;
+      const int bd = tb / g.bs[d];
+      bin += bd * stride;
       stride *= g.nb[d];
+      if (d == 1) row += tb - bd * g.bs[1];
+      if (d == 2) row += (tb - bd * g.bs[2]) * g.bs[1];
     }
+    if (g.rows > 1) bin = bin * g.rows + row;  // bin order, then tile row within the bin
     recs_in[j] = r;
     binv[k] = bin;
     if (count_bins) {
@@ -251,6 +259,18 @@ __global__ void scatter_kernel(int64_t M, const int* __restrict__ pt_bin,
   const int pos = bin_start[pt_bin[j]] + pt_rank[j];
   perm[pos] = (int)j;
   recs[pos] = recs_in[j];
+}
+
+// Bin b holds keys [b*rows, (b+1)*rows): its range in the sorted order.
+__global__ void bin_ranges_kernel(int64_t nbins, int rows, int64_t M,
+                                  const int* __restrict__ key_start, int* __restrict__ bin_start,
+                                  int* __restrict__ bin_count) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  const int s0 = key_start[b * rows];
+  const int s1 = b + 1 < nbins ? key_start[(b + 1) * rows] : (int)M;
+  bin_start[b] = s0;
+  bin_count[b] = s1 - s0;
 }
 
 __global__ void subcount_kernel(int64_t nbins, const int* __restrict__ bin_count, int maxsub,
@@ -663,23 +683,23 @@ cudaError_t launch_fold(const Geom& g, const FoldSpec& fs_in, int64_t M, const T
     fs.lnf[d] = l;
   }
   const unsigned nb = grid1(M, kThreads * kFoldPts);
-  const int count = st.bin_count != nullptr;
+  const int count = st.key_count != nullptr;
   switch (g.dim) {
     case 1:
       fold_kernel<TX, TC, 1><<<nb, kThreads, 0, s>>>(g, fs, M, x, y, z, st.pt_bin, st.pt_rank,
-                                                     st.bin_count,
+                                                     st.key_count,
                                                      (PtRec<TC, 1>*)st.recs_in, count);
       note_launch();
       break;
     case 2:
       fold_kernel<TX, TC, 2><<<nb, kThreads, 0, s>>>(g, fs, M, x, y, z, st.pt_bin, st.pt_rank,
-                                                     st.bin_count,
+                                                     st.key_count,
                                                      (PtRec<TC, 2>*)st.recs_in, count);
       note_launch();
       break;
     default:
       fold_kernel<TX, TC, 3><<<nb, kThreads, 0, s>>>(g, fs, M, x, y, z, st.pt_bin, st.pt_rank,
-                                                     st.bin_count,
+                                                     st.key_count,
                                                      (PtRec<TC, 3>*)st.recs_in, count);
       note_launch();
       break;
@@ -707,32 +727,38 @@ template <typename TC>
 cudaError_t launch_sort_finish(const Geom& g, int64_t M, SortState& st, bool sorted,
                                cudaStream_t s) {
   if (!sorted) return cudaSuccess;
-  cudaError_t e = launch_scan(st.bin_count, st.bin_start, g.nbins, st.scan_tmp, s);
+  const int rows = g.rows > 1 ? g.rows : 1;
+  cudaError_t e = launch_scan(st.key_count, st.key_start, g.nbins * rows, st.scan_tmp, s);
   if (e != cudaSuccess) return e;
   if (M > 0) {
     const unsigned nb = grid1(M, kThreads);
     switch (g.dim) {
       case 1:
         scatter_kernel<PtRec<TC, 1>><<<nb, kThreads, 0, s>>>(
-            M, st.pt_bin, st.pt_rank, st.bin_start, (const PtRec<TC, 1>*)st.recs_in,
+            M, st.pt_bin, st.pt_rank, st.key_start, (const PtRec<TC, 1>*)st.recs_in,
             (PtRec<TC, 1>*)st.recs, st.perm);
         note_launch();
         break;
       case 2:
         scatter_kernel<PtRec<TC, 2>><<<nb, kThreads, 0, s>>>(
-            M, st.pt_bin, st.pt_rank, st.bin_start, (const PtRec<TC, 2>*)st.recs_in,
+            M, st.pt_bin, st.pt_rank, st.key_start, (const PtRec<TC, 2>*)st.recs_in,
             (PtRec<TC, 2>*)st.recs, st.perm);
         note_launch();
         break;
       default:
         scatter_kernel<PtRec<TC, 3>><<<nb, kThreads, 0, s>>>(
-            M, st.pt_bin, st.pt_rank, st.bin_start, (const PtRec<TC, 3>*)st.recs_in,
+            M, st.pt_bin, st.pt_rank, st.key_start, (const PtRec<TC, 3>*)st.recs_in,
             (PtRec<TC, 3>*)st.recs, st.perm);
         note_launch();
         break;
     }
   }
   const unsigned nbb = grid1(g.nbins, 256);
+  if (rows > 1) {  // per-bin ranges from the key scan
+    bin_ranges_kernel<<<nbb, 256, 0, s>>>(g.nbins, rows, M, st.key_start, st.bin_start,
+                                          st.bin_count);
+    note_launch();
+  }
   subcount_kernel<<<nbb, 256, 0, s>>>(g.nbins, st.bin_count, g.maxsub, st.sub_count);
   note_launch();
   e = launch_scan(st.sub_count, st.sub_start, g.nbins, st.scan_tmp, s);
