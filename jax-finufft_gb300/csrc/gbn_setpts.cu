@@ -294,14 +294,108 @@ __global__ void subfill_kernel(int64_t nbins, const int* __restrict__ sub_count,
 }
 
 // --- deconvolution -------------------------------------------------------------
-__device__ __forceinline__ int64_t mode_freq(int64_t i, int64_t N, int modeord) {
-  if (modeord == 0) return i - N / 2;
-  return i < (N + 1) / 2 ? i : i - N;
+// Mode index i -> fine index along one axis (modeord 0: CMCL order, k = i - N/2;
+// 1: FFT order).
+__device__ __forceinline__ int mode_to_fine(int i, int N, int nf, int modeord) {
+  const int k = modeord == 0 ? i - N / 2 : (i < (N + 1) / 2 ? i : i - N);
+  return k < 0 ? k + nf : k;
+}
+
+// Deconvolved copy of the fine grid's mode region into the modes (type 1).
+// Items are (output row, chunk of blockDim.x cell pairs of the row); each
+// block walks a contiguous range of items, advancing the row's y/z indices
+// incrementally, and each thread handles pair q = chunk * blockDim.x +
+// threadIdx.x of its items, re-deriving that pair's fine indices and factors
+// only when the chunk changes (never when a row is one chunk).  Pairs whose
+// two fine cells are adjacent and 16-byte aligned move with one 16-byte load
+// and, when vec_out, one 16-byte (FP32) store; indexing inside a transform is
+// 32-bit (a fine grid has < 2^31 cells).
+template <typename TC, typename TD, int DIM>
+__global__ void __launch_bounds__(256)
+    deconv1_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
+                   const TC* __restrict__ p0, const TC* __restrict__ p1,
+                   const TC* __restrict__ p2, const cplx_t<TC>* __restrict__ fine,
+                   cplx_t<TD>* __restrict__ out, int ntr, int64_t nftot, int64_t Ntot,
+                   int vec_out) {
+  const int nrows = N1 * N2;
+  const int npair = (N0 + 1) >> 1;
+  const int nchunk = (npair + blockDim.x - 1) / blockDim.x;
+  const int64_t nitem = (int64_t)nrows * nchunk;
+  const int64_t per = (nitem + gridDim.x - 1) / gridDim.x;
+  const int64_t it0 = blockIdx.x * per, it1 = min(it0 + per, nitem);
+  if (it0 >= it1) return;
+  int row = (int)(it0 / nchunk), chunk = (int)(it0 - (int64_t)row * nchunk);
+  int i1 = DIM > 1 ? row % N1 : 0;
+  int i2 = DIM > 2 ? row / N1 : 0;
+  int g2 = DIM > 2 ? mode_to_fine(i2, N2, nf2, modeord) : 0;
+  TC f2 = DIM > 2 ? p2[i2] : TC(1);
+  int q = -1, ga = 0, gb = 0;
+  TC fa = TC(0), fb = TC(0);
+  bool hasb = false, vin = false;
+  for (int64_t item = it0; item < it1; ++item) {
+    if (item > it0 && ++chunk == nchunk) {
+      chunk = 0;
+      ++row;
+      if (++i1 == N1) {
+        i1 = 0;
+        ++i2;
+        if (DIM > 2) {
+          g2 = mode_to_fine(i2, N2, nf2, modeord);
+          f2 = p2[i2];
+        }
+      }
+    }
+    const int qn = chunk * blockDim.x + threadIdx.x;
+    if (qn >= npair) continue;
+    if (qn != q) {  // this thread's pair changed: its x side of the map
+      q = qn;
+      const int ia = 2 * q, ib = ia + 1;
+      hasb = ib < N0;
+      ga = mode_to_fine(ia, N0, nf0, modeord);
+      gb = hasb ? mode_to_fine(ib, N0, nf0, modeord) : ga;
+      fa = p0[ia];
+      fb = hasb ? p0[ib] : TC(0);
+      vin = sizeof(TC) == 4 && hasb && gb == ga + 1 && (ga & 1) == 0;
+    }
+    const int g1 = DIM > 1 ? mode_to_fine(i1, N1, nf1, modeord) : 0;
+    const TC f12 = DIM > 1 ? f2 * p1[i1] : f2;
+    const TC ca = fa * f12, cb = fb * f12;
+    const cplx_t<TC>* src = fine + (g2 * nf1 + g1) * nf0;
+    cplx_t<TD>* dst = out + row * N0 + 2 * q;
+    for (int t = 0; t < ntr; ++t, src += nftot, dst += Ntot) {
+      cplx_t<TC> a, b;
+      if (vin) {
+        const float4 v = *reinterpret_cast<const float4*>(src + ga);
+        a.x = v.x;
+        a.y = v.y;
+        b.x = v.z;
+        b.y = v.w;
+      } else {
+        a = src[ga];
+        b = src[gb];
+      }
+      if constexpr (sizeof(TC) == 4 && sizeof(TD) == 4) {
+        if (vec_out && hasb) {
+          *reinterpret_cast<float4*>(dst) = make_float4(a.x * ca, a.y * ca, b.x * cb, b.y * cb);
+          continue;
+        }
+      }
+      cplx_t<TD> o;
+      o.x = (TD)(a.x * ca);
+      o.y = (TD)(a.y * ca);
+      dst[0] = o;
+      if (hasb) {
+        o.x = (TD)(b.x * cb);
+        o.y = (TD)(b.y * cb);
+        dst[1] = o;
+      }
+    }
+  }
 }
 
 // Fine index g -> output index along one axis, or -1 when g holds no mode.
-__device__ __forceinline__ int64_t fine_to_mode(int64_t g, int64_t N, int64_t nf, int modeord) {
-  int64_t k;
+__device__ __forceinline__ int fine_to_mode(int g, int N, int nf, int modeord) {
+  int k;
   if (g <= (N - 1) / 2)
     k = g;
   else if (g >= nf - N / 2)
@@ -312,56 +406,15 @@ __device__ __forceinline__ int64_t fine_to_mode(int64_t g, int64_t N, int64_t nf
   return k >= 0 ? k : k + N;
 }
 
-// Both deconvolution kernels index inside one transform with 32-bit
-// arithmetic (a fine grid has < 2^31 cells), take (x-block, y, z) from the
-// grid, and loop over the transforms inside the thread: no division and no
-// 64-bit multiply per element.
-template <typename TC, typename TD, int DIM>
-__global__ void deconv1_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
-                               const TC* __restrict__ p0, const TC* __restrict__ p1,
-                               const TC* __restrict__ p2, const cplx_t<TC>* __restrict__ fine,
-                               cplx_t<TD>* __restrict__ out, int ntr, int64_t nftot,
-                               int64_t Ntot) {
-  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i0 >= N0) return;
-  int k0 = (int)mode_freq(i0, N0, modeord);
-  const int g0 = k0 < 0 ? k0 + nf0 : k0;
-  const TC f0 = p0[i0];
-  for (int i2 = blockIdx.z; i2 < N2; i2 += gridDim.z) {
-    int g2 = 0;
-    TC f2 = f0;
-    if (DIM > 2) {
-      const int k2 = (int)mode_freq(i2, N2, modeord);
-      g2 = k2 < 0 ? k2 + nf2 : k2;
-      f2 *= p2[i2];
-    }
-    for (int i1 = blockIdx.y; i1 < N1; i1 += gridDim.y) {
-      int g1 = 0;
-      TC f = f2;
-      if (DIM > 1) {
-        const int k1 = (int)mode_freq(i1, N1, modeord);
-        g1 = k1 < 0 ? k1 + nf1 : k1;
-        f *= p1[i1];
-      }
-      const int src = (g2 * nf1 + g1) * nf0 + g0;
-      const int dst = (i2 * N1 + i1) * N0 + i0;
-      for (int t = 0; t < ntr; ++t) {
-        const cplx_t<TC> v = fine[t * nftot + src];
-        cplx_t<TD> o;
-        o.x = (TD)(v.x * f);
-        o.y = (TD)(v.y * f);
-        out[t * Ntot + dst] = o;
-      }
-    }
-  }
-}
-
-// Items = up to 512 cells of one fine-grid row (x line), a contiguous range
-// of them per block: the row's y/z mode indices are resolved once per item
-// (rows advanced incrementally, no division), each thread writes two cells with
-// one 16-byte store per transform (zero outside the mode region, so the
-// padding needs no memset).  Rows outside the mode region are pure zero
-// stores.
+// Zero-padded, deconvolved copy of the modes into the fine grid (type 2).
+// Items are (fine-grid row, chunk of blockDim.x cell pairs of the row); each
+// block walks a contiguous range of items, advancing the row's y/z indices
+// incrementally, and each thread writes pair q = chunk * blockDim.x +
+// threadIdx.x of its items with one 16-byte store per transform (zeros
+// outside the mode region, so the padding needs no memset).  The pair's mode
+// indices and factors are re-derived only when the chunk changes (never
+// when a row is one chunk), so a row costs a few instructions per store and
+// the kernel runs at the HBM write rate.
 template <typename TC, typename TD, int DIM>
 __global__ void __launch_bounds__(256)
     deconv2_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
@@ -370,65 +423,65 @@ __global__ void __launch_bounds__(256)
                    cplx_t<TC>* __restrict__ fine, int ntr, int64_t nftot, int64_t Ntot) {
   const int nrows = nf1 * nf2;
   const int npair = nf0 >> 1;  // nf0 is even
-  const int nchunk = (npair + blockDim.x - 1) / blockDim.x;  // blockDim.x pairs per item
-  // each block walks a contiguous range of items, decoding only the first
-  const int nitem = nrows * nchunk;
-  const int per = (nitem + gridDim.x - 1) / gridDim.x;
-  const int it0 = blockIdx.x * per, it1 = min(it0 + per, nitem);
+  const int nchunk = (npair + blockDim.x - 1) / blockDim.x;
+  const int64_t nitem = (int64_t)nrows * nchunk;
+  const int64_t per = (nitem + gridDim.x - 1) / gridDim.x;
+  const int64_t it0 = blockIdx.x * per, it1 = min(it0 + per, nitem);
   if (it0 >= it1) return;
-  int row = it0 / nchunk, chunk = it0 - row * nchunk;
+  int row = (int)(it0 / nchunk), chunk = (int)(it0 - (int64_t)row * nchunk);
   int g1 = DIM > 1 ? row % nf1 : 0;
   int g2 = DIM > 2 ? row / nf1 : 0;
-  for (int item = it0; item < it1; ++item) {
+  int i2 = DIM > 2 ? fine_to_mode(g2, N2, nf2, modeord) : 0;
+  TC f2 = DIM > 2 && i2 >= 0 ? p2[i2] : TC(1);
+  int q = -1, ia = -1, ib = -1;
+  TC fa = TC(0), fb = TC(0);
+  for (int64_t item = it0; item < it1; ++item) {
     if (item > it0 && ++chunk == nchunk) {
       chunk = 0;
       ++row;
       if (++g1 == nf1) {
         g1 = 0;
         ++g2;
+        if (DIM > 2) {
+          i2 = fine_to_mode(g2, N2, nf2, modeord);
+          f2 = i2 >= 0 ? p2[i2] : TC(1);
+        }
       }
     }
-    const int i1 = DIM > 1 ? (int)fine_to_mode(g1, N1, nf1, modeord) : 0;
-    const int i2 = DIM > 2 ? (int)fine_to_mode(g2, N2, nf2, modeord) : 0;
+    const int qn = chunk * blockDim.x + threadIdx.x;
+    if (qn >= npair) continue;
+    if (qn != q) {  // this thread's pair changed: its x side of the map
+      q = qn;
+      ia = fine_to_mode(2 * q, N0, nf0, modeord);
+      ib = fine_to_mode(2 * q + 1, N0, nf0, modeord);
+      fa = ia >= 0 ? p0[ia] : TC(0);
+      fb = ib >= 0 ? p0[ib] : TC(0);
+    }
+    const int i1 = DIM > 1 ? fine_to_mode(g1, N1, nf1, modeord) : 0;
     const bool live = i1 >= 0 && i2 >= 0;
-    TC f12 = TC(1);
-    if (live) {
-      if (DIM > 1) f12 *= p1[i1];
-      if (DIM > 2) f12 *= p2[i2];
-    }
-    const int64_t dst_row = (int64_t)row * nf0;
-    const int64_t src_row = live ? ((int64_t)i2 * N1 + i1) * N0 : 0;
-    const int q = chunk * blockDim.x + threadIdx.x;
-    if (q < npair) {
-      const int g0 = 2 * q;
-      int ia = -1, ib = -1;
-      TC fa = TC(0), fb = TC(0);
-      if (live) {
-        ia = (int)fine_to_mode(g0, N0, nf0, modeord);
-        ib = (int)fine_to_mode(g0 + 1, N0, nf0, modeord);
-        if (ia >= 0) fa = p0[ia] * f12;
-        if (ib >= 0) fb = p0[ib] * f12;
+    const TC f12 = live ? (DIM > 1 ? f2 * p1[i1] : f2) : TC(0);
+    const int ja = live ? ia : -1, jb = live ? ib : -1;
+    const TC ca = fa * f12, cb = fb * f12;
+    const cplx_t<TD>* src = in + (live ? (i2 * N1 + i1) * N0 : 0);
+    cplx_t<TC>* d = fine + row * nf0 + 2 * q;  // even cell: 16-byte aligned pair
+    for (int t = 0; t < ntr; ++t, src += Ntot, d += nftot) {
+      cplx_t<TC> a, b;
+      a.x = a.y = b.x = b.y = TC(0);
+      if (ja >= 0) {
+        const cplx_t<TD> v = src[ja];
+        a.x = (TC)v.x * ca;
+        a.y = (TC)v.y * ca;
       }
-      for (int t = 0; t < ntr; ++t) {
-        cplx_t<TC> a, b;
-        a.x = a.y = b.x = b.y = TC(0);
-        if (ia >= 0) {
-          const cplx_t<TD> v = in[t * Ntot + src_row + ia];
-          a.x = (TC)v.x * fa;
-          a.y = (TC)v.y * fa;
-        }
-        if (ib >= 0) {
-          const cplx_t<TD> v = in[t * Ntot + src_row + ib];
-          b.x = (TC)v.x * fb;
-          b.y = (TC)v.y * fb;
-        }
-        cplx_t<TC>* d = fine + t * nftot + dst_row + g0;  // even cell: 16-byte aligned pair
-        if constexpr (sizeof(TC) == 4) {
-          *reinterpret_cast<float4*>(d) = make_float4(a.x, a.y, b.x, b.y);
-        } else {
-          d[0] = a;
-          d[1] = b;
-        }
+      if (jb >= 0) {
+        const cplx_t<TD> v = src[jb];
+        b.x = (TC)v.x * cb;
+        b.y = (TC)v.y * cb;
+      }
+      if constexpr (sizeof(TC) == 4) {
+        *reinterpret_cast<float4*>(d) = make_float4(a.x, a.y, b.x, b.y);
+      } else {
+        d[0] = a;
+        d[1] = b;
       }
     }
   }
@@ -774,14 +827,23 @@ cudaError_t launch_deconv1(int dim, const int64_t* N, const int64_t* nf, int mod
                            const TC* const* phi, const void* fine, void* out, int ntr,
                            cudaStream_t s) {
   const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
-  dim3 grid(grid1(N[0], 128), (unsigned)(N[1] < 65535 ? N[1] : 65535),
-            (unsigned)(N[2] < 65535 ? N[2] : 65535));
+  // threads per block: the row's pairs, rounded up to whole warps (<= 256)
+  const int64_t npair = (N[0] + 1) / 2;
+  const int threads = (int)std::min<int64_t>(256, (npair + 31) / 32 * 32);
+  const int64_t items = N[1] * N[2] * ((npair + threads - 1) / threads);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)std::min<int64_t>(items, (int64_t)nsm * 32);
+  // 16-byte stores need an even row length and a 16-byte aligned output
+  const int vec_out = N[0] % 2 == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
+                      (Ntot % 2 == 0 || ntr == 1);
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
   auto args = [&](auto kern) {
-    kern<<<grid, 128, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
-                              (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TC>*)fine,
-                              (cplx_t<TD>*)out, ntr, nftot, Ntot);
+    kern<<<grid, threads, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
+                                  (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TC>*)fine,
+                                  (cplx_t<TD>*)out, ntr, nftot, Ntot, vec_out);
   };
   switch (dim) {
     case 1:
@@ -803,7 +865,9 @@ cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int mod
                            const TC* const* phi, const void* in, void* fine, int ntr,
                            cudaStream_t s) {
   const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
-  const int64_t items = nf[1] * nf[2] * ((nf[0] / 2 + 255) / 256);
+  const int64_t npair = nf[0] / 2;
+  const int threads = (int)std::min<int64_t>(256, (npair + 31) / 32 * 32);
+  const int64_t items = nf[1] * nf[2] * ((npair + threads - 1) / threads);
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -811,9 +875,9 @@ cudaError_t launch_deconv2(int dim, const int64_t* N, const int64_t* nf, int mod
   const TC* p1 = dim > 1 ? phi[1] : nullptr;
   const TC* p2 = dim > 2 ? phi[2] : nullptr;
   auto args = [&](auto kern) {
-    kern<<<grid, 256, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
-                              (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TD>*)in,
-                              (cplx_t<TC>*)fine, ntr, nftot, Ntot);
+    kern<<<grid, threads, 0, s>>>((int)N[0], (int)N[1], (int)N[2], (int)nf[0], (int)nf[1],
+                                  (int)nf[2], modeord, phi[0], p1, p2, (const cplx_t<TD>*)in,
+                                  (cplx_t<TC>*)fine, ntr, nftot, Ntot);
   };
   switch (dim) {
     case 1:
