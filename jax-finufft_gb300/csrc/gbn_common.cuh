@@ -107,6 +107,7 @@ struct FoldSpec {
   unsigned long long kmant;
   int kexp;
   int lnf[3];
+  unsigned bs_mul[3];  // floor(2^32 / bs) per axis (bin index by multiply-high)
 };
 
 // Kernel evaluation: piecewise Horner coefficients coef[piece*(deg+1)+n]

@@ -94,6 +94,14 @@ __global__ void __launch_bounds__(kThreads)
   int slot[kFoldPts], lrank[kFoldPts], binv[kFoldPts];
   const TX* c[3] = {x, y, z};
   const int h = g.w >> 1;
+  // all the thread's coordinates in flight at once
+  TX cv[kFoldPts][DIM];
+#pragma unroll
+  for (int k = 0; k < kFoldPts; ++k) {
+    const int64_t j = j0 + (int64_t)k * kThreads;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) cv[k][d] = j < M ? c[d][j] : TX(0);
+  }
 #pragma unroll
   for (int k = 0; k < kFoldPts; ++k) {
     const int64_t j = j0 + (int64_t)k * kThreads;
@@ -109,12 +117,12 @@ __global__ void __launch_bounds__(kThreads)
       if constexpr (sizeof(TX) == 4 && sizeof(TC) == 4) {
         if (fs.mode == 0) {
           float dl;
-          done = fold_fast_f32((float)c[d][j], nf, g.w, fs.lnf[d], fs.kmant, fs.kexp, i0, dl);
+          done = fold_fast_f32((float)cv[k][d], nf, g.w, fs.lnf[d], fs.kmant, fs.kexp, i0, dl);
           if (done) r.d[d] = (TC)dl;
         }
       }
       if (!done) {
-        const double sh = grid_shift(c[d][j], fs.mode, fs.center[d], fs.scale[d], fs.nf_d[d],
+        const double sh = grid_shift(cv[k][d], fs.mode, fs.center[d], fs.scale[d], fs.nf_d[d],
                                      fs.hw);
         const double cl = ceil(sh);
         i0 = (int)cl;
@@ -130,7 +138,12 @@ __global__ void __launch_bounds__(kThreads)
         i0 -= nf;
       }
       r.i[d] = i0;
-      const int bd = tb / g.bs[d];
+      // tb / bs by multiply-high with floor(2^32 / bs): one correction step
+      int bd = tb;
+      if (g.bs[d] > 1) {
+        bd = (int)__umulhi((unsigned)tb, fs.bs_mul[d]);
+        if (tb - bd * g.bs[d] >= g.bs[d]) ++bd;
+      }
       bin += bd * stride;
       stride *= g.nb[d];
       if (d == 1) row += tb - bd * g.bs[1];
@@ -734,6 +747,7 @@ cudaError_t launch_fold(const Geom& g, const FoldSpec& fs_in, int64_t M, const T
     int l = 0;
     while (l < 62 && ((int64_t)1 << l) < g.nf[d]) ++l;
     fs.lnf[d] = l;
+    fs.bs_mul[d] = g.bs[d] > 1 ? (unsigned)((1ull << 32) / (unsigned)g.bs[d]) : 0u;
   }
   const unsigned nb = grid1(M, kThreads * kFoldPts);
   const int count = st.key_count != nullptr;
