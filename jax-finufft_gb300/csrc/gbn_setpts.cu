@@ -262,16 +262,38 @@ __global__ void scan_add_kernel(int* out, int64_t n, const int* sums) {
 }
 
 // --- bin-order scatter and subproblems ---------------------------------------
+// kScatterPts points per thread, each stage's loads issued for all of them
+// before the next stage needs them (the bin start depends on the bin).
+constexpr int kScatterPts = 4;
+
 template <typename REC>
-__global__ void scatter_kernel(int64_t M, const int* __restrict__ pt_bin,
-                               const int* __restrict__ pt_rank, const int* __restrict__ bin_start,
-                               const REC* __restrict__ recs_in, REC* __restrict__ recs,
-                               int* __restrict__ perm) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= M) return;
-  const int pos = bin_start[pt_bin[j]] + pt_rank[j];
-  perm[pos] = (int)j;
-  recs[pos] = recs_in[j];
+__global__ void __launch_bounds__(kThreads)
+    scatter_kernel(int64_t M, const int* __restrict__ pt_bin, const int* __restrict__ pt_rank,
+                   const int* __restrict__ bin_start, const REC* __restrict__ recs_in,
+                   REC* __restrict__ recs, int* __restrict__ perm) {
+  const int64_t j0 = (int64_t)blockIdx.x * (kScatterPts * kThreads) + threadIdx.x;
+  int b[kScatterPts], rk[kScatterPts], pos[kScatterPts];
+  REC rv[kScatterPts];
+#pragma unroll
+  for (int k = 0; k < kScatterPts; ++k) {
+    const int64_t j = j0 + (int64_t)k * kThreads;
+    if (j < M) {
+      b[k] = pt_bin[j];
+      rk[k] = pt_rank[j];
+      rv[k] = recs_in[j];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kScatterPts; ++k)
+    if (j0 + (int64_t)k * kThreads < M) pos[k] = bin_start[b[k]] + rk[k];
+#pragma unroll
+  for (int k = 0; k < kScatterPts; ++k) {
+    const int64_t j = j0 + (int64_t)k * kThreads;
+    if (j < M) {
+      perm[pos[k]] = (int)j;
+      recs[pos[k]] = rv[k];
+    }
+  }
 }
 
 // Bin b holds keys [b*rows, (b+1)*rows): its range in the sorted order.
@@ -798,7 +820,7 @@ cudaError_t launch_sort_finish(const Geom& g, int64_t M, SortState& st, bool sor
   cudaError_t e = launch_scan(st.key_count, st.key_start, g.nbins * rows, st.scan_tmp, s);
   if (e != cudaSuccess) return e;
   if (M > 0) {
-    const unsigned nb = grid1(M, kThreads);
+    const unsigned nb = grid1(M, kThreads * kScatterPts);
     switch (g.dim) {
       case 1:
         scatter_kernel<PtRec<TC, 1>><<<nb, kThreads, 0, s>>>(
