@@ -346,7 +346,7 @@ __device__ __forceinline__ int mode_to_fine(int i, int N, int nf, int modeord) {
 // and, when vec_out, one 16-byte (FP32) store; indexing inside a transform is
 // 32-bit (a fine grid has < 2^31 cells).
 template <typename TC, typename TD, int DIM>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(TC) == 4 && sizeof(TD) == 4 ? 6 : 1)
     deconv1_kernel(int N0, int N1, int N2, int nf0, int nf1, int nf2, int modeord,
                    const TC* __restrict__ p0, const TC* __restrict__ p1,
                    const TC* __restrict__ p2, const cplx_t<TC>* __restrict__ fine,
