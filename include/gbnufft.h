@@ -312,8 +312,9 @@ GBN_API int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x
  * Bin-sort nonuniform points without allocating any memory.  No counterpart
  * in the reference: it serves callers that cannot call cudaMalloc (plugins
  * whose host framework owns all device memory, pipelines that reserve every
- * byte up front, hooks that must not allocate).  It runs the FP64 fold and
- * bin sort of setpts on caller-provided points (float32 when single = 1,
+ * byte up front, hooks that must not allocate).  It runs the fold (with
+ * the FP64 chain's results) and bin sort of setpts on caller-provided
+ * points (float32 when single = 1,
  * else float64; device pointers, backend order) for a fine grid of nf[d]
  * cells in bins of binsize[d] cells per axis and kernel width w (2..16; a
  * point belongs to the bin holding the first cell of its w-wide support, as
