@@ -24,8 +24,8 @@ BUILD_DIR = os.path.join(OUT_DIR, "obj")
 LIB_NAME = "libgbnufft.so"
 
 SOURCES = ["gbn_setpts.cu", "gbn_spread.cu", "gbn_interp.cu", "gbn_grad.cu", "gbn_plan.cu",
-           "gbn_tune.cu", "gbn_probe.cu", "gbn_noalloc.cu"]
-HEADERS = ["gbn_common.cuh", "gbn_device.cuh"]
+           "gbn_fft.cu", "gbn_tune.cu", "gbn_probe.cu", "gbn_noalloc.cu"]
+HEADERS = ["gbn_common.cuh", "gbn_device.cuh", "gbn_fold.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-fvisibility=hidden", "-I", INCLUDE,

@@ -17,6 +17,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 namespace gbn {
 
@@ -211,6 +212,22 @@ template <typename TC, typename TD>
 cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
                           const SortState& st, const void* fine, void* c, int ntr,
                           cudaStream_t s, const CUtensorMap* tmap = nullptr);
+
+// The library's pruned FP32 FFT for power-of-two fine grids (gbn_fft.cu):
+// applicability, the twiddle table exp(2 pi i m / n) (n cos/sin pairs), and
+// the two directions with the deconvolution fused -- type 2 reads the modes
+// (TD) and leaves the transformed fine grid; type 1 reads the fine grid and
+// writes the modes.  phi: 1/psihat per axis; tw: twiddles per axis.
+bool fft_pow2_supported(int dim, const int64_t* nf, int nb);
+void fft_pow2_twiddles(int64_t n, std::vector<float>& out);
+template <typename TD>
+cudaError_t launch_fft_type2(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                             const float* const* phi, const float2* const* tw,
+                             const void* modes, void* fine, int nb, int sign, cudaStream_t s);
+template <typename TD>
+cudaError_t launch_fft_type1(int dim, const int64_t* N, const int64_t* nf, int modeord,
+                             const float* const* phi, const float2* const* tw, void* fine,
+                             void* modes, int nb, int sign, cudaStream_t s);
 
 // Type-1 deconvolution + mode reorder: fine (ntr, nf) -> out (ntr, N).
 // phi[d] holds 1/psihat for each output index along axis d.

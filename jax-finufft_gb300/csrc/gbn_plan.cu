@@ -336,6 +336,10 @@ struct gbn_plan_s {
   int64_t prune_lo = 0, prune_hi = 0;
   int prune_state = 0;  // 0 not tried, 1 ready, -1 not applicable
   DevBuf fft_work;
+  // FP32 power-of-two grids: the library's own pruned FFT with the
+  // deconvolution fused (gbn_fft.cu), twiddles exp(2 pi i m / nf) per axis
+  bool fft_own = false;
+  DevBuf fft_tw[3];
 
   // type 3
   std::unique_ptr<gbn_plan_s> inner;
@@ -352,9 +356,9 @@ struct gbn_plan_s {
 
   ~gbn_plan_s() {
     cudaStreamSynchronize(stream);
-    DevBuf* bufs[] = {&coef,      &phi[0],    &phi[1],    &phi[2], &fine,    &gfine,
-                      &t3_tau[0], &t3_tau[1], &t3_tau[2], &t3_pre, &t3_post, &t3_cbuf,
-                      &t3_obuf,   &t3_minmax};
+    DevBuf* bufs[] = {&coef,      &phi[0],    &phi[1],    &phi[2],    &fine,      &gfine,
+                      &t3_tau[0], &t3_tau[1], &t3_tau[2], &t3_pre,    &t3_post,   &t3_cbuf,
+                      &t3_obuf,   &t3_minmax, &fft_tw[0], &fft_tw[1], &fft_tw[2]};
     for (DevBuf* b : bufs) b->release(stream);
     own.stream = stream;
     own.release();
@@ -478,6 +482,21 @@ int setup_phi(gbn_plan_s* p) {
     kernel_ft(p->w, p->beta, om, ph);
     for (auto& v : ph) v = 1.0 / v;
     GBN_TRY(upload_doubles_as(ph, p->comp_single, p->phi[d], p->stream));
+  }
+  return GBN_OK;
+}
+
+// The library's own FFT applies to FP32 type-1/2 plans whose fine-grid axes
+// all have 128, 256, 512 or 1024 cells; GBN_DISABLE_OWN_FFT=1 at execute
+// time selects cuFFT and the separate deconvolution instead.
+int setup_fft_own(gbn_plan_s* p) {
+  p->fft_own = p->comp_single && p->type != 3 && fft_pow2_supported(p->dim, p->nf, p->batch);
+  if (!p->fft_own) return GBN_OK;
+  for (int d = 0; d < p->dim; ++d) {
+    std::vector<float> tw;
+    fft_pow2_twiddles(p->nf[d], tw);
+    std::vector<double> twd(tw.begin(), tw.end());
+    GBN_TRY(upload_doubles_as(twd, true, p->fft_tw[d], p->stream));
   }
   return GBN_OK;
 }
@@ -658,6 +677,7 @@ int plan_create(int type, int dim, const int64_t* nmodes, int iflag, int ntransf
     if (p->nftot > (int64_t)INT32_MAX) return fail(GBN_ERR_ARGS, "fine grid too large (> 2^31 cells)");
     setup_geom(p.get());
     GBN_TRY(setup_phi(p.get()));
+    GBN_TRY(setup_fft_own(p.get()));
   }
   GBN_TRY(setup_kernel_coef(p.get()));
   // transforms per batch: bounded so the fine grids stay within 8 GiB
@@ -976,6 +996,27 @@ int do_deconv(gbn_plan_s* p, void* modes, int nb, bool to_modes, void* grid) {
   return GBN_OK;
 }
 
+// The library's pruned FFT between the fine grids and the modes (to_modes:
+// type-1 direction, grid -> modes; else modes -> grid), deconvolution fused.
+int own_fft(gbn_plan_s* p, void* grid, void* modes, int nb, int sign, bool to_modes) {
+  const float* phi[3] = {p->phi[0].as<float>(), p->phi[1].as<float>(), p->phi[2].as<float>()};
+  const float2* tw[3] = {p->fft_tw[0].as<float2>(), p->fft_tw[1].as<float2>(),
+                         p->fft_tw[2].as<float2>()};
+  cudaError_t e;
+  if (to_modes)
+    e = p->data_single ? launch_fft_type1<float>(p->dim, p->N, p->nf, p->opts.modeord, phi, tw,
+                                                 grid, modes, nb, sign, p->stream)
+                       : launch_fft_type1<double>(p->dim, p->N, p->nf, p->opts.modeord, phi, tw,
+                                                  grid, modes, nb, sign, p->stream);
+  else
+    e = p->data_single ? launch_fft_type2<float>(p->dim, p->N, p->nf, p->opts.modeord, phi, tw,
+                                                 modes, grid, nb, sign, p->stream)
+                       : launch_fft_type2<double>(p->dim, p->N, p->nf, p->opts.modeord, phi, tw,
+                                                  modes, grid, nb, sign, p->stream);
+  GBN_CUDA(e);
+  return GBN_OK;
+}
+
 void ev_record(cudaEvent_t* ev, int i, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[i], s);
 }
@@ -993,6 +1034,8 @@ int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int 
   const size_t dsz = cplx_size(p->data_single);
   const size_t csz = cplx_size(p->comp_single);
   const int op = dir > 0 ? p->type : (p->type == 1 ? 2 : 1);
+  const char* no_own = std::getenv("GBN_DISABLE_OWN_FFT");
+  const bool own = p->fft_own && !(no_own && no_own[0] == '1');
   const int sign = dir > 0 ? p->iflag : -p->iflag;
   GBN_CUDA(p->fine.ensure((size_t)p->batch * p->nftot * csz, s));
   for (int t0 = 0; t0 < ntr; t0 += p->batch) {
@@ -1005,17 +1048,27 @@ int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int 
       GBN_CUDA(cudaMemsetAsync(p->fine.p, 0, (size_t)nb * p->nftot * csz, s));
       GBN_TRY(do_spread(p, ps, cb, nb, false, p->fine.p));
       ev_record(ev, 1, s);
-      GBN_TRY(exec_fft(p, p->fine.p, nb, sign, 2));
-      ev_record(ev, 2, s);
-      GBN_TRY(do_deconv(p, fb, nb, true, p->fine.p));
+      if (own) {  // pruned FFT with the deconvolution fused (deconv stage empty)
+        GBN_TRY(own_fft(p, p->fine.p, fb, nb, sign, true));
+        ev_record(ev, 2, s);
+      } else {
+        GBN_TRY(exec_fft(p, p->fine.p, nb, sign, 2));
+        ev_record(ev, 2, s);
+        GBN_TRY(do_deconv(p, fb, nb, true, p->fine.p));
+      }
       ev_record(ev, 3, s);
     } else if (op == 2) {
       char* cb = (char*)c + (size_t)t0 * ps.M * dsz;
       const char* fb = (const char*)f + (size_t)t0 * p->Ntot * dsz;
       ev_record(ev, 0, s);
-      GBN_TRY(do_deconv(p, (void*)fb, nb, false, p->fine.p));
-      ev_record(ev, 1, s);
-      GBN_TRY(exec_fft(p, p->fine.p, nb, sign, 1));
+      if (own) {  // pruned FFT with the deconvolution fused (deconv stage empty)
+        ev_record(ev, 1, s);
+        GBN_TRY(own_fft(p, p->fine.p, (void*)fb, nb, sign, false));
+      } else {
+        GBN_TRY(do_deconv(p, (void*)fb, nb, false, p->fine.p));
+        ev_record(ev, 1, s);
+        GBN_TRY(exec_fft(p, p->fine.p, nb, sign, 1));
+      }
       ev_record(ev, 2, s);
       GBN_TRY(do_interp(p, ps, cb, nb, p->fine.p));
       ev_record(ev, 3, s);
