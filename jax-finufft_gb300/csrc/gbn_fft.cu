@@ -93,8 +93,9 @@ __device__ __forceinline__ void dft(float2* a) {
     dft2<SIGN>(a);
 }
 
-// Radix of pass p for length N (8 threads' worth of elements per thread:
-// N/8 threads per line).
+// Radix of pass p for a line of N cells; every thread holds 8 elements, so
+// a line takes N/8 threads (one radix-8 butterfly, two radix-4 or four
+// radix-2 butterflies per thread and pass).
 __host__ __device__ constexpr int fft_radix(int N, int p) {
   return N == 128 ? (p < 2 ? 8 : 2) : N == 256 ? (p < 2 ? 8 : 4) : N == 1024 ? (p < 3 ? 8 : 2) : 8;
 }
