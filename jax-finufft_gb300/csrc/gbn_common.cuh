@@ -219,11 +219,20 @@ cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int6
 // (TD) and leaves the transformed fine grid; type 1 reads the fine grid and
 // writes the modes.  phi: 1/psihat per axis; tw: twiddles per axis.
 bool fft_pow2_supported(int dim, const int64_t* nf, int nb);
+// Weighted grids of the fused gradient for launch_fft_type2: E grids per
+// transform, grid e the deconvolved modes times 1 (e < base) or times
+// (a_re + i a_im) k along axis dims[e] (k the signed integer frequency).
+struct FftWeights {
+  int E, base;
+  int dims[4];
+  double a_re, a_im;
+};
 void fft_pow2_twiddles(int64_t n, std::vector<float>& out);
 template <typename TD>
 cudaError_t launch_fft_type2(int dim, const int64_t* N, const int64_t* nf, int modeord,
                              const float* const* phi, const float2* const* tw,
-                             const void* modes, void* fine, int nb, int sign, cudaStream_t s);
+                             const void* modes, void* fine, int nb, int sign, cudaStream_t s,
+                             const FftWeights* wts = nullptr);
 template <typename TD>
 cudaError_t launch_fft_type1(int dim, const int64_t* N, const int64_t* nf, int modeord,
                              const float* const* phi, const float2* const* tw, void* fine,

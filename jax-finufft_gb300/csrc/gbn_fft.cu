@@ -195,7 +195,19 @@ struct AxisSpec {
   int N[3];     // modes per axis
   int nf[3];    // fine cells per axis
   int modeord;
+  // type-2 direction with E weighted grids per transform (fused gradient):
+  // grid e of transform t is launch grid t*E + e and gets the modes times 1
+  // (e < base) or times (a_re + i a_im) k along axis wdim[e]; E = base = 1
+  // for a plain transform
+  int E, base;
+  int wdim[4];
+  float a_re, a_im;
 };
+
+// Signed integer frequency of mode index i along an axis of N modes.
+__device__ __forceinline__ int mode_freq_f(int i, int N, int modeord) {
+  return modeord == 0 ? i - N / 2 : (i < (N + 1) / 2 ? i : i - N);
+}
 
 // x pass over mode rows.  Row r of the launch (r < M1*M2 per transform,
 // blockIdx.y = transform) is mode row (i1, i2) = (r % M1, r / M1), fine row
@@ -227,7 +239,12 @@ __global__ void __launch_bounds__(256)
   }
   const int64_t tr = blockIdx.y;
   float2* frow = fine + tr * nftot + ((int64_t)g2 * ax.nf[1] + g1) * N;
-  cplx_t<TD>* mrow = modes + tr * Ntot + ((int64_t)i2 * M1 + i1) * M0;
+  // grid tr holds weighted grid we of transform tm (TO_GRID; E = 1 otherwise)
+  const int64_t tm = TO_GRID ? tr / ax.E : tr;
+  const int we = TO_GRID ? (int)(tr - tm * ax.E) : 0;
+  cplx_t<TD>* mrow = modes + tm * Ntot + ((int64_t)i2 * M1 + i1) * M0;
+  const bool weighted = TO_GRID && we >= ax.base;
+  const int wd = weighted ? ax.wdim[we] : 0;
   float2 a[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
@@ -239,6 +256,12 @@ __global__ void __launch_bounds__(256)
         const cplx_t<TD> v = mrow[i0];
         const float f = p0[i0] * f12;
         a[e] = make_float2((float)v.x * f, (float)v.y * f);
+        if (weighted) {
+          const float kk = (float)(wd == 0   ? mode_freq_f(i0, M0, ax.modeord)
+                                   : wd == 1 ? mode_freq_f(i1, M1, ax.modeord)
+                                             : mode_freq_f(i2, M2, ax.modeord));
+          a[e] = c_mul(a[e], make_float2(ax.a_re * kk, ax.a_im * kk));
+        }
       }
     } else {
       a[e] = live ? frow[n] : make_float2(0.f, 0.f);
@@ -430,14 +453,29 @@ static void mode_span(int64_t N, int* lo, int* hi) {
 template <typename TD>
 cudaError_t launch_fft_type2(int dim, const int64_t* N, const int64_t* nf, int modeord,
                              const float* const* phi, const float2* const* tw,
-                             const void* modes, void* fine, int nb, int sign,
-                             cudaStream_t s) {
+                             const void* modes, void* fine, int nb, int sign, cudaStream_t s,
+                             const FftWeights* wts) {
   AxisSpec ax;
   for (int d = 0; d < 3; ++d) {
     ax.N[d] = (int)N[d];
     ax.nf[d] = (int)nf[d];
   }
   ax.modeord = modeord;
+  ax.E = 1;
+  ax.base = 1;
+  ax.wdim[0] = ax.wdim[1] = ax.wdim[2] = ax.wdim[3] = 0;
+  ax.a_re = 1.f;
+  ax.a_im = 0.f;
+  if (wts) {
+    if (wts->E < 1 || wts->E > 4 || wts->base < 0 || wts->base > wts->E) return cudaErrorInvalidValue;
+    ax.E = wts->E;
+    ax.base = wts->base;
+    for (int e = 0; e < 4; ++e) ax.wdim[e] = wts->dims[e];
+    ax.a_re = (float)wts->a_re;
+    ax.a_im = (float)wts->a_im;
+    nb *= wts->E;  // every weighted grid is a transform of its own from here on
+  }
+  if (nb > 65535) return cudaErrorInvalidValue;
   const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
   float2* g = (float2*)fine;
   cudaError_t e = launch_row_any<true, TD>(dim, sign, ax, phi, tw[0], g, (void*)modes, nftot,
@@ -467,6 +505,11 @@ cudaError_t launch_fft_type1(int dim, const int64_t* N, const int64_t* nf, int m
     ax.nf[d] = (int)nf[d];
   }
   ax.modeord = modeord;
+  ax.E = 1;
+  ax.base = 1;
+  ax.wdim[0] = ax.wdim[1] = ax.wdim[2] = ax.wdim[3] = 0;
+  ax.a_re = 1.f;
+  ax.a_im = 0.f;
   const int64_t nftot = nf[0] * nf[1] * nf[2], Ntot = N[0] * N[1] * N[2];
   float2* g = (float2*)fine;
   cudaError_t e = cudaSuccess;
@@ -492,10 +535,12 @@ cudaError_t launch_fft_type1(int dim, const int64_t* N, const int64_t* nf, int m
 
 template cudaError_t launch_fft_type2<float>(int, const int64_t*, const int64_t*, int,
                                              const float* const*, const float2* const*,
-                                             const void*, void*, int, int, cudaStream_t);
+                                             const void*, void*, int, int, cudaStream_t,
+                                             const FftWeights*);
 template cudaError_t launch_fft_type2<double>(int, const int64_t*, const int64_t*, int,
                                               const float* const*, const float2* const*,
-                                              const void*, void*, int, int, cudaStream_t);
+                                              const void*, void*, int, int, cudaStream_t,
+                                              const FftWeights*);
 template cudaError_t launch_fft_type1<float>(int, const int64_t*, const int64_t*, int,
                                              const float* const*, const float2* const*, void*,
                                              void*, int, int, cudaStream_t);

@@ -1147,21 +1147,38 @@ int plan_grad(gbn_plan_s* p, gbn_points_s& ps, int ntr, const void* src, const v
     const void* win = wsrc + (size_t)t0 * ps.M * dsz;
     void* outc = base ? (void*)((char*)grad_src + (size_t)t0 * ps.M * dsz) : nullptr;
     cudaError_t e;
-    if (p->comp_single) {
+    const char* no_own = std::getenv("GBN_DISABLE_OWN_FFT");
+    if (p->fft_own && !(no_own && no_own[0] == '1') &&
+        fft_pow2_supported(p->dim, p->nf, nb * E)) {
+      // the library's pruned FFT builds the weighted grids in its x pass
       const float* phi[3] = {p->phi[0].as<float>(), p->phi[1].as<float>(), p->phi[2].as<float>()};
+      const float2* tw[3] = {p->fft_tw[0].as<float2>(), p->fft_tw[1].as<float2>(),
+                             p->fft_tw[2].as<float2>()};
+      FftWeights wts{E, base, {dims[0], dims[1], dims[2], dims[3]}, a_re, a_im};
       e = p->data_single
-              ? launch_deconv2w<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
-                                              p->gfine.p, nb, E, base, dims, a_re, a_im, s)
-              : launch_deconv2w<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
-                                               p->gfine.p, nb, E, base, dims, a_re, a_im, s);
+              ? launch_fft_type2<float>(p->dim, p->N, p->nf, p->opts.modeord, phi, tw, min,
+                                        p->gfine.p, nb, sign, s, &wts)
+              : launch_fft_type2<double>(p->dim, p->N, p->nf, p->opts.modeord, phi, tw, min,
+                                         p->gfine.p, nb, sign, s, &wts);
+      GBN_CUDA(e);
     } else {
-      const double* phi[3] = {p->phi[0].as<double>(), p->phi[1].as<double>(),
-                              p->phi[2].as<double>()};
-      e = launch_deconv2w<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
-                                          p->gfine.p, nb, E, base, dims, a_re, a_im, s);
+      if (p->comp_single) {
+        const float* phi[3] = {p->phi[0].as<float>(), p->phi[1].as<float>(),
+                               p->phi[2].as<float>()};
+        e = p->data_single
+                ? launch_deconv2w<float, float>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
+                                                p->gfine.p, nb, E, base, dims, a_re, a_im, s)
+                : launch_deconv2w<float, double>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
+                                                 p->gfine.p, nb, E, base, dims, a_re, a_im, s);
+      } else {
+        const double* phi[3] = {p->phi[0].as<double>(), p->phi[1].as<double>(),
+                                p->phi[2].as<double>()};
+        e = launch_deconv2w<double, double>(p->dim, p->N, p->nf, p->opts.modeord, phi, min,
+                                            p->gfine.p, nb, E, base, dims, a_re, a_im, s);
+      }
+      GBN_CUDA(e);
+      GBN_TRY(exec_fft(p, p->gfine.p, nb * E, sign, 1));
     }
-    GBN_CUDA(e);
-    GBN_TRY(exec_fft(p, p->gfine.p, nb * E, sign, 1));
     if (p->comp_single) {
       CUtensorMap map;
       const CUtensorMap* tm = grid_map(p, ps, p->gfine.p, nb * E, &map);
