@@ -1877,12 +1877,24 @@ int batch_execute(gbn_batch_s* b, void* c, void* f) {
     }
     return GBN_OK;
   }
+  // problems on FP32 power-of-two grids take the library's pruned FFT with
+  // the deconvolution fused (per problem); the others the per-group cuFFT
+  // and separate deconvolution
+  const char* no_own = std::getenv("GBN_DISABLE_OWN_FFT");
+  const bool own_off = no_own && no_own[0] == '1';
+  auto own_k = [&](int k) { return !own_off && b->sub[k]->fft_own; };
   if (b->type == 2) {
-    for (int k = 0; k < b->K; ++k)
-      GBN_TRY(do_deconv(b->sub[k].get(), (char*)f + b->f_off[k] * dsz, b->T, false,
-                        arena + b->grid_off[k] * csz));
+    for (int k = 0; k < b->K; ++k) {
+      char* fk = (char*)f + b->f_off[k] * dsz;
+      char* gk = arena + b->grid_off[k] * csz;
+      if (own_k(k))
+        GBN_TRY(own_fft(b->sub[k].get(), gk, fk, b->T, b->iflag, false));
+      else
+        GBN_TRY(do_deconv(b->sub[k].get(), fk, b->T, false, gk));
+    }
     for (const auto& g : b->groups)
-      GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
+      if (!own_k(g.first))
+        GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
     GBN_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(int), s));
     cudaError_t e;
     if (b->comp_single)
@@ -1924,10 +1936,16 @@ int batch_execute(gbn_batch_s* b, void* c, void* f) {
                                               b->T, c, arena, b->smem, s);
     GBN_CUDA(e);
     for (const auto& g : b->groups)
-      GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
-    for (int k = 0; k < b->K; ++k)
-      GBN_TRY(do_deconv(b->sub[k].get(), (char*)f + b->f_off[k] * dsz, b->T, true,
-                        arena + b->grid_off[k] * csz));
+      if (!own_k(g.first))
+        GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
+    for (int k = 0; k < b->K; ++k) {
+      char* fk = (char*)f + b->f_off[k] * dsz;
+      char* gk = arena + b->grid_off[k] * csz;
+      if (own_k(k))
+        GBN_TRY(own_fft(b->sub[k].get(), gk, fk, b->T, b->iflag, true));
+      else
+        GBN_TRY(do_deconv(b->sub[k].get(), fk, b->T, true, gk));
+    }
   }
   GBN_CUDA(cudaGetLastError());
   return GBN_OK;
