@@ -2,7 +2,11 @@
 // FP64 chain it stands in for: for every float bit pattern in a stride over
 // all 2^32 (non-finite ones included), wherever fold_fast_f32 accepts a
 // point, its grid start and FP32 offset must equal those of the FP64 chain.
-// Usage: fold_fast_check nf w stride threads; prints "<accepted> <mismatches>".
+// Usage: fold_fast_check nf w stride threads [boundary]; prints
+// "<accepted> <mismatches>".  With "boundary" the inputs are instead the
+// floats within 64 ulps of every grid cell and half cell, x = 2 pi (j + o)/nf
+// for j in [-nf, nf) and o in {0, 1/2}: where the ceiling of s and the FP32
+// rounding of the offset are closest to a decision.
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -50,6 +54,35 @@ int main(int argc, char** argv) {
   int lnf = 0;
   while ((1ll << lnf) < nf) ++lnf;
   std::atomic<long long> accepted{0}, bad{0};
+  auto check = [&](float x, long long& a, long long& m) {
+    int i0 = 0;
+    float d = 0.f;
+    if (!gbn::fold_fast_f32(x, nf, w, lnf, kmant, kexp, i0, d)) return;
+    ++a;
+    const double sh = grid_shift(x, nf, 0.5 * w);
+    const double cl = std::ceil(sh);
+    const float rd = (float)(cl - sh);
+    if ((int)cl != i0 || std::memcmp(&d, &rd, 4) != 0) ++m;
+  };
+  if (argc > 5 && std::strcmp(argv[5], "boundary") == 0) {
+    long long a = 0, m = 0;
+    const double pi = 3.14159265358979323846;
+    for (long long j = -nf; j < nf; ++j) {
+      for (int h = 0; h < 2; ++h) {
+        const float x0 = (float)(2.0 * pi * ((double)j + 0.5 * h) / nf);
+        uint32_t b0;
+        std::memcpy(&b0, &x0, 4);
+        for (int k = -64; k <= 64; ++k) {
+          const uint32_t bk = b0 + (uint32_t)k;
+          float x;
+          std::memcpy(&x, &bk, 4);
+          check(x, a, m);
+        }
+      }
+    }
+    std::printf("%lld %lld\n", a, m);
+    return 0;
+  }
   std::vector<std::thread> th;
   for (int t = 0; t < nt; ++t) {
     th.emplace_back([&, t] {

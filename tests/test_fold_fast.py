@@ -41,3 +41,13 @@ def test_fold_fast_path_matches_fp64_chain(checker, nf, w):
     # most finite patterns in range are accepted (non-finite, zero, subnormal
     # and |x| >= 2^22 pi are always declined)
     assert accepted > (1 << 32) // 97 // 10
+
+
+@pytest.mark.parametrize("nf, w", [(512, 6), (540, 7), (1024, 8), (128, 2), (4096, 16)])
+def test_fold_fast_path_at_grid_boundaries(checker, nf, w):
+    """Floats within 64 ulps of every grid cell and half cell."""
+    out = subprocess.run([checker, str(nf), str(w), "1", "1", "boundary"], check=True,
+                         capture_output=True, text=True).stdout.split()
+    accepted, mismatches = int(out[0]), int(out[1])
+    assert mismatches == 0
+    assert accepted > 0
