@@ -225,8 +225,20 @@ GBN_API void gbn_autotune_clear(int forget_file);
 
 /* Number of bounded device-side waits (the bulk tensor copy of a tile into
  * shared memory) that gave up on the current device since the last reset;
- * 0 in a healthy run.  reset = 1 clears it.  Synchronous. */
+ * 0 in a healthy run.  reset = 1 clears it.  Synchronous.
+ *
+ * A wait that gives up skips its block's output, and the first call of
+ * gbn_execute, gbn_execute_points, gbn_grad, gbn_run (and the named
+ * entry points) or gbn_batch_run on that device that observes it returns
+ * GBN_ERR_CUDA -- the reference turns a failed execute into an error the
+ * same way (lib/kernels.cc.cu:70-79).  The check reads mapped host memory
+ * without synchronising, so it reports work enqueued by that call or an
+ * earlier one; synchronise the stream first to attribute it to one call. */
 GBN_API int gbn_wait_timeouts(long long* count, int reset);
+
+/* Test hook: mark the current device as if a bounded wait had given up, so
+ * the error path above can be exercised without stalling a GPU. */
+GBN_API void gbn_debug_raise_wait_timeout(void);
 
 /* Measurement aid (no counterpart in the reference): int32 shared-memory
  * atomic adds per second over the whole GPU with the access pattern of the

@@ -207,6 +207,16 @@ bool tile_tensor_map(const Geom& g, const void* grid, int nb, CUtensorMap* out);
 // should take microseconds); 0 in a healthy run.  reset clears the count.
 cudaError_t read_wait_timeouts(unsigned* out, bool reset);
 
+// A bounded wait that gave up also raises a word of mapped pinned host
+// memory of its device, which the host reads without synchronising.
+// wait_flag_setup: allocate and publish that word for the current device
+// (once per device; plan and batch creation call it).  wait_flag_take: true
+// if it was raised on the current device since the last take, and clears
+// it.  wait_flag_raise: raise it from the host (test hook, as a kernel would).
+cudaError_t wait_flag_setup();
+bool wait_flag_take();
+void wait_flag_raise();
+
 // Interpolate ntr transforms: fine -> c (ntr, M).
 template <typename TC, typename TD>
 cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,

@@ -24,8 +24,12 @@ namespace gbn {
 
 namespace {
 
-// Bounded waits that gave up (see read_wait_timeouts).
+// Bounded waits that gave up: counted on the device (read_wait_timeouts)
+// and raised in a word of mapped pinned host memory (g_wait_host, set up per
+// device by wait_flag_setup), which the host reads on every API call without
+// synchronising.
 __device__ unsigned g_wait_timeouts;
+__device__ unsigned* g_wait_host;
 constexpr int kWaitPolls = 1 << 20;
 
 // Grids per shared-memory interpolation block: up to four stacked grids share
@@ -181,9 +185,18 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
         }
       }
       __syncthreads();  // the barrier is initialised before anyone polls it
-      if (!mbar_wait_bounded(&s_bar, 0, kWaitPolls)) {
-        if (threadIdx.x == 0) atomicAdd(&g_wait_timeouts, 1u);
-        mbar_wait_bounded(&s_bar, 0, kWaitPolls);  // the copies in flight, bounded again
+      // block-uniform outcome: if any thread gave up, all take the error path
+      if (__syncthreads_or(!mbar_wait_bounded(&s_bar, 0, kWaitPolls))) {
+        if (threadIdx.x == 0) {
+          atomicAdd(&g_wait_timeouts, 1u);
+          if (g_wait_host) {
+            atomicAdd_system(g_wait_host, 1u);
+            __threadfence_system();
+          }
+        }
+        // wait (bounded again) for the copies in flight; a tile that still
+        // has not arrived is never read and the block writes no output
+        if (__syncthreads_or(!mbar_wait_bounded(&s_bar, 0, kWaitPolls))) return;
       }
       staged = true;
     }
@@ -696,6 +709,55 @@ cudaError_t launch_interp_grad_sm(const Geom& g, const KerSpec<TC>& ks, int64_t 
 GBN_INST_IGS(float, float)
 GBN_INST_IGS(float, double)
 GBN_INST_IGS(double, double)
+
+namespace {
+struct WaitFlag {
+  std::once_flag once;
+  cudaError_t err = cudaSuccess;
+  volatile unsigned* host = nullptr;
+};
+constexpr int kMaxDevices = 64;
+WaitFlag g_flags[kMaxDevices];
+
+WaitFlag* flag_of_current(int* dev_out = nullptr) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  if (dev_out) *dev_out = dev;
+  return &g_flags[dev];
+}
+}  // namespace
+
+cudaError_t wait_flag_setup() {
+  WaitFlag* f = flag_of_current();
+  if (!f) return cudaErrorInvalidDevice;
+  std::call_once(f->once, [f]() {
+    void* h = nullptr;
+    f->err = cudaHostAlloc(&h, sizeof(unsigned), cudaHostAllocMapped | cudaHostAllocPortable);
+    if (f->err != cudaSuccess) return;
+    *(volatile unsigned*)h = 0u;
+    void* d = nullptr;
+    f->err = cudaHostGetDevicePointer(&d, h, 0);
+    if (f->err == cudaSuccess) f->err = cudaMemcpyToSymbol(g_wait_host, &d, sizeof(d));
+    if (f->err != cudaSuccess) {
+      cudaFreeHost(h);
+      return;
+    }
+    f->host = (volatile unsigned*)h;
+  });
+  return f->err;
+}
+
+bool wait_flag_take() {
+  WaitFlag* f = flag_of_current();
+  if (!f || !f->host || *f->host == 0u) return false;
+  *f->host = 0u;
+  return true;
+}
+
+void wait_flag_raise() {
+  WaitFlag* f = flag_of_current();
+  if (f && f->host) *f->host += 1u;
+}
 
 cudaError_t read_wait_timeouts(unsigned* out, bool reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_wait_timeouts, sizeof(unsigned));

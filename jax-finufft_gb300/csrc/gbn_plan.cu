@@ -48,6 +48,21 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+// A bounded device-side wait that gave up (a tile copy into shared memory
+// that never completed; the kernel then skipped that block's output) turns
+// the status of the first API call on that device that observes it into an
+// error: the check reads mapped host memory and does not synchronise, so it
+// reports work enqueued by this or an earlier call, like CUDA's own
+// asynchronous errors.
+int check_waits(int r) {
+  if (r >= 2) return r;
+  if (gbn::wait_flag_take())
+    return fail(GBN_ERR_CUDA,
+                "a bounded device-side wait gave up (tile copy into shared memory): outputs of "
+                "the calls enqueued on this device since the previous check are invalid");
+  return r;
+}
+
 #define GBN_CUDA(expr)                                                                    \
   do {                                                                                    \
     cudaError_t e_ = (expr);                                                              \
@@ -651,6 +666,7 @@ int plan_create(int type, int dim, const int64_t* nmodes, int iflag, int ntransf
   p->eps = eps;
   p->stream = (cudaStream_t)stream;
   GBN_CUDA(cudaGetDevice(&p->device));
+  GBN_CUDA(wait_flag_setup());
   GBN_TRY(resolve_precision(p.get()));
   p->sigma = p->opts.upsampfac > 0.0 ? p->opts.upsampfac : 2.0;
   if (!(p->sigma > 1.0)) return fail(GBN_ERR_ARGS, "upsampfac must be > 1");
@@ -1395,7 +1411,8 @@ int gbnf_setpts(gbn_plan plan, int64_t M, const float* x, const float* y, const 
 
 int gbn_execute(gbn_plan plan, void* c, void* f) {
   if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
-  return execute_ntr(plan, plan->own, c, f, plan->ntransf, 1);
+  if (int r = check_waits(GBN_OK)) return r;
+  return check_waits(execute_ntr(plan, plan->own, c, f, plan->ntransf, 1));
 }
 
 int gbn_set_stream(gbn_plan plan, void* stream) {
@@ -1536,13 +1553,15 @@ int gbn_execute_points(gbn_plan plan, gbn_points pts, int ntr, int dir, void* c,
   if (!plan || !pts) return fail(GBN_ERR_ARGS, "NULL plan or point set");
   if (dir != 1 && dir != -1) return fail(GBN_ERR_ARGS, "dir must be +1 or -1");
   if (ntr < 1) return fail(GBN_ERR_ARGS, "ntr must be >= 1");
-  return execute_ntr(plan, *pts, c, f, ntr, dir);
+  if (int r = check_waits(GBN_OK)) return r;
+  return check_waits(execute_ntr(plan, *pts, c, f, ntr, dir));
 }
 
 int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void* g,
              void* grad_src, void* const* grad_x) {
   if (!plan || !pts || !src || !g) return fail(GBN_ERR_ARGS, "NULL argument");
-  return plan_grad(plan, *pts, ntr, src, g, grad_src, grad_x);
+  if (int r = check_waits(GBN_OK)) return r;
+  return check_waits(plan_grad(plan, *pts, ntr, src, g, grad_src, grad_x));
 }
 
 void gbn_clear_cache(void) { cache().clear(); }
@@ -1553,9 +1572,12 @@ int gbn_wait_timeouts(long long* count, int reset) {
   if (!count) return fail(GBN_ERR_ARGS, "NULL argument");
   unsigned v = 0;
   GBN_CUDA(read_wait_timeouts(&v, reset != 0));
+  if (reset) gbn::wait_flag_take();
   *count = (long long)v;
   return GBN_OK;
 }
+
+void gbn_debug_raise_wait_timeout(void) { gbn::wait_flag_raise(); }
 
 int gbn_run(int type, int dim, int single, void* stream, double eps, int iflag, int64_t n_tot,
             int64_t n_transf, int64_t n_j, const int64_t* n_k, const gbn_opts* opts,
@@ -1563,22 +1585,23 @@ int gbn_run(int type, int dim, int single, void* stream, double eps, int iflag, 
   if (type < 1 || type > 3 || dim < 1 || dim > 3) return fail(GBN_ERR_ARGS, "bad type or dim");
   if (!n_k || !pts) return fail(GBN_ERR_ARGS, "NULL n_k or points");
   if (type == 3 && !tgts) return fail(GBN_ERR_ARGS, "NULL targets");
+  if (int r = check_waits(GBN_OK)) return r;
   if (single) {
     const float* p[3] = {(const float*)pts[0], dim > 1 ? (const float*)pts[1] : nullptr,
                          dim > 2 ? (const float*)pts[2] : nullptr};
     const float* t[3] = {nullptr, nullptr, nullptr};
     if (type == 3)
       for (int d = 0; d < dim; ++d) t[d] = (const float*)tgts[d];
-    return run_oneshot<float>(type, dim, true, stream, eps, iflag, n_tot, n_transf, n_j, n_k,
-                              opts, source, p, t, output);
+    return check_waits(run_oneshot<float>(type, dim, true, stream, eps, iflag, n_tot,
+                                          n_transf, n_j, n_k, opts, source, p, t, output));
   }
   const double* p[3] = {(const double*)pts[0], dim > 1 ? (const double*)pts[1] : nullptr,
                         dim > 2 ? (const double*)pts[2] : nullptr};
   const double* t[3] = {nullptr, nullptr, nullptr};
   if (type == 3)
     for (int d = 0; d < dim; ++d) t[d] = (const double*)tgts[d];
-  return run_oneshot<double>(type, dim, false, stream, eps, iflag, n_tot, n_transf, n_j, n_k,
-                             opts, source, p, t, output);
+  return check_waits(run_oneshot<double>(type, dim, false, stream, eps, iflag, n_tot, n_transf,
+                                         n_j, n_k, opts, source, p, t, output));
 }
 
 }  // extern "C"
@@ -2022,7 +2045,8 @@ int gbn_batch_create(int type, int dim, int single, int K, const int64_t* nmodes
 int gbn_batch_run(gbn_batch b, const void* x, const void* y, const void* z, void* c, void* f,
                   int use_graph) {
   if (!b) return fail(GBN_ERR_ARGS, "NULL batch");
-  return batch_run(b, x, y, z, c, f, use_graph);
+  if (int r = check_waits(GBN_OK)) return r;
+  return check_waits(batch_run(b, x, y, z, c, f, use_graph));
 }
 
 int gbn_batch_info(gbn_batch b, int* ngroups, int* queue, int64_t* arena_bytes) {

@@ -82,3 +82,46 @@ def test_no_wait_gave_up(native):
     n = ctypes.c_longlong(-1)
     assert native.gbn_wait_timeouts(ctypes.byref(n), 0) == 0
     assert n.value == 0
+
+
+def test_gave_up_wait_is_an_error(jf, native):
+    """A bounded wait that gave up makes the next call on the device return
+    GBN_ERR_CUDA (lib/kernels.cc.cu:70-79 turns a failed execute into an
+    error); the flag is raised from the host, no wait is made to run out."""
+    from jax_finufft_gb300 import _native
+
+    rng = np.random.default_rng(5)
+    x = [torch.tensor(rng.uniform(-np.pi, np.pi, 2000).astype(np.float32), device=DEV)
+         for _ in range(2)]
+    f = torch.tensor((rng.standard_normal((32, 32)) + 1j * rng.standard_normal((32, 32)))
+                     .astype(np.complex64), device=DEV)
+    good = jf.nufft2(f, *x, eps=1e-5)
+    torch.cuda.synchronize()
+    native.gbn_debug_raise_wait_timeout()
+    with pytest.raises(_native.NufftError) as err:
+        jf.nufft2(f, *x, eps=1e-5)
+    assert err.value.code == 3 and "wait gave up" in str(err.value)
+    # reported once: the next call runs and agrees with the first
+    again = jf.nufft2(f, *x, eps=1e-5)
+    torch.cuda.synchronize()
+    assert torch.equal(good, again)
+    # the plan API reports it the same way
+    opts = _native.default_opts()
+    nm = (ctypes.c_int64 * 3)(32, 32, 1)
+    plan = ctypes.c_void_p()
+    _native.check(native.gbnf_makeplan(2, 2, nm, -1, 1, 1e-5, ctypes.byref(plan),
+                                       ctypes.byref(opts), None))
+    try:
+        _native.check(native.gbnf_setpts(plan, 2000, ctypes.c_void_p(x[1].data_ptr()),
+                                         ctypes.c_void_p(x[0].data_ptr()), None, 0, None, None,
+                                         None))
+        c = torch.empty(2000, dtype=torch.complex64, device=DEV)
+        native.gbn_debug_raise_wait_timeout()
+        assert native.gbn_execute(plan, ctypes.c_void_p(c.data_ptr()),
+                                  ctypes.c_void_p(f.data_ptr())) == 3
+        assert native.gbn_execute(plan, ctypes.c_void_p(c.data_ptr()),
+                                  ctypes.c_void_p(f.data_ptr())) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(c, good)
+    finally:
+        native.gbn_destroy(plan)
