@@ -17,9 +17,11 @@ and modes and the device->host copy of the result inside the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
---impl reference times the CPU restatement of the algorithm (the oracle
-port: C/OpenMP spreading + scipy pocketfft) on the host cores: the
-reference's own FINUFFT cannot be built here (empty submodule).
+--impl reference times the CPU restatement of the algorithm on the host
+cores, on the full workload, in single precision as FINUFFT runs complex64
+(C/OpenMP spreading and interpolation + scipy pocketfft), with the FP64
+oracle port as a second, labelled number: the reference's own FINUFFT cannot
+be built here (empty submodule).
 """
 import argparse
 import ctypes
@@ -174,15 +176,32 @@ def job_value(points_per_rank, ms_max, ws):
 # ---------------------------------------------------------------------------
 # CPU arm (oracle port)
 # ---------------------------------------------------------------------------
-def cpu_round_trip(M):
-    """One round trip of the CPU restatement on M points of the workload."""
+_CPU_INPUTS = {}
+
+
+def cpu_round_trip(M, single=True):
+    """One round trip of the CPU restatement on M points of the workload:
+    single=True is its single-precision fast path (complex64 throughout, as
+    FINUFFT runs complex64 transforms: Horner kernel values, bin-sorted
+    private subgrids, complex64 pocketfft), single=False the FP64 oracle."""
     from oracle import cpu_nufft
 
-    pts, f = make_inputs(M=M)
+    if M not in _CPU_INPUTS:
+        _CPU_INPUTS.clear()
+        _CPU_INPUTS[M] = make_inputs(M=M)
+    pts, f = _CPU_INPUTS[M]
     t0 = time.perf_counter()
-    c = cpu_nufft.nufft2(f, *pts, eps=EPS, iflag=-1)
-    cpu_nufft.nufft1((N_MODES,) * 3, c, *pts, eps=EPS, iflag=1)
+    c = cpu_nufft.nufft2(f, *pts, eps=EPS, iflag=-1, single=single)
+    cpu_nufft.nufft1((N_MODES,) * 3, c, *pts, eps=EPS, iflag=1, single=single)
     return time.perf_counter() - t0
+
+
+CPU_SAMPLE_FP32 = ("the full workload (M=1e7, 256^3 modes) through the CPU restatement's "
+                   "single-precision path: complex64 data and arithmetic as FINUFFT runs "
+                   "complex64, kernel by Horner's rule, bin-sorted points spread into private "
+                   "subgrids, scipy pocketfft in complex64 with one worker per core")
+CPU_SAMPLE_FP64 = ("one full round trip through the FP64 oracle port (C/OpenMP with the exact "
+                   "kernel, scipy pocketfft in complex128)")
 
 
 def cpu_cores():
@@ -200,23 +219,23 @@ def run_reference(args):
 
     cores = cpu_cores()
     cpu_nufft.set_threads(cores)
-    budget_steps = args.steps + args.warmup
-    M = M_POINTS if budget_steps <= 13 else max(1_000_000, int(M_POINTS * 13 / budget_steps))
+    M = M_POINTS
     for _ in range(args.warmup):
         cpu_round_trip(M)
     times = [cpu_round_trip(M) for _ in range(args.steps)]
     t = sum(times) / len(times)
     value = 2 * M / t
-    sample = ("oracle port (C/OpenMP spread/interp + scipy pocketfft, FP64) on the full "
-              "workload" if M == M_POINTS else "oracle port on M=%d points of the workload "
-              "(same 256^3 grid)" % M)
+    t64 = cpu_round_trip(M, single=False)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "M_sample": M},
+        "data": "synthetic", "config": {"workload": WORKLOAD, "M": M, "modes": [N_MODES] * 3,
+                                        "eps": EPS, "same_config": True},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": CPU_SAMPLE_FP32,
+                         "fp64_port": {"value": 2 * M / t64, "unit": UNIT, "ms_per_step": t64 * 1e3,
+                                       "sample": CPU_SAMPLE_FP64}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "FINUFFT (the reference's CPU library) is an empty submodule and cannot be "
                 "built; the CPU restatement of its algorithm stands in for it",
@@ -755,11 +774,16 @@ def finish(args, result, rank, ws):
 
         cores = cpu_cores()
         cpu_nufft.set_threads(cores)
-        t_cpu = cpu_round_trip(M_POINTS)
+        cpu_round_trip(M_POINTS)  # warm-up (FFT plans, page faults)
+        t_cpu = min(cpu_round_trip(M_POINTS) for _ in range(2))
+        t64 = cpu_round_trip(M_POINTS, single=False)
         result["cpu_baseline"] = {
             "value": 2 * M_POINTS / t_cpu, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "one full round trip of the workload on the oracle port "
-                      "(C/OpenMP + scipy pocketfft, FP64), %.1f s" % t_cpu}
+            "sample": CPU_SAMPLE_FP32 + "; best of 2 round trips after one warm-up, %.2f s"
+                      % t_cpu,
+            "fp64_port": {"value": 2 * M_POINTS / t64, "unit": UNIT, "ms_per_step": t64 * 1e3,
+                          "sample": CPU_SAMPLE_FP64}}
+        _CPU_INPUTS.clear()
     if rank == 0:
         print(json.dumps(result), flush=True)
     if ws > 1:

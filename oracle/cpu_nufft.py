@@ -62,6 +62,15 @@ def lib():
         L.orc_interp.restype = None
         L.orc_interp.argtypes = [ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_double,
                                  ctypes.c_int64, _i64p, _dp, _dp, _dp]
+        _fp = ctypes.POINTER(ctypes.c_float)
+        for name in ("orc_spread_f32", "orc_interp_f32"):
+            fn = getattr(L, name)
+            fn.restype = None
+            fn.argtypes = [ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int64,
+                           _i64p, _fp, _fp, _fp]
+        L.orc_deconv_f32.restype = None
+        L.orc_deconv_f32.argtypes = [ctypes.c_int, ctypes.c_int, _i64p, _i64p, _i64p, _i64p,
+                                     _i64p, _fp, _fp, _fp, _fp, _fp]
         L.orc_horner_fit.restype = None
         L.orc_horner_fit.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]
         L.orc_type3_params.restype = ctypes.c_int64
@@ -229,10 +238,76 @@ class Plan:
         return i0, de
 
 
-def nufft1(n_modes, c, *points, eps=1e-6, iflag=1, modeord=0, sigma=2.0, workers=None):
-    """Type 1 in the user's axis order.  c: (M,) or (T, M) complex."""
+def _f32_args(plan, i0, de):
+    """Arguments of the single-precision C routines for plan's geometry."""
+    deg = plan.w + 2
+    coef = np.ascontiguousarray(horner_fit(plan.w, plan.beta, deg).ravel())
+    nf = np.ones(3, dtype=np.int64)
+    nf[:plan.dim] = list(plan.nf)[::-1]
+    return (plan.dim, _p(nf, _i64p), plan.w, deg, _p(coef, _dp), i0.shape[0], _p(i0, _i64p),
+            _p(np.ascontiguousarray(de, dtype=np.float32), ctypes.POINTER(ctypes.c_float))), \
+        (nf, coef, de)
+
+
+def _spread_f32(plan, i0, de, c):
+    args, keep = _f32_args(plan, i0, de)
+    de32 = np.ascontiguousarray(de, dtype=np.float32)
+    cc = np.ascontiguousarray(c, dtype=np.complex64)
+    grid = np.zeros(int(np.prod(plan.nf)), dtype=np.complex64)
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib().orc_spread_f32(*args[:7], _p(de32, fp), cc.view(np.float32).ctypes.data_as(fp),
+                         grid.view(np.float32).ctypes.data_as(fp))
+    return grid.reshape(plan.nf)
+
+
+def _interp_f32(plan, i0, de, grid):
+    args, keep = _f32_args(plan, i0, de)
+    de32 = np.ascontiguousarray(de, dtype=np.float32)
+    g = np.ascontiguousarray(grid, dtype=np.complex64).ravel()
+    out = np.empty(i0.shape[0], dtype=np.complex64)
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib().orc_interp_f32(*args[:7], _p(de32, fp), g.view(np.float32).ctypes.data_as(fp),
+                         out.view(np.float32).ctypes.data_as(fp))
+    return out
+
+
+def _deconv_f32(plan, direction, f, grid):
+    """Single-precision deconvolution between modes f and the fine grid
+    (direction 1: zero-pad into grid; -1: crop into f), in C with threads."""
+    fp = ctypes.POINTER(ctypes.c_float)
+    rev = list(range(plan.dim))[::-1]  # backend order: the user's last axis first
+    n = np.array([plan.n_modes[a] for a in rev] + [1] * (3 - plan.dim), dtype=np.int64)
+    nf = np.array([plan.nf[a] for a in rev] + [1] * (3 - plan.dim), dtype=np.int64)
+    idx = [np.ascontiguousarray(plan.idx[a], dtype=np.int64) for a in rev]
+    fac = [np.ascontiguousarray(1.0 / plan.phihat[a], dtype=np.float32) for a in rev]
+    while len(idx) < 3:
+        idx.append(np.zeros(1, dtype=np.int64))
+        fac.append(np.ones(1, dtype=np.float32))
+    lib().orc_deconv_f32(direction, plan.dim, _p(n, _i64p), _p(nf, _i64p),
+                         *[_p(i, _i64p) for i in idx], *[_p(a, fp) for a in fac],
+                         f.view(np.float32).ctypes.data_as(fp),
+                         grid.view(np.float32).ctypes.data_as(fp))
+
+
+def nufft1(n_modes, c, *points, eps=1e-6, iflag=1, modeord=0, sigma=2.0, workers=None,
+           single=False):
+    """Type 1 in the user's axis order.  c: (M,) or (T, M) complex.
+
+    single=True runs the single-precision fast path (complex64 throughout,
+    kernel by Horner's rule, bin-sorted private subgrids): the timed CPU
+    baseline, not the checker."""
     workers = workers or _workers()
     plan = Plan(n_modes, eps, sigma, modeord)
+    if single:
+        i0, de = plan.fold(points)
+        cs = np.asarray(c)
+        cs = cs[None] if cs.ndim == 1 else cs
+        out = np.empty((cs.shape[0],) + plan.n_modes, dtype=np.complex64)
+        for t in range(cs.shape[0]):
+            B = np.ascontiguousarray(_fft(_spread_f32(plan, i0, de, cs[t]), iflag, workers),
+                                     dtype=np.complex64)
+            _deconv_f32(plan, -1, out[t], B)
+        return out[0] if np.asarray(c).ndim == 1 else out
     c = np.asarray(c)
     single = c.ndim == 1
     cs = c[None] if single else c
@@ -247,24 +322,32 @@ def nufft1(n_modes, c, *points, eps=1e-6, iflag=1, modeord=0, sigma=2.0, workers
     return out[0] if single else out
 
 
-def nufft2(f, *points, eps=1e-6, iflag=-1, modeord=0, sigma=2.0, workers=None):
-    """Type 2 in the user's axis order.  f: (N...) or (T, N...) complex."""
+def nufft2(f, *points, eps=1e-6, iflag=-1, modeord=0, sigma=2.0, workers=None, single=False):
+    """Type 2 in the user's axis order.  f: (N...) or (T, N...) complex.
+    single=True: the single-precision fast path (see nufft1)."""
     workers = workers or _workers()
     d = len(points)
     f = np.asarray(f)
-    single = f.ndim == d
-    fs = f[None] if single else f
+    one = f.ndim == d
+    fs = f[None] if one else f
     plan = Plan(fs.shape[1:], eps, sigma, modeord)
     i0, de = plan.fold(points)
-    fac = plan.deconv_factor()
     outs = []
+    if single:
+        grid = np.empty(plan.nf, dtype=np.complex64)
+        for t in range(fs.shape[0]):
+            _deconv_f32(plan, 1, np.ascontiguousarray(fs[t], dtype=np.complex64), grid)
+            outs.append(_interp_f32(plan, i0, de, _fft(grid, iflag, workers)))
+        out = np.stack(outs)
+        return out[0] if one else out
+    fac = plan.deconv_factor()
     for t in range(fs.shape[0]):
         grid = np.zeros(plan.nf, dtype=np.complex128)
         grid[np.ix_(*plan.idx)] = fs[t] * fac
         b = _fft(grid, iflag, workers)
         outs.append(_interp(list(plan.nf)[::-1], plan.w, plan.beta, i0, de, b))
     out = np.stack(outs)
-    return out[0] if single else out
+    return out[0] if one else out
 
 
 def type3_setup(sources, targets, eps, sigma=2.0):

@@ -448,3 +448,240 @@ int64_t orc_type3_params(double xmin, double xmax, double smin, double smax, dou
   out[2] = sigma * S / ORC_PI;
   return nf;
 }
+
+/* ----------------------------------------------------------------------- */
+/* Single-precision fast path: the timed CPU baseline                       */
+/* ----------------------------------------------------------------------- */
+/* Not a checker: the FP64 routines above are the oracle.  These restate
+ * the CPU method of the paper cited at the top of this file (section 3 of
+ * Barnett, Magland, af Klinteberg 2019) in single precision, as FINUFFT runs
+ * complex64 transforms: kernel values from the piecewise polynomials of
+ * orc_horner_fit evaluated by Horner's rule, points bin-sorted for locality,
+ * each bin spread by one thread into a private padded subgrid that is then
+ * added to the fine grid.  Bins are coloured by the parity of their index
+ * along every axis; bins of one colour are two bins apart, so their
+ * subgrids never overlap when the bin size is at least w - 1 and the adds
+ * need no atomics.  The eight colours run one after another. */
+
+typedef struct {
+  int dim, w, deg;
+  int64_t nf[3], bs[3], nb[3];
+  float coef[ORC_MAX_W * 24]; /* coef[n * w + j]: u^n on piece j (j contiguous) */
+} orc_f32_geom;
+
+static void f32_geom(orc_f32_geom *g, int dim, const int64_t *nf, int w, int deg,
+                     const double *coef) {
+  g->dim = dim;
+  g->w = w;
+  g->deg = deg;
+  for (int d = 0; d < 3; ++d) {
+    g->nf[d] = d < dim ? nf[d] : 1;
+    /* an even number of equal bins of >= max(16, w - 1) cells where the axis
+     * allows (equal bins keep the colouring valid across the periodic wrap),
+     * else one bin */
+    int64_t nb = 1;
+    if (d < dim)
+      for (int64_t k = g->nf[d] / 16; k >= 2; --k)
+        if (k % 2 == 0 && g->nf[d] % k == 0 && g->nf[d] / k >= w - 1) {
+          nb = k;
+          break;
+        }
+    g->nb[d] = nb;
+    g->bs[d] = g->nf[d] / nb;
+  }
+  for (int j = 0; j < w; ++j)
+    for (int n = 0; n <= deg; ++n) g->coef[n * w + j] = (float)coef[j * (deg + 1) + n];
+}
+
+/* All w kernel values of one axis by Horner's rule, the pieces side by
+ * side (the inner loop over pieces vectorises). */
+static inline void f32_kernel(const orc_f32_geom *g, float delta, float *k) {
+  const int w = g->w;
+  const float u = 2.0f * delta - 1.0f;
+  const float *c = g->coef + g->deg * w;
+  for (int j = 0; j < w; ++j) k[j] = c[j];
+  for (int n = g->deg - 1; n >= 0; --n) {
+    c -= w;
+    for (int j = 0; j < w; ++j) k[j] = k[j] * u + c[j];
+  }
+}
+
+static inline int64_t f32_bin(const orc_f32_geom *g, const int64_t *i0) {
+  int64_t b = 0;
+  for (int d = g->dim - 1; d >= 0; --d) b = b * g->nb[d] + wrapi(i0[d], g->nf[d]) / g->bs[d];
+  return b;
+}
+
+/* Counting sort of the points by bin: start[nbins + 1] and perm[M]. */
+static void f32_sort(const orc_f32_geom *g, int64_t M, const int64_t *i0, int64_t *start,
+                     int64_t *perm) {
+  const int64_t nbins = g->nb[0] * g->nb[1] * g->nb[2];
+  int64_t *bin = (int64_t *)malloc(sizeof(int64_t) * (M > 0 ? M : 1));
+  memset(start, 0, sizeof(int64_t) * (nbins + 1));
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < M; ++j) bin[j] = f32_bin(g, i0 + 3 * j);
+  for (int64_t j = 0; j < M; ++j) start[bin[j] + 1]++;
+  for (int64_t b = 0; b < nbins; ++b) start[b + 1] += start[b];
+  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (nbins > 0 ? nbins : 1));
+  memcpy(fill, start, sizeof(int64_t) * nbins);
+  for (int64_t j = 0; j < M; ++j) perm[fill[bin[j]]++] = j;
+  free(fill);
+  free(bin);
+}
+
+/* grid (complex64 interleaved, x fastest) += spread of c (complex64) at the
+ * folded points (i0, delta as float). */
+void orc_spread_f32(int dim, const int64_t *nf, int w, int deg, const double *coef, int64_t M,
+                    const int64_t *i0, const float *delta, const float *c, float *grid) {
+  orc_f32_geom g;
+  f32_geom(&g, dim, nf, w, deg, coef);
+  const int64_t nbins = g.nb[0] * g.nb[1] * g.nb[2];
+  int64_t *start = (int64_t *)malloc(sizeof(int64_t) * (nbins + 1));
+  int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * (M > 0 ? M : 1));
+  f32_sort(&g, M, i0, start, perm);
+  int64_t T[3];
+  for (int d = 0; d < 3; ++d) T[d] = d < dim ? g.bs[d] + w - 1 : 1;
+  const int64_t sub_cells = T[0] * T[1] * T[2];
+  const int ncol = (g.nb[0] > 1 ? 2 : 1) * (g.nb[1] > 1 ? 2 : 1) * (g.nb[2] > 1 ? 2 : 1);
+#pragma omp parallel
+  {
+    float *sub = (float *)malloc(sizeof(float) * 2 * sub_cells);
+    float kv[3][ORC_MAX_W];
+    for (int col = 0; col < ncol; ++col) {
+#pragma omp for schedule(dynamic, 4)
+      for (int64_t b = 0; b < nbins; ++b) {
+        int64_t bc[3] = {b % g.nb[0], (b / g.nb[0]) % g.nb[1], b / (g.nb[0] * g.nb[1])};
+        int cb = 0, m = 1;
+        for (int d = 0; d < 3; ++d)
+          if (g.nb[d] > 1) {
+            cb += (int)(bc[d] & 1) * m;
+            m *= 2;
+          }
+        if (cb != col || start[b + 1] == start[b]) continue;
+        memset(sub, 0, sizeof(float) * 2 * sub_cells);
+        int64_t lo[3];
+        for (int d = 0; d < 3; ++d) lo[d] = bc[d] * g.bs[d];
+        for (int64_t s = start[b]; s < start[b + 1]; ++s) {
+          const int64_t j = perm[s];
+          for (int d = 0; d < 3; ++d) {
+            kv[d][0] = 1.0f;
+            if (d < dim) f32_kernel(&g, delta[3 * j + d], kv[d]);
+          }
+          int64_t o[3];
+          for (int d = 0; d < 3; ++d) o[d] = d < dim ? wrapi(i0[3 * j + d], g.nf[d]) - lo[d] : 0;
+          const float cr = c[2 * j], ci = c[2 * j + 1];
+          const int wy = dim > 1 ? w : 1, wz = dim > 2 ? w : 1;
+          for (int qz = 0; qz < wz; ++qz)
+            for (int qy = 0; qy < wy; ++qy) {
+              const float kyz = kv[1][qy] * kv[2][qz];
+              const float vr = cr * kyz, vi = ci * kyz;
+              float *row = sub + 2 * (((o[2] + qz) * T[1] + (o[1] + qy)) * T[0] + o[0]);
+              for (int qx = 0; qx < w; ++qx) {
+                row[2 * qx] += vr * kv[0][qx];
+                row[2 * qx + 1] += vi * kv[0][qx];
+              }
+            }
+        }
+        /* x: the part before the wrap, then the wrapped part */
+        const int64_t x_run = lo[0] + T[0] <= g.nf[0] ? T[0] : g.nf[0] - lo[0];
+        for (int64_t z = 0; z < T[2]; ++z)
+          for (int64_t y = 0; y < T[1]; ++y) {
+            const int64_t gz = dim > 2 ? wrapi(lo[2] + z, g.nf[2]) : 0;
+            const int64_t gy = dim > 1 ? wrapi(lo[1] + y, g.nf[1]) : 0;
+            float *dst = grid + 2 * ((gz * g.nf[1] + gy) * g.nf[0]);
+            const float *src = sub + 2 * ((z * T[1] + y) * T[0]);
+            float *d0 = dst + 2 * lo[0];
+            for (int64_t x = 0; x < 2 * x_run; ++x) d0[x] += src[x];
+            for (int64_t x = x_run; x < T[0]; ++x) {
+              const int64_t gx = wrapi(lo[0] + x, g.nf[0]);
+              dst[2 * gx] += src[2 * x];
+              dst[2 * gx + 1] += src[2 * x + 1];
+            }
+          }
+      }
+    }
+    free(sub);
+  }
+  free(perm);
+  free(start);
+}
+
+/* c (complex64) = interpolation of grid (complex64) at the folded points,
+ * visited in bin order for locality. */
+void orc_interp_f32(int dim, const int64_t *nf, int w, int deg, const double *coef, int64_t M,
+                    const int64_t *i0, const float *delta, const float *grid, float *c) {
+  orc_f32_geom g;
+  f32_geom(&g, dim, nf, w, deg, coef);
+  const int64_t nbins = g.nb[0] * g.nb[1] * g.nb[2];
+  int64_t *start = (int64_t *)malloc(sizeof(int64_t) * (nbins + 1));
+  int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * (M > 0 ? M : 1));
+  f32_sort(&g, M, i0, start, perm);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t s = 0; s < M; ++s) {
+    const int64_t j = perm[s];
+    float kv[3][ORC_MAX_W];
+    for (int d = 0; d < 3; ++d) {
+      kv[d][0] = 1.0f;
+      if (d < dim) f32_kernel(&g, delta[3 * j + d], kv[d]);
+    }
+    const int wy = dim > 1 ? w : 1, wz = dim > 2 ? w : 1;
+    int64_t gx[ORC_MAX_W];
+    for (int q = 0; q < w; ++q) gx[q] = 2 * wrapi(i0[3 * j] + q, g.nf[0]);
+    float sr = 0.0f, si = 0.0f;
+    for (int qz = 0; qz < wz; ++qz) {
+      const int64_t gz = dim > 2 ? wrapi(i0[3 * j + 2] + qz, g.nf[2]) : 0;
+      for (int qy = 0; qy < wy; ++qy) {
+        const int64_t gy = dim > 1 ? wrapi(i0[3 * j + 1] + qy, g.nf[1]) : 0;
+        const float *row = grid + 2 * ((gz * g.nf[1] + gy) * g.nf[0]);
+        float rr = 0.0f, ri = 0.0f;
+        for (int qx = 0; qx < w; ++qx) {
+          rr += row[gx[qx]] * kv[0][qx];
+          ri += row[gx[qx] + 1] * kv[0][qx];
+        }
+        const float kyz = kv[1][qy] * kv[2][qz];
+        sr += rr * kyz;
+        si += ri * kyz;
+      }
+    }
+    c[2 * j] = sr;
+    c[2 * j + 1] = si;
+  }
+  free(perm);
+  free(start);
+}
+
+/* Deconvolution between the modes and the fine grid, single precision.
+ * Modes f (complex64, user axis order = backend reversed: x fastest) of
+ * n[0] x n[1] x n[2] entries; fine grid of nf[0] x nf[1] x nf[2]; mode k of
+ * axis d (storage index i) sits at grid index idx_d[i] and is scaled by
+ * fac_d[i].  dir = 1: grid = 0 except grid[idx] = f * fac (type 2);
+ * dir = -1: f = grid[idx] * fac (type 1). */
+void orc_deconv_f32(int dir, int dim, const int64_t *n, const int64_t *nf, const int64_t *idx0,
+                    const int64_t *idx1, const int64_t *idx2, const float *fac0,
+                    const float *fac1, const float *fac2, float *f, float *grid) {
+  const int64_t n1 = dim > 1 ? n[1] : 1, n2 = dim > 2 ? n[2] : 1;
+  const int64_t g1 = dim > 1 ? nf[1] : 1, g2 = dim > 2 ? nf[2] : 1;
+  if (dir > 0) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < g1 * g2; ++r) memset(grid + 2 * r * nf[0], 0, sizeof(float) * 2 * nf[0]);
+  }
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int64_t k2 = 0; k2 < n2; ++k2)
+    for (int64_t k1 = 0; k1 < n1; ++k1) {
+      const float s = (dim > 2 ? fac2[k2] : 1.0f) * (dim > 1 ? fac1[k1] : 1.0f);
+      const int64_t grow = ((dim > 2 ? idx2[k2] : 0) * g1 + (dim > 1 ? idx1[k1] : 0)) * nf[0];
+      float *fr = f + 2 * ((k2 * n1 + k1) * n[0]);
+      float *gr = grid + 2 * grow;
+      for (int64_t k0 = 0; k0 < n[0]; ++k0) {
+        const float a = s * fac0[k0];
+        const int64_t gi = 2 * idx0[k0];
+        if (dir > 0) {
+          gr[gi] = fr[2 * k0] * a;
+          gr[gi + 1] = fr[2 * k0 + 1] * a;
+        } else {
+          fr[2 * k0] = gr[gi] * a;
+          fr[2 * k0 + 1] = gr[gi + 1] * a;
+        }
+      }
+    }
+}

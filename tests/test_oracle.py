@@ -198,3 +198,23 @@ def test_fold_edges(cn):
     assert cn.lib().orc_fold(float("inf"), nf) == 0.0
     assert 0.0 <= cn.lib().orc_fold(1e300, nf) < nf
     assert 0.0 <= cn.lib().orc_fold(-1e-300, nf) < nf
+
+
+@pytest.mark.parametrize("shape", [(40,), (33, 20), (20, 17, 24), (64, 64, 64)])
+@pytest.mark.parametrize("mo", [0, 1])
+def test_single_precision_path_matches_fp64(cn, shape, mo):
+    """The timed CPU baseline (single-precision fast path: Horner kernel,
+    coloured bin subgrids, complex64 FFT) against the FP64 oracle on the same
+    points: agreement to single-precision round-off."""
+    rng = np.random.default_rng(len(shape) + 10 * mo)
+    M = 5000
+    x = [np.concatenate([rng.uniform(-np.pi, np.pi, M // 2), rng.normal(0, 0.1, M - M // 2)])
+         for _ in shape]
+    c = rng.normal(size=M) + 1j * rng.normal(size=M)
+    f = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    a = cn.nufft1(shape, c, *x, eps=1e-5, iflag=1, modeord=mo, single=True)
+    assert a.dtype == np.complex64
+    assert rel_l2(a, cn.nufft1(shape, c, *x, eps=1e-5, iflag=1, modeord=mo)) < 2e-6
+    b = cn.nufft2(f, *x, eps=1e-5, iflag=-1, modeord=mo, single=True)
+    assert b.dtype == np.complex64
+    assert rel_l2(b, cn.nufft2(f, *x, eps=1e-5, iflag=-1, modeord=mo)) < 2e-6
