@@ -68,7 +68,17 @@ typedef struct gbn_opts {
   int gpu_autotune;       /* batched plans: 0 off; GBN_TUNE_ON (| GBN_TUNE_SM_ONLY,
                              | GBN_TUNE_KEEP_SIGMA) picks each problem's settings with
                              gbn_autotune.  Ignored by the plan and one-shot entry points. */
+  int gpu_kernel;         /* spreading kernel shape, same width rule either way:
+                             GBN_KERNEL_ES (0, default) the exponential of semicircle of
+                             FINUFFT, beta = 2.30 w at sigma = 2;
+                             GBN_KERNEL_KB (1) Kaiser-Bessel I0(beta sqrt(1-z^2)) / I0(beta),
+                             beta = pi sqrt((w/sigma)^2 (sigma-1/2)^2 - 0.8) (Beatty,
+                             Nishimura, Pauly, IEEE TMI 2005): 1.5-2.5x smaller aliasing
+                             error at the same width and cost. */
 } gbn_opts;
+
+#define GBN_KERNEL_ES 0
+#define GBN_KERNEL_KB 1
 
 #define GBN_TUNE_ON 1         /* tune sigma, method, bin size and points per subproblem */
 #define GBN_TUNE_SM_ONLY 2    /* only the shared-memory method (keeps batches on the work queue) */

@@ -15,6 +15,8 @@
 #include <cuda.h>  // CUtensorMap (a plain struct; the encoder is resolved at run time)
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -119,7 +121,30 @@ struct KerSpec {
   int deg;
   int meth;
   T beta;
+  int shape;   // GBN_KERNEL_ES or GBN_KERNEL_KB (direct formula when meth == 0)
+  T inv_i0b;   // 1 / I0(beta) for the Kaiser-Bessel shape
 };
+
+// Modified Bessel function I0 by its power series sum_k ((x/2)^2k / (k!)^2):
+// every term is positive, so the sum keeps full relative precision (host).
+inline double bessel_i0(double x) {
+  const double q = 0.25 * x * x;
+  double term = 1.0, sum = 1.0;
+  for (int k = 1; k < 500; ++k) {
+    term *= q / ((double)k * (double)k);
+    sum += term;
+    if (term < 1e-17 * sum) break;
+  }
+  return sum;
+}
+
+// Kernel shape as a function of s = sqrt(1 - z^2) in [0, 1], z = 2t/w
+// (host): exp(beta (s - 1)) for the exponential of semicircle, I0(beta s) /
+// I0(beta) for Kaiser-Bessel.
+inline double kernel_of_s(int shape, double beta, double s) {
+  if (shape == 1) return bessel_i0(beta * s) / bessel_i0(beta);
+  return std::exp(beta * (s - 1.0));
+}
 
 // Device-side sort state produced by setpts.
 struct SortState {
@@ -284,6 +309,7 @@ cudaError_t launch_t3_prephase_factors(int dim, int64_t M, const TX* const* x, c
 template <typename TX, typename TC>
 cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
                                    const double* const* tau, int iflag, int w, double beta,
+                                   int shape,
                                    void* fac, cudaStream_t s, double tau_max = 0.0);
 
 // Gradient grids: for every transform, E fine grids from its modes `in`

@@ -33,8 +33,12 @@ __device__ __forceinline__ void load_coef(T (&co)[NCO], const KerSpec<T>& ks, in
     co[n] = (piece < w && n <= ks.deg) ? ks.coef[piece * (ks.deg + 1) + n] : T(0);
 }
 
+__device__ __forceinline__ float bessel_i0_dev(float x) { return cyl_bessel_i0f(x); }
+__device__ __forceinline__ double bessel_i0_dev(double x) { return cyl_bessel_i0(x); }
+
 // Kernel value of piece `piece` at offset delta in [0, 1): Horner in
-// u = 2*delta - 1, or the direct formula exp(beta*(sqrt(1-z^2)-1)).
+// u = 2*delta - 1, or the direct formula: exp(beta*(sqrt(1-z^2)-1)), or
+// I0(beta*sqrt(1-z^2)) / I0(beta) for the Kaiser-Bessel shape.
 template <typename T, int NCO>
 __device__ __forceinline__ T kerval(const T (&co)[NCO], const KerSpec<T>& ks, T delta, int piece,
                                     int w) {
@@ -43,7 +47,9 @@ __device__ __forceinline__ T kerval(const T (&co)[NCO], const KerSpec<T>& ks, T 
     const T t = (T)piece - T(0.5) * (T)w + delta;
     const T z = t * (T(2) / (T)w);
     const T s = T(1) - z * z;
-    return s > T(0) ? exp(ks.beta * (sqrt(s) - T(1))) : T(0);
+    if (!(s > T(0))) return T(0);
+    if (ks.shape == 1) return bessel_i0_dev(ks.beta * sqrt(s)) * ks.inv_i0b;
+    return exp(ks.beta * (sqrt(s) - T(1)));
   }
   const T u = T(2) * delta - T(1);
   T v = T(0);

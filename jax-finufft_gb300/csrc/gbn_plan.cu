@@ -93,9 +93,11 @@ int64_t next235even(int64_t n0) {
   }
 }
 
-// Width w and shape beta of the ES kernel for tolerance eps; returns 1 when
-// the width is clamped at kMaxW.
-int kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
+// Width w and shape parameter beta for tolerance eps; returns 1 when the
+// width is clamped at kMaxW.  The width rule is the published one for the
+// exponential of semicircle (shape 0) and is kept for Kaiser-Bessel (shape
+// 1), whose beta follows Beatty, Nishimura and Pauly (IEEE TMI 2005).
+int kernel_params(double eps, double sigma, int shape, int* w_out, double* beta_out) {
   int warn = 0;
   double a = (sigma == 2.0) ? -std::log10(eps / 10.0)
                             : -std::log(eps) / (kPi * std::sqrt(1.0 - 1.0 / sigma));
@@ -120,6 +122,10 @@ int kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
   }
   *w_out = w;
   *beta_out = ratio * (double)w;
+  if (shape == 1) {
+    const double a = ((double)w / sigma) * (sigma - 0.5);
+    *beta_out = kPi * std::sqrt(std::max(a * a - 0.8, 0.25));
+  }
   return warn;
 }
 
@@ -129,15 +135,15 @@ int64_t fine_size(int64_t n, double sigma, int w) {
   return next235even(m);
 }
 
-double es_kernel(double t, int w, double beta) {
+double kernel_value(double t, int w, double beta, int shape) {
   const double z = 2.0 * t / (double)w;
   const double s = 1.0 - z * z;
-  return s < 0.0 ? 0.0 : std::exp(beta * (std::sqrt(s) - 1.0));
+  return s < 0.0 ? 0.0 : kernel_of_s(shape, beta, std::sqrt(s));
 }
 
 // Chebyshev interpolation of each unit piece at degree deg, as monomials in
 // u = 2*delta - 1.
-void horner_fit(int w, double beta, int deg, std::vector<double>& coef) {
+void horner_fit(int w, double beta, int shape, int deg, std::vector<double>& coef) {
   const int n1 = deg + 1;
   std::vector<double> node(n1), val(n1), cheb(n1);
   std::vector<std::vector<double>> tk(n1, std::vector<double>(n1, 0.0));
@@ -148,7 +154,8 @@ void horner_fit(int w, double beta, int deg, std::vector<double>& coef) {
     for (int n = 0; n < n1; ++n) tk[k][n] = (n ? 2.0 * tk[k - 1][n - 1] : 0.0) - tk[k - 2][n];
   coef.assign((size_t)w * n1, 0.0);
   for (int j = 0; j < w; ++j) {
-    for (int i = 0; i < n1; ++i) val[i] = es_kernel(j - 0.5 * w + 0.5 * (node[i] + 1.0), w, beta);
+    for (int i = 0; i < n1; ++i)
+      val[i] = kernel_value(j - 0.5 * w + 0.5 * (node[i] + 1.0), w, beta, shape);
     for (int k = 0; k < n1; ++k) {
       double s = 0.0;
       for (int i = 0; i < n1; ++i) s += val[i] * std::cos(kPi * k * (i + 0.5) / n1);
@@ -192,7 +199,8 @@ void gauss_legendre(int q, double* x, double* wt) {
 }
 
 // psihat(omega) = int psi(t) cos(omega t) dt, t = (w/2) sin(theta) substitution.
-void kernel_ft(int w, double beta, const std::vector<double>& omega, std::vector<double>& out) {
+void kernel_ft(int w, double beta, int shape, const std::vector<double>& omega,
+               std::vector<double>& out) {
   const int q = 2 * w + 10;
   double xg[64], wg[64], tq[64], fq[64];
   gauss_legendre(q, xg, wg);
@@ -200,7 +208,7 @@ void kernel_ft(int w, double beta, const std::vector<double>& omega, std::vector
     const double th = (xg[i] + 1.0) * kPi / 4.0;
     const double wt = wg[i] * kPi / 4.0;
     tq[i] = 0.5 * w * std::sin(th);
-    fq[i] = 2.0 * wt * std::exp(beta * (std::cos(th) - 1.0)) * 0.5 * w * std::cos(th);
+    fq[i] = 2.0 * wt * kernel_of_s(shape, beta, std::cos(th)) * 0.5 * w * std::cos(th);
   }
   out.resize(omega.size());
   for (size_t k = 0; k < omega.size(); ++k) {
@@ -494,7 +502,7 @@ int setup_phi(gbn_plan_s* p) {
     for (int64_t i = 0; i < p->N[d]; ++i)
       om[(size_t)i] = 2.0 * kPi * (double)mode_freq(i, p->N[d], p->opts.modeord) / (double)p->nf[d];
     std::vector<double> ph;
-    kernel_ft(p->w, p->beta, om, ph);
+    kernel_ft(p->w, p->beta, p->opts.gpu_kernel, om, ph);
     for (auto& v : ph) v = 1.0 / v;
     GBN_TRY(upload_doubles_as(ph, p->comp_single, p->phi[d], p->stream));
   }
@@ -518,7 +526,7 @@ int setup_fft_own(gbn_plan_s* p) {
 
 int setup_kernel_coef(gbn_plan_s* p) {
   std::vector<double> coef;
-  horner_fit(p->w, p->beta, p->deg, coef);
+  horner_fit(p->w, p->beta, p->opts.gpu_kernel, p->deg, coef);
   return upload_doubles_as(coef, p->comp_single, p->coef, p->stream);
 }
 
@@ -679,7 +687,9 @@ int plan_create(int type, int dim, const int64_t* nmodes, int iflag, int ntransf
     e = 1e-7;
     warn = 1;
   }
-  warn |= kernel_params(e, p->sigma, &p->w, &p->beta);
+  if (p->opts.gpu_kernel != 0 && p->opts.gpu_kernel != 1)
+    return fail(GBN_ERR_ARGS, "gpu_kernel must be 0 (exponential of semicircle) or 1 (Kaiser-Bessel)");
+  warn |= kernel_params(e, p->sigma, p->opts.gpu_kernel, &p->w, &p->beta);
   p->warn = warn;
   p->deg = p->w + 2;
   if (type != 3) {
@@ -911,14 +921,16 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
       GBN_CUDA((launch_t3_prephase_factors<TX, float>(p->dim, M, xs, p->t3_cx, p->t3_cs,
                                                        p->iflag, p->t3_pre.p, st)));
       GBN_CUDA((launch_t3_post_factors<TX, float>(p->dim, N, ss, p->t3_cx, ctaus, p->iflag,
-                                                   p->w, p->beta, p->t3_post.p, st, tau_max)));
+                                                   p->w, p->beta, p->opts.gpu_kernel,
+                                                   p->t3_post.p, st, tau_max)));
     } else {
       GBN_CUDA((launch_t3_prephase_factors<double, double>(p->dim, M, (const double* const*)xs,
                                                            p->t3_cx, p->t3_cs, p->iflag,
                                                            p->t3_pre.p, st)));
       GBN_CUDA((launch_t3_post_factors<double, double>(p->dim, N, (const double* const*)ss,
                                                        p->t3_cx, ctaus, p->iflag, p->w,
-                                                       p->beta, p->t3_post.p, st, tau_max)));
+                                                       p->beta, p->opts.gpu_kernel,
+                                                       p->t3_post.p, st, tau_max)));
     }
   }
   if (sev) GBN_CUDA(cudaEventRecord(sev[1], st));
@@ -932,6 +944,8 @@ KerSpec<TC> ker_spec(gbn_plan_s* p) {
   ks.deg = p->deg;
   ks.meth = p->opts.gpu_kerevalmeth != 0 ? 1 : 0;
   ks.beta = (TC)p->beta;
+  ks.shape = p->opts.gpu_kernel;
+  ks.inv_i0b = (TC)(1.0 / bessel_i0(p->beta));
   return ks;
 }
 
@@ -1236,7 +1250,7 @@ struct CacheKey {
            a.gpu_maxbatchsize == b.gpu_maxbatchsize && a.debug == b.debug &&
            a.gpu_binsizex == b.gpu_binsizex && a.gpu_binsizey == b.gpu_binsizey &&
            a.gpu_binsizez == b.gpu_binsizez && a.gpu_maxsubprobsize == b.gpu_maxsubprobsize &&
-           a.gpu_precision == b.gpu_precision;
+           a.gpu_precision == b.gpu_precision && a.gpu_kernel == b.gpu_kernel;
   }
 };
 
@@ -1376,6 +1390,7 @@ void gbn_default_opts(gbn_opts* o) {
   o->debug = 0;
   o->gpu_maxsubprobsize = 1024;
   o->gpu_precision = 0;
+  o->gpu_kernel = 0;
 }
 
 const char* gbn_last_error(void) { return g_err.c_str(); }

@@ -1077,7 +1077,7 @@ bool fit_psihat(const Quad& qd, double tau_max, double rel_tol, int D, std::vect
 template <typename TX, typename TC>
 cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
                                    const double* const* tau, int iflag, int w, double beta,
-                                   void* fac, cudaStream_t s, double tau_max) {
+                                   int shape, void* fac, cudaStream_t s, double tau_max) {
   if (N == 0) return cudaSuccess;
   const double pi = 3.141592653589793238462643383279502884;
   Quad qd;
@@ -1088,7 +1088,7 @@ cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, cons
     const double th = (xg[i] + 1.0) * pi / 4.0;
     const double wt = wg[i] * pi / 4.0;
     qd.t[i] = 0.5 * w * sin(th);
-    qd.f[i] = 2.0 * wt * exp(beta * (cos(th) - 1.0)) * 0.5 * w * cos(th);
+    qd.f[i] = 2.0 * wt * kernel_of_s(shape, beta, cos(th)) * 0.5 * w * cos(th);
   }
   Ptrs3 sp{};
   CDPtrs3 tp{};
@@ -1181,8 +1181,8 @@ template cudaError_t launch_t3_targets<double>(int, int64_t, const double* const
                                                           void*, cudaStream_t);                \
   template cudaError_t launch_t3_post_factors<TX, TC>(int, int64_t, const TX* const*,          \
                                                       const double*, const double* const*,     \
-                                                      int, int, double, void*, cudaStream_t,   \
-                                                      double);
+                                                      int, int, double, int, void*,            \
+                                                      cudaStream_t, double);
 GBN_INST_T3(float, float)
 GBN_INST_T3(double, float)
 GBN_INST_T3(double, double)

@@ -189,10 +189,11 @@ std::string class_key(int type, int dim, bool single, const int64_t* nm, int64_t
   while (lg < 62 && ((int64_t)1 << lg) < std::max<int64_t>(M, 1)) ++lg;
   char buf[512];
   std::snprintf(buf, sizeof(buf),
-                "v1 %s t%d d%d s%d n%lldx%lldx%lld m2^%d T%d e%.3g p%d k%d sig%.3g gm%d",
+                "v1 %s t%d d%d s%d n%lldx%lldx%lld m2^%d T%d e%.3g p%d k%d sig%.3g gm%d%s",
                 gpu.c_str(), type, dim, single ? 1 : 0, (long long)nm[0],
                 (long long)(dim > 1 ? nm[1] : 1), (long long)(dim > 2 ? nm[2] : 1), lg, T, eps,
-                base.gpu_precision, base.gpu_kerevalmeth, sigma_fixed, allow_gm ? 1 : 0);
+                base.gpu_precision, base.gpu_kerevalmeth, sigma_fixed, allow_gm ? 1 : 0,
+                base.gpu_kernel == 1 ? " kb" : "");
   return buf;
 }
 

@@ -44,6 +44,7 @@ class GbnOpts(ctypes.Structure):
         ("gpu_maxsubprobsize", ctypes.c_int),
         ("gpu_precision", ctypes.c_int),
         ("gpu_autotune", ctypes.c_int),
+        ("gpu_kernel", ctypes.c_int),
     ]
 
 

@@ -8,8 +8,9 @@ equality, hashing and keyword construction identical.  Only the GPU fields
 and ``modeord`` reach the GB300 engine (as in ``to_cufinufft_opts``,
 options.py:105-119), plus the bin-size / subproblem fields that the reference
 carries but never forwards, and the engine's own fields: ``gpu_precision`` (compute precision; 0 = the
-data's, the reference behaviour), ``gpu_fused_adjoint`` and
-``gpu_autotune``.
+data's, the reference behaviour), ``gpu_fused_adjoint``, ``gpu_autotune`` and
+``gpu_kernel`` (spreading kernel shape: 0 the exponential of semicircle, the
+reference's; 1 Kaiser-Bessel, more accurate at the same width).
 """
 from dataclasses import dataclass
 from enum import IntEnum
@@ -52,6 +53,11 @@ class SpreadThread(IntEnum):
     Auto = 0
     Sequential = 1
     Parallel = 2
+
+
+class GpuKernel(IntEnum):
+    ExponentialOfSemicircle = 0
+    KaiserBessel = 1
 
 
 class GpuMethod(IntEnum):
@@ -109,6 +115,9 @@ class Opts:
     # types 1/2: look up (or tune, on a cache miss) sigma, method, bin sizes
     # and points per subproblem for each call's class (see tune.py)
     gpu_autotune: bool = False
+    # spreading kernel: 0 exponential of semicircle (FINUFFT's), 1 Kaiser-Bessel
+    # (same width rule and cost, 1.5-2.5x smaller aliasing error)
+    gpu_kernel: GpuKernel = 0
 
     def __post_init__(self):
         if int(self.modeord) not in (0, 1):
@@ -119,6 +128,8 @@ class Opts:
             raise ValueError("gpu_method must be 0, 1 or 2")
         if int(self.gpu_precision) not in (0, 1, 2, 3):
             raise ValueError("gpu_precision must be 0..3")
+        if int(self.gpu_kernel) not in (0, 1):
+            raise ValueError("gpu_kernel must be 0 (exponential of semicircle) or 1 (Kaiser-Bessel)")
         if self.gpu_spreadinterponly:
             raise ValueError("gpu_spreadinterponly is not supported")
 
@@ -187,4 +198,5 @@ def to_native(opts):
     n.gpu_binsizez = int(o.gpu_binsizez)
     n.gpu_maxsubprobsize = int(o.gpu_maxsubprobsize)
     n.gpu_precision = int(o.gpu_precision)
+    n.gpu_kernel = int(o.gpu_kernel)
     return n

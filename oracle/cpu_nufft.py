@@ -43,13 +43,14 @@ def lib():
         L.orc_next235even.restype = ctypes.c_int64
         L.orc_next235even.argtypes = [ctypes.c_int64]
         L.orc_kernel_params.restype = ctypes.c_int
-        L.orc_kernel_params.argtypes = [ctypes.c_double, ctypes.c_double, _ip, _dp]
+        L.orc_kernel_params.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _ip, _dp]
         L.orc_fine_size.restype = ctypes.c_int64
         L.orc_fine_size.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_int]
         L.orc_kernel.restype = ctypes.c_double
-        L.orc_kernel.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_kernel.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.orc_kernel_ft.restype = None
-        L.orc_kernel_ft.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int64, _dp, _dp]
+        L.orc_kernel_ft.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int64,
+                                    _dp, _dp]
         L.orc_fold.restype = ctypes.c_double
         L.orc_fold.argtypes = [ctypes.c_double, ctypes.c_int64]
         L.orc_fold_points.restype = None
@@ -57,10 +58,10 @@ def lib():
                                       ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _i64p, _dp,
                                       _i64p]
         L.orc_spread.restype = None
-        L.orc_spread.argtypes = [ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_double,
+        L.orc_spread.argtypes = [ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int64, _i64p, _dp, _dp, _dp]
         L.orc_interp.restype = None
-        L.orc_interp.argtypes = [ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_double,
+        L.orc_interp.argtypes = [ctypes.c_int, _i64p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int64, _i64p, _dp, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         for name in ("orc_spread_f32", "orc_interp_f32"):
@@ -72,7 +73,8 @@ def lib():
         L.orc_deconv_f32.argtypes = [ctypes.c_int, ctypes.c_int, _i64p, _i64p, _i64p, _i64p,
                                      _i64p, _fp, _fp, _fp, _fp, _fp]
         L.orc_horner_fit.restype = None
-        L.orc_horner_fit.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]
+        L.orc_horner_fit.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                     _dp]
         L.orc_type3_params.restype = ctypes.c_int64
         L.orc_type3_params.argtypes = [ctypes.c_double] * 5 + [ctypes.c_int, _dp]
         L.orc_num_threads.restype = ctypes.c_int
@@ -97,11 +99,13 @@ def num_threads():
 # plan-time parameters
 # --------------------------------------------------------------------------
 
-def kernel_params(eps, sigma=2.0):
-    """(w, beta, warn) for tolerance eps at upsampling factor sigma."""
+def kernel_params(eps, sigma=2.0, shape=0):
+    """(w, beta, warn) for tolerance eps at upsampling factor sigma; shape 0
+    the exponential of semicircle, 1 Kaiser-Bessel."""
     w = ctypes.c_int()
     b = ctypes.c_double()
-    warn = lib().orc_kernel_params(float(eps), float(sigma), ctypes.byref(w), ctypes.byref(b))
+    warn = lib().orc_kernel_params(float(eps), float(sigma), int(shape), ctypes.byref(w),
+                                   ctypes.byref(b))
     return w.value, b.value, int(warn)
 
 
@@ -113,20 +117,21 @@ def next235even(n):
     return int(lib().orc_next235even(int(n)))
 
 
-def kernel(t, w, beta):
-    return np.array([lib().orc_kernel(float(x), int(w), float(beta)) for x in np.ravel(t)])
+def kernel(t, w, beta, shape=0):
+    return np.array([lib().orc_kernel(float(x), int(w), float(beta), int(shape))
+                     for x in np.ravel(t)])
 
 
-def kernel_ft(w, beta, omega):
+def kernel_ft(w, beta, omega, shape=0):
     om = np.ascontiguousarray(np.ravel(omega), dtype=np.float64)
     out = np.empty_like(om)
-    lib().orc_kernel_ft(int(w), float(beta), om.size, _p(om, _dp), _p(out, _dp))
+    lib().orc_kernel_ft(int(w), float(beta), int(shape), om.size, _p(om, _dp), _p(out, _dp))
     return out.reshape(np.shape(omega))
 
 
-def horner_fit(w, beta, deg):
+def horner_fit(w, beta, deg, shape=0):
     coef = np.empty(w * (deg + 1))
-    lib().orc_horner_fit(int(w), float(beta), int(deg), _p(coef, _dp))
+    lib().orc_horner_fit(int(w), float(beta), int(shape), int(deg), _p(coef, _dp))
     return coef.reshape(w, deg + 1)
 
 
@@ -168,26 +173,28 @@ def fold_points(coords_b, nf_b, w, binsize_b=(1, 1, 1), mode=0, center_b=None, s
     return X, i0, de, b
 
 
-def _spread(nf_b, w, beta, i0, de, c):
+def _spread(nf_b, w, beta, i0, de, c, shape=0):
     dim = len(nf_b)
     nf = np.ones(3, dtype=np.int64)
     nf[:dim] = nf_b
     grid = np.zeros(int(np.prod(nf_b)), dtype=np.complex128)
     cc = np.ascontiguousarray(c, dtype=np.complex128)
-    lib().orc_spread(dim, _p(nf, _i64p), int(w), float(beta), cc.shape[0], _p(i0, _i64p),
+    lib().orc_spread(dim, _p(nf, _i64p), int(w), float(beta), int(shape), cc.shape[0],
+                     _p(i0, _i64p),
                      _p(de, _dp), cc.view(np.float64).ctypes.data_as(_dp),
                      grid.view(np.float64).ctypes.data_as(_dp))
     return grid.reshape(tuple(nf_b[::-1]))
 
 
-def _interp(nf_b, w, beta, i0, de, grid):
+def _interp(nf_b, w, beta, i0, de, grid, shape=0):
     dim = len(nf_b)
     nf = np.ones(3, dtype=np.int64)
     nf[:dim] = nf_b
     g = np.ascontiguousarray(grid, dtype=np.complex128).ravel()
     M = i0.shape[0]
     out = np.empty(M, dtype=np.complex128)
-    lib().orc_interp(dim, _p(nf, _i64p), int(w), float(beta), M, _p(i0, _i64p), _p(de, _dp),
+    lib().orc_interp(dim, _p(nf, _i64p), int(w), float(beta), int(shape), M, _p(i0, _i64p),
+                     _p(de, _dp),
                      g.view(np.float64).ctypes.data_as(_dp),
                      out.view(np.float64).ctypes.data_as(_dp))
     return out
@@ -215,16 +222,17 @@ def _workers():
 class Plan:
     """Plan-time quantities for types 1/2 in the user's axis order."""
 
-    def __init__(self, n_modes, eps, sigma=2.0, modeord=0):
+    def __init__(self, n_modes, eps, sigma=2.0, modeord=0, kernel=0):
         self.n_modes = tuple(int(n) for n in n_modes)
         self.dim = len(self.n_modes)
-        self.w, self.beta, self.warn = kernel_params(eps, sigma)
+        self.shape = int(kernel)
+        self.w, self.beta, self.warn = kernel_params(eps, sigma, self.shape)
         self.sigma = sigma
         self.modeord = modeord
         self.nf = tuple(fine_size(n, sigma, self.w) for n in self.n_modes)
         self.ks = [frequencies(n, modeord) for n in self.n_modes]
         self.idx = [np.mod(k, nf) for k, nf in zip(self.ks, self.nf)]
-        self.phihat = [kernel_ft(self.w, self.beta, 2 * np.pi * k / nf)
+        self.phihat = [kernel_ft(self.w, self.beta, 2 * np.pi * k / nf, self.shape)
                        for k, nf in zip(self.ks, self.nf)]
 
     def deconv_factor(self):
@@ -241,7 +249,7 @@ class Plan:
 def _f32_args(plan, i0, de):
     """Arguments of the single-precision C routines for plan's geometry."""
     deg = plan.w + 2
-    coef = np.ascontiguousarray(horner_fit(plan.w, plan.beta, deg).ravel())
+    coef = np.ascontiguousarray(horner_fit(plan.w, plan.beta, deg, plan.shape).ravel())
     nf = np.ones(3, dtype=np.int64)
     nf[:plan.dim] = list(plan.nf)[::-1]
     return (plan.dim, _p(nf, _i64p), plan.w, deg, _p(coef, _dp), i0.shape[0], _p(i0, _i64p),
@@ -290,14 +298,15 @@ def _deconv_f32(plan, direction, f, grid):
 
 
 def nufft1(n_modes, c, *points, eps=1e-6, iflag=1, modeord=0, sigma=2.0, workers=None,
-           single=False):
+           single=False, kernel=0):
     """Type 1 in the user's axis order.  c: (M,) or (T, M) complex.
 
     single=True runs the single-precision fast path (complex64 throughout,
     kernel by Horner's rule, bin-sorted private subgrids): the timed CPU
-    baseline, not the checker."""
+    baseline, not the checker.  kernel: 0 the exponential of semicircle, 1
+    Kaiser-Bessel."""
     workers = workers or _workers()
-    plan = Plan(n_modes, eps, sigma, modeord)
+    plan = Plan(n_modes, eps, sigma, modeord, kernel)
     if single:
         i0, de = plan.fold(points)
         cs = np.asarray(c)
@@ -315,14 +324,15 @@ def nufft1(n_modes, c, *points, eps=1e-6, iflag=1, modeord=0, sigma=2.0, workers
     fac = plan.deconv_factor()
     outs = []
     for t in range(cs.shape[0]):
-        grid = _spread(list(plan.nf)[::-1], plan.w, plan.beta, i0, de, cs[t])
+        grid = _spread(list(plan.nf)[::-1], plan.w, plan.beta, i0, de, cs[t], plan.shape)
         B = _fft(grid, iflag, workers)
         outs.append(B[np.ix_(*plan.idx)] * fac)
     out = np.stack(outs)
     return out[0] if single else out
 
 
-def nufft2(f, *points, eps=1e-6, iflag=-1, modeord=0, sigma=2.0, workers=None, single=False):
+def nufft2(f, *points, eps=1e-6, iflag=-1, modeord=0, sigma=2.0, workers=None, single=False,
+           kernel=0):
     """Type 2 in the user's axis order.  f: (N...) or (T, N...) complex.
     single=True: the single-precision fast path (see nufft1)."""
     workers = workers or _workers()
@@ -330,7 +340,7 @@ def nufft2(f, *points, eps=1e-6, iflag=-1, modeord=0, sigma=2.0, workers=None, s
     f = np.asarray(f)
     one = f.ndim == d
     fs = f[None] if one else f
-    plan = Plan(fs.shape[1:], eps, sigma, modeord)
+    plan = Plan(fs.shape[1:], eps, sigma, modeord, kernel)
     i0, de = plan.fold(points)
     outs = []
     if single:
@@ -345,14 +355,14 @@ def nufft2(f, *points, eps=1e-6, iflag=-1, modeord=0, sigma=2.0, workers=None, s
         grid = np.zeros(plan.nf, dtype=np.complex128)
         grid[np.ix_(*plan.idx)] = fs[t] * fac
         b = _fft(grid, iflag, workers)
-        outs.append(_interp(list(plan.nf)[::-1], plan.w, plan.beta, i0, de, b))
+        outs.append(_interp(list(plan.nf)[::-1], plan.w, plan.beta, i0, de, b, plan.shape))
     out = np.stack(outs)
     return out[0] if one else out
 
 
-def type3_setup(sources, targets, eps, sigma=2.0):
+def type3_setup(sources, targets, eps, sigma=2.0, kernel=0):
     """Per-dimension type-3 parameters in the user's axis order."""
-    w, beta, warn = kernel_params(eps, sigma)
+    w, beta, warn = kernel_params(eps, sigma, kernel)
     prm = []
     for x, s in zip(sources, targets):
         x = np.asarray(x, dtype=np.float64)
@@ -361,7 +371,7 @@ def type3_setup(sources, targets, eps, sigma=2.0):
     return w, beta, prm
 
 
-def nufft3(c, *points, eps=1e-6, iflag=-1, sigma=2.0, workers=None):
+def nufft3(c, *points, eps=1e-6, iflag=-1, sigma=2.0, workers=None, kernel=0):
     """Type 3 in the user's axis order: points = sources..., targets...."""
     workers = workers or _workers()
     d = len(points) // 2
@@ -370,7 +380,7 @@ def nufft3(c, *points, eps=1e-6, iflag=-1, sigma=2.0, workers=None):
     c = np.asarray(c)
     single = c.ndim == 1
     cs = c[None] if single else c
-    w, beta, prm = type3_setup(xs, ss, eps, sigma)
+    w, beta, prm = type3_setup(xs, ss, eps, sigma, kernel)
     nf = [p[0] for p in prm]
     cen = [p[1] for p in prm]
     tcen = [p[2] for p in prm]
@@ -383,12 +393,12 @@ def nufft3(c, *points, eps=1e-6, iflag=-1, sigma=2.0, workers=None):
     taus = [(s - tc) / sc for s, tc, sc in zip(ss, tcen, scale)]
     post = np.exp(1j * iflag * sum(cc * s for cc, s in zip(cen, ss)))
     for a in range(d):
-        post = post / kernel_ft(w, beta, taus[a])
+        post = post / kernel_ft(w, beta, taus[a], kernel)
     outs = []
     for t in range(cs.shape[0]):
-        grid = _spread(nf[::-1], w, beta, i0, de, cs[t] * pre)
+        grid = _spread(nf[::-1], w, beta, i0, de, cs[t] * pre, kernel)
         inner = nufft2(grid, *taus, eps=eps, iflag=iflag, modeord=0, sigma=sigma,
-                       workers=workers)
+                       workers=workers, kernel=kernel)
         outs.append(inner * post)
     out = np.stack(outs)
     return out[0] if single else out

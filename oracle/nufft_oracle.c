@@ -68,9 +68,12 @@ int64_t orc_next235even(int64_t n0) {
  * sigma gives w = ceil(-ln(eps) / (pi*sqrt(1-1/sigma))).  Shape: beta =
  * 2.30*w at sigma == 2 (2.20, 2.26, 2.38 for w = 2, 3, 4), else
  * beta = 0.97*pi*(1-1/(2*sigma))*w.
+ * Kaiser-Bessel (shape 1, an option of the CUDA library) keeps the width
+ * rule with beta = pi*sqrt((w/sigma)^2 (sigma-1/2)^2 - 0.8) (Beatty,
+ * Nishimura, Pauly, IEEE TMI 2005).
  * Returns 1 when the width had to be clamped at ORC_MAX_W (tolerance not
  * reachable, the reference's FINUFFT_WARN_EPS_TOO_SMALL), else 0. */
-int orc_kernel_params(double eps, double sigma, int *w_out, double *beta_out) {
+int orc_kernel_params(double eps, double sigma, int shape, int *w_out, double *beta_out) {
   int warn = 0;
   double a;
   if (sigma == 2.0)
@@ -98,6 +101,11 @@ int orc_kernel_params(double eps, double sigma, int *w_out, double *beta_out) {
   }
   *w_out = w;
   *beta_out = ratio * (double)w;
+  if (shape == 1) {
+    double a = ((double)w / sigma) * (sigma - 0.5);
+    double r = a * a - 0.8;
+    *beta_out = ORC_PI * sqrt(r > 0.25 ? r : 0.25);
+  }
   return warn;
 }
 
@@ -109,12 +117,30 @@ int64_t orc_fine_size(int64_t nmodes, double sigma, int w) {
   return orc_next235even(n);
 }
 
-/* The ES kernel at offset t (grid units). */
-double orc_kernel(double t, int w, double beta) {
+/* Modified Bessel function I0 by its power series (positive terms). */
+static double orc_bessel_i0(double x) {
+  double q = 0.25 * x * x, term = 1.0, sum = 1.0;
+  for (int k = 1; k < 500; ++k) {
+    term *= q / ((double)k * (double)k);
+    sum += term;
+    if (term < 1e-17 * sum) break;
+  }
+  return sum;
+}
+
+/* The kernel as a function of s = sqrt(1 - (2t/w)^2): shape 0 the ES kernel
+ * exp(beta*(s-1)), shape 1 Kaiser-Bessel I0(beta*s)/I0(beta). */
+static double orc_kernel_s(double s, double beta, int shape) {
+  if (shape == 1) return orc_bessel_i0(beta * s) / orc_bessel_i0(beta);
+  return exp(beta * (s - 1.0));
+}
+
+/* The kernel at offset t (grid units). */
+double orc_kernel(double t, int w, double beta, int shape) {
   double z = 2.0 * t / (double)w;
   double s = 1.0 - z * z;
   if (s < 0.0) return 0.0;
-  return exp(beta * (sqrt(s) - 1.0));
+  return orc_kernel_s(sqrt(s), beta, shape);
 }
 
 /* Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_q. */
@@ -158,7 +184,7 @@ static void orc_gauss_legendre(int q, double *x, double *wt) {
  * by Gauss-Legendre quadrature after the substitution t = (w/2) sin(theta),
  * which removes the square-root endpoint singularity (q = 2w + 10 nodes on
  * [0, pi/2]). */
-void orc_kernel_ft(int w, double beta, int64_t n, const double *omega, double *out) {
+void orc_kernel_ft(int w, double beta, int shape, int64_t n, const double *omega, double *out) {
   int q = 2 * w + 10;
   double xg[64], wg[64], tq[64], fq[64];
   orc_gauss_legendre(q, xg, wg);
@@ -166,7 +192,7 @@ void orc_kernel_ft(int w, double beta, int64_t n, const double *omega, double *o
     double th = (xg[i] + 1.0) * ORC_PI / 4.0;
     double wt = wg[i] * ORC_PI / 4.0;
     tq[i] = 0.5 * w * sin(th);
-    fq[i] = 2.0 * wt * exp(beta * (cos(th) - 1.0)) * 0.5 * w * cos(th);
+    fq[i] = 2.0 * wt * orc_kernel_s(cos(th), beta, shape) * 0.5 * w * cos(th);
   }
 #pragma omp parallel for schedule(static)
   for (int64_t k = 0; k < n; ++k) {
@@ -262,8 +288,8 @@ static inline int64_t wrapi(int64_t i, int64_t n) {
   return i < 0 ? i + n : i;
 }
 
-static void kernel_values(double delta, int w, double beta, double *k) {
-  for (int j = 0; j < w; ++j) k[j] = orc_kernel((double)j - 0.5 * w + delta, w, beta);
+static void kernel_values(double delta, int w, double beta, int shape, double *k) {
+  for (int j = 0; j < w; ++j) k[j] = orc_kernel((double)j - 0.5 * w + delta, w, beta, shape);
 }
 
 /* grid (complex interleaved, nf[0]*nf[1]*nf[2] cells, x fastest) +=
@@ -271,7 +297,8 @@ static void kernel_values(double delta, int w, double beta, double *k) {
  * Parallel over slabs of the slowest used axis; each thread owns a slab and
  * clips every point's support to it, so the result is deterministic.
  * X/i0/delta are the per-point outputs of orc_fold_points. */
-void orc_spread(int dim, const int64_t *nf, int w, double beta, int64_t M, const int64_t *i0,
+void orc_spread(int dim, const int64_t *nf, int w, double beta, int shape, int64_t M,
+                const int64_t *i0,
                 const double *delta, const double *c, double *grid) {
   int slow = dim - 1;
   int64_t nslow = nf[slow];
@@ -299,7 +326,7 @@ void orc_spread(int dim, const int64_t *nf, int w, double beta, int64_t M, const
         }
       }
       if (!hit) continue;
-      for (int d = 0; d < dim; ++d) kernel_values(delta[j * 3 + d], w, beta, kv[d]);
+      for (int d = 0; d < dim; ++d) kernel_values(delta[j * 3 + d], w, beta, shape, kv[d]);
       double cr = c[2 * j], ci = c[2 * j + 1];
       for (int qs = 0; qs < w; ++qs) {
         int64_t gs = wrapi(s0 + qs, nslow);
@@ -336,14 +363,15 @@ void orc_spread(int dim, const int64_t *nf, int w, double beta, int64_t M, const
 }
 
 /* c_j = sum over the w^dim touched cells of grid(l) psi(l - X_j). */
-void orc_interp(int dim, const int64_t *nf, int w, double beta, int64_t M, const int64_t *i0,
+void orc_interp(int dim, const int64_t *nf, int w, double beta, int shape, int64_t M,
+                const int64_t *i0,
                 const double *delta, const double *grid, double *c) {
 #pragma omp parallel for schedule(static)
   for (int64_t j = 0; j < M; ++j) {
     double kv[3][ORC_MAX_W];
     for (int d = 0; d < 3; ++d)
       for (int q = 0; q < ORC_MAX_W; ++q) kv[d][q] = (d == 0 || q == 0) ? 1.0 : 0.0;
-    for (int d = 0; d < dim; ++d) kernel_values(delta[j * 3 + d], w, beta, kv[d]);
+    for (int d = 0; d < dim; ++d) kernel_values(delta[j * 3 + d], w, beta, shape, kv[d]);
     int wy = dim >= 2 ? w : 1, wz = dim >= 3 ? w : 1;
     double sr = 0.0, si = 0.0;
     for (int qz = 0; qz < wz; ++qz) {
@@ -372,7 +400,7 @@ void orc_interp(int dim, const int64_t *nf, int w, double beta, int64_t M, const
  * `deg`, converted to monomials in u = 2*delta - 1).  coef[j*(deg+1)+n] is
  * the coefficient of u^n on piece j.  Exposed so the tests can check the fit
  * error against the exact kernel. */
-void orc_horner_fit(int w, double beta, int deg, double *coef) {
+void orc_horner_fit(int w, double beta, int shape, int deg, double *coef) {
   int n1 = deg + 1;
   double node[32], val[32], cheb[32], mono[32], tk[32][32];
   for (int i = 0; i < n1; ++i) node[i] = cos(ORC_PI * (i + 0.5) / n1);
@@ -384,7 +412,7 @@ void orc_horner_fit(int w, double beta, int deg, double *coef) {
     for (int n = 0; n < n1; ++n) tk[k][n] = (n ? 2.0 * tk[k - 1][n - 1] : 0.0) - tk[k - 2][n];
   for (int j = 0; j < w; ++j) {
     for (int i = 0; i < n1; ++i)
-      val[i] = orc_kernel((double)j - 0.5 * w + 0.5 * (node[i] + 1.0), w, beta);
+      val[i] = orc_kernel((double)j - 0.5 * w + 0.5 * (node[i] + 1.0), w, beta, shape);
     for (int k = 0; k < n1; ++k) {
       double s = 0.0;
       for (int i = 0; i < n1; ++i) s += val[i] * cos(ORC_PI * k * (i + 0.5) / n1);

@@ -168,6 +168,12 @@ CASES += [(1, 1, True, dict(gpu_upsampfac=1.25), "cluster"),
           (3, 2, False, dict(gpu_method=1), "uniform"),
           (2, 1, False, dict(gpu_precision=1), "uniform"),
           (2, 2, False, dict(gpu_precision=3), "uniform")]
+# Kaiser-Bessel kernel shape: every dimension and type in both precisions,
+# and its direct evaluation (I0 on the device) in place of the polynomials
+for _ndim, _ty, _single in product([1, 2, 3], [1, 2, 3], [True, False]):
+    CASES.append((_ndim, _ty, _single, dict(gpu_kernel=1), "uniform"))
+CASES += [(2, 1, True, dict(gpu_kernel=1, gpu_kerevalmeth=False), "cluster"),
+          (3, 2, False, dict(gpu_kernel=1, gpu_kerevalmeth=False), "uniform")]
 
 
 @pytest.mark.parametrize("ndim, ty, single, kw, kind", CASES,
@@ -186,23 +192,25 @@ def test_against_oracle(jf, cn, ndim, ty, single, kw, kind):
     opts = _opts(**kw)
     mo = int(kw.get("modeord", 0))
     sigma = kw.get("gpu_upsampfac", 2.0)
+    kern = int(kw.get("gpu_kernel", 0))
     x = [v.astype(rdt) for v in _points(rng, ndim, M, kind)]
     iflag = 1 if (ndim + ty) % 2 else -1
     if ty == 1:
         c = (rng.normal(size=(2, M)) + 1j * rng.normal(size=(2, M))).astype(cdt)
         out = jf.nufft1(SHAPES[ndim], T(c), *[T(v) for v in x], eps=eps, iflag=iflag, opts=opts)
-        ref = cn.nufft1(SHAPES[ndim], c, *x, eps=eps, iflag=iflag, modeord=mo, sigma=sigma)
+        ref = cn.nufft1(SHAPES[ndim], c, *x, eps=eps, iflag=iflag, modeord=mo, sigma=sigma,
+                        kernel=kern)
     elif ty == 2:
         f = (rng.normal(size=(2,) + SHAPES[ndim]) + 1j * rng.normal(size=(2,) + SHAPES[ndim])
              ).astype(cdt)
         out = jf.nufft2(T(f), *[T(v) for v in x], eps=eps, iflag=iflag, opts=opts)
-        ref = cn.nufft2(f, *x, eps=eps, iflag=iflag, modeord=mo, sigma=sigma)
+        ref = cn.nufft2(f, *x, eps=eps, iflag=iflag, modeord=mo, sigma=sigma, kernel=kern)
     else:
         s = [rng.uniform(-20, 20, 700).astype(rdt) for _ in range(ndim)]
         c = (rng.normal(size=(2, M)) + 1j * rng.normal(size=(2, M))).astype(cdt)
         out = jf.nufft3(T(c), *[T(v) for v in x], *[T(v) for v in s], eps=eps, iflag=iflag,
                         opts=opts)
-        ref = cn.nufft3(c, *x, *s, eps=eps, iflag=iflag, sigma=sigma)
+        ref = cn.nufft3(c, *x, *s, eps=eps, iflag=iflag, sigma=sigma, kernel=kern)
     out = out.cpu().numpy()
     assert out.shape == ref.shape
     assert np.isfinite(out).all()

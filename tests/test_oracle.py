@@ -218,3 +218,51 @@ def test_single_precision_path_matches_fp64(cn, shape, mo):
     b = cn.nufft2(f, *x, eps=1e-5, iflag=-1, modeord=mo, single=True)
     assert b.dtype == np.complex64
     assert rel_l2(b, cn.nufft2(f, *x, eps=1e-5, iflag=-1, modeord=mo)) < 2e-6
+
+
+@pytest.mark.parametrize("eps", [1e-3, 1e-5, 1e-6, 1e-9])
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+def test_kaiser_bessel_meets_eps(cn, eps, ndim):
+    """The Kaiser-Bessel shape (gpu_kernel=1; beta of Beatty et al. 2005,
+    the same width rule) against the direct sum: within eps at these sizes,
+    and below the exponential of semicircle's error at the same width."""
+    from oracle import direct
+
+    rng = np.random.default_rng(20 + ndim)
+    shape = {1: (30,), 2: (24, 31), 3: (20, 17, 24)}[ndim]
+    x = [rng.uniform(-np.pi, np.pi, 3000) for _ in range(ndim)]
+    f = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    exact = direct.type2(f, x, 1)
+    e_kb = rel_l2(cn.nufft2(f, *x, eps=eps, iflag=1, kernel=1), exact)
+    e_es = rel_l2(cn.nufft2(f, *x, eps=eps, iflag=1, kernel=0), exact)
+    assert e_kb <= eps and e_kb < e_es, (e_kb, e_es)
+    c = rng.normal(size=3000) + 1j * rng.normal(size=3000)
+    assert rel_l2(cn.nufft1(shape, c, *x, eps=eps, iflag=1, kernel=1),
+                  direct.type1(c, x, shape, 1)) <= eps
+    s = [rng.uniform(-15, 15, 200) for _ in range(ndim)]
+    assert rel_l2(cn.nufft3(c, *x, *s, eps=eps, iflag=1, kernel=1),
+                  direct.type3(c, x, s, 1)) <= 2 * eps
+
+
+def test_kaiser_bessel_meets_the_held_case(cn):
+    """The one known answer the exponential of semicircle misses elementwise
+    at width 11 (helpers.ORACLE_HELD) is met by Kaiser-Bessel at the same
+    width."""
+    g = golden("forward.npz")
+    k = "t1_d3_x64_i-1"
+    x, c, f = g[k + "_x"], g[k + "_c"], g[k + "_f"]
+    check_reference(cn.nufft1(f.shape, c, *x, eps=1e-10, iflag=-1, kernel=1), f)
+
+
+def test_kaiser_bessel_horner_fit(cn):
+    """Degree w+2 piecewise polynomials reproduce the Kaiser-Bessel shape
+    to ~1e-8 at w = 6 and to round-off from w = 10 (sigma = 2)."""
+    for w, bound in ((4, 2e-5), (6, 5e-8), (8, 1e-10), (10, 1e-13), (13, 5e-14), (16, 5e-14)):
+        _, beta, _ = cn.kernel_params(10.0 ** (1 - w), 2.0, 1)
+        coef = cn.horner_fit(w, beta, w + 2, shape=1)
+        d = np.linspace(0, 1, 257)[:-1]
+        worst = 0.0
+        for j in range(w):
+            fit = np.polynomial.polynomial.polyval(2 * d - 1, coef[j])
+            worst = max(worst, np.max(np.abs(fit - cn.kernel(j - w / 2 + d, w, beta, 1))))
+        assert worst < bound, (w, worst)
