@@ -342,14 +342,16 @@ def run_ours(args):
     ms_step = job_max(ms_step)
     value = job_value(2 * M, ms_step, ws)
 
-    accuracy = round_trip_errors(dev, pts_h, f, c, g, N)
-    # ---- e2e through the C ABI with host buffers
+    # ---- e2e through the C ABI with host buffers (before the accuracy check,
+    # whose FP64 direct sums leave several GB in torch's caching allocator;
+    # the e2e calls recompute c and g with the same kernel)
     e2e_value = e2e_ms = None
     h2d = pts_h.nbytes + f_h.nbytes
     d2h = N * N * N * 8
     if not args.no_e2e:
         e2e_value, e2e_ms = run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws,
                                     barrier, job_max, opts.gpu_kernel)
+    accuracy = round_trip_errors(dev, pts_h, f, c, g, N)
     rate = ctypes.c_double()
     _native.check(lib.gbn_probe_smem_atomics(sp, min(w.value, 8), ctypes.byref(rate)), "probe")
     updates = M * w.value ** 3  # grid cells touched per transform
