@@ -742,6 +742,7 @@ def measure_lsq_grad(dev, steps, warmup):
     with torch.no_grad():
         d = jf.nufft2(c2, *pts, eps=1e-6) + noise
     out = {}
+    grads = {}
     for name, fused in (("fused_adjoint", True), ("stacked_transforms", False)):
         opts = Opts(gpu_fused_adjoint=fused)
         a = [c.clone().requires_grad_(True)] + [p.clone().requires_grad_(True) for p in pts]
@@ -750,6 +751,8 @@ def measure_lsq_grad(dev, steps, warmup):
             r = jf.nufft2(a[0], *a[1:], eps=1e-6, opts=opts) - d
             loss = torch.sum(torch.real(r) ** 2 + torch.imag(r) ** 2)
             return torch.autograd.grad(loss, a)
+
+        grads[name] = step()
 
         for _ in range(warmup):
             step()
@@ -766,6 +769,11 @@ def measure_lsq_grad(dev, steps, warmup):
     out["workload"] = ("3D type-2 least-squares loss, 128^3 modes, M=2e6 uniform points, "
                        "complex64, eps=1e-6, gradients w.r.t. c and x, y, z (torch API)")
     out["speedup_fused"] = out["stacked_transforms"]["ms_per_step"] / out["fused_adjoint"]["ms_per_step"]
+    # the fused gradient against the stacked rules' at full size
+    out["fused_vs_stacked_rel_l2"] = {
+        n: float(torch.linalg.norm((u - v).reshape(-1)) / torch.linalg.norm(v.reshape(-1)))
+        for n, u, v in zip(("c", "x", "y", "z"), grads["fused_adjoint"],
+                           grads["stacked_transforms"])}
     return out
 
 
@@ -775,13 +783,15 @@ def measure_batched(dev, steps, warmup):
     (b) 64 independent type-2 transforms, M_k = floor(10^U(3,6)) points each,
         modes drawn from {128^2, 256^2, 512^2, 1024^2}.
     Plain = the per-call path with default settings (nufft1 with 32 stacked
-    transforms; 64 nufft2 calls); batched = one autotuned NufftBatch pass
-    replayed from a CUDA graph (tuning and planning timed separately).
-    Returns NU points/s/transform for each."""
+    transforms; 64 nufft2 calls); batched = one autotuned NufftBatch pass per
+    part replayed from a CUDA graph; chain = both parts in one graph
+    (NufftBatchChain: the two batches on forked streams, one replay).  Tuning
+    and planning are timed separately.  Errors: relative l2 against FP64
+    direct sums on 1,000 sampled outputs per part."""
     import torch
 
     import jax_finufft_gb300 as jf
-    from jax_finufft_gb300.batch import NufftBatch
+    from jax_finufft_gb300.batch import NufftBatch, NufftBatchChain
 
     def timed(fn):
         for _ in range(warmup):
@@ -804,18 +814,29 @@ def measure_batched(dev, steps, warmup):
          for _ in range(2)]
     c = torch.tensor((rng.standard_normal((T, M)) + 1j * rng.standard_normal((T, M)))
                      .astype(np.complex64), device=dev)
-    ms_plain = timed(lambda: jf.nufft1((N, N), c, *x, eps=1e-6))
+    ms_plain_a = timed(lambda: jf.nufft1((N, N), c, *x, eps=1e-6))
     t0 = time.perf_counter()
-    b = NufftBatch(1, [(N, N)], [M], ntransf=T, eps=1e-6, use_graph=True, autotune=True)
+    ba = NufftBatch(1, [(N, N)], [M], ntransf=T, eps=1e-6, use_graph=True, autotune=True)
     tune_a = time.perf_counter() - t0
-    P = torch.stack(x)
-    f = b.empty_modes()
-    cb = c.reshape(-1)
-    ms_batch = timed(lambda: b.run_packed(P, cb, f))
+    Pa = torch.stack(x)
+    fa = ba.empty_modes()
+    ca = c.reshape(-1)
+    ms_batch_a = timed(lambda: ba.run_packed(Pa, ca, fa))
+    # error of transforms 0 and T-1 at 500 random modes each
+    erng = np.random.default_rng(SEED + 13)
+    errs = []
+    for t in (0, T - 1):
+        kidx = torch.from_numpy(erng.integers(0, N, size=(500, 2))).to(dev)
+        ref = direct_type1_subset(c[t], x, kidx, (N, N), 1)
+        got = fa.reshape(T, N, N)[t][kidx[:, 0], kidx[:, 1]]
+        errs.append((got.to(torch.complex128) - ref, ref))
+    err_a = float(torch.linalg.norm(torch.cat([e[0] for e in errs])) /
+                  torch.linalg.norm(torch.cat([e[1] for e in errs])))
     out["stacked_type1_32x4e6_512sq"] = {
-        "plain_pts_per_s": T * M / (ms_plain * 1e-3), "batched_pts_per_s": T * M / (ms_batch * 1e-3),
-        "plain_ms": ms_plain, "batched_ms": ms_batch, "plan_and_tune_s": tune_a}
-    del b, c, f
+        "plain_pts_per_s": T * M / (ms_plain_a * 1e-3),
+        "batched_pts_per_s": T * M / (ms_batch_a * 1e-3),
+        "plain_ms": ms_plain_a, "batched_ms": ms_batch_a, "plan_and_tune_s": tune_a,
+        "rel_l2_vs_fp64_direct_1000_modes": err_a}
     # (b) independent uneven problems
     K = 64
     Ms = [int(10 ** rng.uniform(3, 6)) for _ in range(K)]
@@ -824,19 +845,39 @@ def measure_batched(dev, steps, warmup):
             for _ in range(2)] for m in Ms]
     fs = [torch.tensor((rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64),
                        device=dev) for s in shapes]
-    ms_plain = timed(lambda: [jf.nufft2(fk, *pk, eps=1e-6) for fk, pk in zip(fs, pts)])
+    ms_plain_b = timed(lambda: [jf.nufft2(fk, *pk, eps=1e-6) for fk, pk in zip(fs, pts)])
     t0 = time.perf_counter()
-    b = NufftBatch(2, shapes, Ms, eps=1e-6, use_graph=True, autotune=True)
+    bb = NufftBatch(2, shapes, Ms, eps=1e-6, use_graph=True, autotune=True)
     tune_b = time.perf_counter() - t0
-    P = b.pack_points(pts)
+    Pb = bb.pack_points(pts)
     fb = torch.cat([fk.reshape(-1) for fk in fs])
-    cb = b.empty_strengths()
-    ms_batch = timed(lambda: b.run_packed(P, cb, fb))
+    cb = bb.empty_strengths()
+    ms_batch_b = timed(lambda: bb.run_packed(Pb, cb, fb))
+    # error at 1,000 (problem, point) samples: 16 problems x 63 points
+    num, den = [], []
+    for k in erng.choice(K, size=16, replace=False):
+        idx = torch.from_numpy(erng.choice(Ms[k], size=min(63, Ms[k]), replace=False)).to(dev)
+        ref = direct_type2_subset(fs[k], pts[k], idx, -1)
+        got = cb[int(bb.pt_off[k]):int(bb.pt_off[k + 1])][idx]
+        num.append(got.to(torch.complex128) - ref)
+        den.append(ref)
+    err_b = float(torch.linalg.norm(torch.cat(num)) / torch.linalg.norm(torch.cat(den)))
     tot = sum(Ms)
     out["independent_type2_64"] = {
-        "plain_pts_per_s": tot / (ms_plain * 1e-3), "batched_pts_per_s": tot / (ms_batch * 1e-3),
-        "plain_ms": ms_plain, "batched_ms": ms_batch, "total_points": tot,
-        "fft_groups": b.info()["fft_groups"], "plan_and_tune_s": tune_b}
+        "plain_pts_per_s": tot / (ms_plain_b * 1e-3), "batched_pts_per_s": tot / (ms_batch_b * 1e-3),
+        "plain_ms": ms_plain_b, "batched_ms": ms_batch_b, "total_points": tot,
+        "fft_groups": bb.info()["fft_groups"], "plan_and_tune_s": tune_b,
+        "rel_l2_vs_fp64_direct_1000_points": err_b}
+    # (a) + (b) in one graph
+    chain = NufftBatchChain([ba, bb], use_graph=True)
+    ms_chain = timed(lambda: chain.run_packed([(Pa, ca, fa), (Pb, cb, fb)]))
+    out["both_parts_one_graph"] = {
+        "chain_ms": ms_chain, "plain_ms": ms_plain_a + ms_plain_b,
+        "speedup_vs_plain": (ms_plain_a + ms_plain_b) / ms_chain,
+        "pts_per_s": (T * M + tot) / (ms_chain * 1e-3),
+        "note": "NufftBatchChain: the type-1 batch (a) and the type-2 batch (b) forked onto "
+                "their own streams inside one captured CUDA graph, one replay per step"}
+    del chain
     return out
 
 

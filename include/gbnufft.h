@@ -209,6 +209,25 @@ GBN_API int gbn_batch_info(gbn_batch b, int* ngroups, int* queue, int64_t* arena
 GBN_API int gbn_batch_destroy(gbn_batch b);
 
 /*
+ * Batch chains (no counterpart in the reference): n batches, of either
+ * type and any shapes, run as one pass -- each on its own stream, forked
+ * from and joined back to the chain's stream so that they overlap -- and,
+ * with use_graph = 1, captured into one CUDA graph on the first call and
+ * replayed while the 5n pointers stay the same.  x/y/z/c/f hold one pointer
+ * per batch, as gbn_batch_run takes them (y, z may be NULL arrays below
+ * 3D).  The chain does not own its batches: destroy it before them, and do
+ * not run its batches on their own while the chain is in use.  Ordered
+ * after the work already on `stream` and before the work queued on it later.
+ */
+typedef struct gbn_batch_chain_s* gbn_batch_chain;
+GBN_API int gbn_batch_chain_create(const gbn_batch* batches, int n, void* stream,
+                                   gbn_batch_chain* out);
+GBN_API int gbn_batch_chain_run(gbn_batch_chain ch, const void* const* x, const void* const* y,
+                                const void* const* z, void* const* c, void* const* f,
+                                int use_graph);
+GBN_API int gbn_batch_chain_destroy(gbn_batch_chain ch);
+
+/*
  * Autotuner (no counterpart in the reference, whose settings are fixed
  * per call).  For one problem class -- type (1 or 2), dim, precision, the
  * mode shape nmodes (backend order), M rounded up to a power of two,

@@ -1834,9 +1834,12 @@ int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, c
     else if (T >= 2 && 2 * b->smem <= 100 * 1024)
       b->tb = 2;
   }
+  // a single problem gains nothing from the work queue: it runs the plain
+  // per-subproblem kernels (stacked transforms per block) on its own grid
+  if (K == 1) b->queue = false;
   const size_t csz = cplx_size(b->comp_single);
   cudaStream_t s = b->stream;
-  GBN_CUDA(b->arena.ensure((size_t)off * csz, s));
+  if (b->queue) GBN_CUDA(b->arena.ensure((size_t)off * csz, s));
   GBN_CUDA(b->item_start.ensure((size_t)(K + 1) * sizeof(int64_t), s));
   GBN_CUDA(b->counter.ensure(sizeof(int), s));
   *out = b.release();
@@ -2074,6 +2077,126 @@ int gbn_batch_info(gbn_batch b, int* ngroups, int* queue, int64_t* arena_bytes) 
 
 int gbn_batch_destroy(gbn_batch b) {
   delete b;
+  return GBN_OK;
+}
+
+}  // extern "C"
+
+// =============================================================================
+// batch chains: several batches (of either type) run as one pass -- each on
+// its own stream, forked from and joined back to the chain's stream, so the
+// batches overlap -- and, with use_graph, captured into one CUDA graph.
+// =============================================================================
+struct gbn_batch_chain_s {
+  std::vector<gbn_batch_s*> b;  // not owned
+  cudaStream_t user = nullptr, stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_fork = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<const void*> gkey;
+
+  ~gbn_batch_chain_s() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    cudaEvent_t evs[] = {ev_in, ev_fork, ev_out};
+    for (cudaEvent_t e : evs)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+using PtrList = std::vector<const void*>;
+
+int chain_pass(gbn_batch_chain_s* ch, const PtrList& key) {
+  const size_t n = ch->b.size();
+  GBN_CUDA(cudaEventRecord(ch->ev_fork, ch->stream));
+  for (size_t i = 0; i < n; ++i) {
+    gbn_batch_s* b = ch->b[i];
+    const void* const* k = key.data() + 5 * i;
+    GBN_CUDA(cudaStreamWaitEvent(b->stream, ch->ev_fork, 0));
+    GBN_TRY(batch_pass(b, k[0], k[1], k[2], (void*)k[3], (void*)k[4]));
+    GBN_CUDA(cudaEventRecord(b->ev_out, b->stream));
+    GBN_CUDA(cudaStreamWaitEvent(ch->stream, b->ev_out, 0));
+  }
+  return GBN_OK;
+}
+
+int chain_run(gbn_batch_chain_s* ch, const PtrList& key, int use_graph) {
+  GBN_CUDA(cudaEventRecord(ch->ev_in, ch->user));
+  GBN_CUDA(cudaStreamWaitEvent(ch->stream, ch->ev_in, 0));
+  int r = GBN_OK;
+  if (!use_graph) {
+    r = chain_pass(ch, key);
+  } else if (ch->gexec && ch->gkey == key) {
+    GBN_CUDA(cudaGraphLaunch(ch->gexec, ch->stream));
+  } else {
+    // an eager pass sizes every buffer and plan, then the same pass is
+    // captured (the batches' streams join the capture through the fork event)
+    GBN_TRY(chain_pass(ch, key));
+    if (ch->gexec) {
+      cudaGraphExecDestroy(ch->gexec);
+      ch->gexec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    GBN_CUDA(cudaStreamBeginCapture(ch->stream, cudaStreamCaptureModeThreadLocal));
+    r = chain_pass(ch, key);
+    cudaError_t e = cudaStreamEndCapture(ch->stream, &graph);
+    if (r >= 2) {
+      if (graph) cudaGraphDestroy(graph);
+      return r;
+    }
+    GBN_CUDA(e);
+    e = cudaGraphInstantiate(&ch->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    GBN_CUDA(e);
+    ch->gkey = key;
+  }
+  GBN_CUDA(cudaEventRecord(ch->ev_out, ch->stream));
+  GBN_CUDA(cudaStreamWaitEvent(ch->user, ch->ev_out, 0));
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbn_batch_chain_create(const gbn_batch* batches, int n, void* stream, gbn_batch_chain* out) {
+  if (!out || !batches || n < 1) return fail(GBN_ERR_ARGS, "NULL argument or no batches");
+  *out = nullptr;
+  std::unique_ptr<gbn_batch_chain_s> ch(new gbn_batch_chain_s());
+  for (int i = 0; i < n; ++i) {
+    if (!batches[i]) return fail(GBN_ERR_ARGS, "NULL batch in the chain");
+    for (gbn_batch_s* o : ch->b)
+      if (o == batches[i]) return fail(GBN_ERR_ARGS, "a batch appears twice in the chain");
+    ch->b.push_back(batches[i]);
+  }
+  ch->user = (cudaStream_t)stream;
+  GBN_CUDA(cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking));
+  GBN_CUDA(cudaEventCreateWithFlags(&ch->ev_in, cudaEventDisableTiming));
+  GBN_CUDA(cudaEventCreateWithFlags(&ch->ev_fork, cudaEventDisableTiming));
+  GBN_CUDA(cudaEventCreateWithFlags(&ch->ev_out, cudaEventDisableTiming));
+  *out = ch.release();
+  return GBN_OK;
+}
+
+int gbn_batch_chain_run(gbn_batch_chain ch, const void* const* x, const void* const* y,
+                        const void* const* z, void* const* c, void* const* f, int use_graph) {
+  if (!ch || !x || !c || !f) return fail(GBN_ERR_ARGS, "NULL argument");
+  if (int r = check_waits(GBN_OK)) return r;
+  PtrList key;
+  for (size_t i = 0; i < ch->b.size(); ++i) {
+    key.push_back(x[i]);
+    key.push_back(y ? y[i] : nullptr);
+    key.push_back(z ? z[i] : nullptr);
+    key.push_back(c[i]);
+    key.push_back(f[i]);
+  }
+  return check_waits(chain_run(ch, key, use_graph));
+}
+
+int gbn_batch_chain_destroy(gbn_batch_chain ch) {
+  delete ch;
   return GBN_OK;
 }
 

@@ -91,6 +91,10 @@ SIGNATURES = {
     "gbn_batch_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int), _i64p]),
     "gbn_batch_destroy": (ctypes.c_int, [_vp]),
+    "gbn_batch_chain_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _vp,
+                                              ctypes.POINTER(_vp)]),
+    "gbn_batch_chain_run": (ctypes.c_int, [_vp] + [ctypes.POINTER(_vp)] * 5 + [ctypes.c_int]),
+    "gbn_batch_chain_destroy": (ctypes.c_int, [_vp]),
     "gbn_autotune": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _i64p, _i64,
                                     ctypes.c_int, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp,
                                     _vp]),

@@ -20,7 +20,7 @@ import torch
 from . import _native
 from .options import Opts, to_native
 
-__all__ = ["NufftBatch"]
+__all__ = ["NufftBatch", "NufftBatchChain"]
 
 
 class NufftBatch:
@@ -157,3 +157,55 @@ class NufftBatch:
             o = c[self.T * self.pt_off[k]:self.T * self.pt_off[k + 1]]
             outs.append(o.reshape(self.T, -1) if self.T > 1 else o)
         return outs
+
+
+class NufftBatchChain:
+    """Several NufftBatch objects (of either type) run as one pass.
+
+    Each batch runs on its own stream, forked from and joined back to the
+    chain's stream so the batches overlap, and the whole pass is captured
+    into one CUDA graph on the first call and replayed while the buffers
+    stay at the same addresses (gbn_batch_chain_run).  The chain keeps its
+    batches alive; do not run them on their own while the chain is in use.
+    """
+
+    def __init__(self, batches, use_graph=True):
+        self.batches = list(batches)
+        if not self.batches:
+            raise ValueError("a chain needs at least one batch")
+        self.lib = _native.load()
+        self.use_graph = use_graph
+        dev = self.batches[0].device
+        if any(b.device != dev for b in self.batches):
+            raise ValueError("all batches of a chain must be on one device")
+        self.device = dev
+        self.stream = torch.cuda.current_stream(dev)
+        arr = (ctypes.c_void_p * len(self.batches))(*[b.handle.value for b in self.batches])
+        self.handle = ctypes.c_void_p()
+        with torch.cuda.device(dev):
+            _native.check(self.lib.gbn_batch_chain_create(
+                arr, len(self.batches), ctypes.c_void_p(self.stream.cuda_stream),
+                ctypes.byref(self.handle)), "batch_chain_create")
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.gbn_batch_chain_destroy(self.handle)
+        except Exception:
+            pass
+        self.handle = None
+
+    def run_packed(self, args):
+        """args: one (points, c, f) tuple per batch, as NufftBatch.run_packed."""
+        n = len(self.batches)
+        if len(args) != n:
+            raise ValueError("one (points, c, f) tuple per batch")
+        X, Y, Z, C, F = [(ctypes.c_void_p * n)() for _ in range(5)]
+        for i, (b, (points, c, f)) in enumerate(zip(self.batches, args)):
+            pts = [points[u] for u in range(b.dim)][::-1]  # backend order
+            ptr = [p.data_ptr() for p in pts] + [None] * (3 - b.dim)
+            X[i], Y[i], Z[i] = ptr
+            C[i], F[i] = c.data_ptr(), f.data_ptr()
+        with torch.cuda.device(self.device):
+            _native.check(self.lib.gbn_batch_chain_run(self.handle, X, Y, Z, C, F,
+                                                       int(self.use_graph)), "batch_chain_run")

@@ -133,3 +133,53 @@ def test_graph_replay_follows_new_points(jf):
         results.append(c.clone())
     assert not torch.equal(results[0], results[1])
     assert b.info()["work_queue"]
+
+
+def test_chain_of_type1_and_type2_batches(jf):
+    """A chain runs a type-1 batch (one problem, stacked transforms: the
+    plain per-subproblem kernels) and a type-2 batch (several problems: the
+    work queue) as one pass; captured and replayed, twice, it gives each
+    batch's own results, and the replay follows point values changed in
+    place."""
+    from jax_finufft_gb300.batch import NufftBatch, NufftBatchChain
+
+    rng = np.random.default_rng(42)
+    T, M1 = 4, 20000
+    b1 = NufftBatch(1, [(64, 64)], [M1], ntransf=T, eps=1e-6, use_graph=False)
+    shapes = [(32, 32), (64, 48), (40, 40)]
+    Ms = [3000, 500, 8000]
+    b2 = NufftBatch(2, shapes, Ms, eps=1e-6, use_graph=False)
+    P1 = b1.pack_points([tuple(rng.uniform(-np.pi, np.pi, M1).astype(np.float32)
+                               for _ in range(2))])
+    c1 = torch.tensor((rng.standard_normal(T * M1) + 1j * rng.standard_normal(T * M1))
+                      .astype(np.complex64), device=DEV)
+    P2 = b2.pack_points([tuple(rng.uniform(-np.pi, np.pi, m).astype(np.float32)
+                               for _ in range(2)) for m in Ms])
+    f2 = torch.tensor((rng.standard_normal(sum(int(np.prod(s)) for s in shapes)) +
+                       1j * rng.standard_normal(sum(int(np.prod(s)) for s in shapes)))
+                      .astype(np.complex64), device=DEV)
+    f1_ref, c2_ref = b1.empty_modes(), b2.empty_strengths()
+    b1.run_packed(P1, c1, f1_ref)
+    b2.run_packed(P2, c2_ref, f2)
+    # the single problem matches nufft1 on the same data
+    plain = jf.nufft1((64, 64), c1.reshape(T, M1), P1[0], P1[1], eps=1e-6)
+    assert rel_l2(f1_ref.reshape(T, 64, 64).cpu().numpy(), plain.cpu().numpy()) < 1e-5
+    chain = NufftBatchChain([b1, b2], use_graph=True)
+    f1, c2 = b1.empty_modes(), b2.empty_strengths()
+    for _ in range(2):
+        f1.zero_()
+        c2.zero_()
+        chain.run_packed([(P1, c1, f1), (P2, c2, f2)])
+        torch.cuda.synchronize()
+        assert rel_l2(f1.cpu().numpy(), f1_ref.cpu().numpy()) < 1e-5
+        assert rel_l2(c2.cpu().numpy(), c2_ref.cpu().numpy()) < 1e-5
+    # new point values at the same addresses: the replayed graph re-sorts them
+    P1.copy_(torch.remainder(P1 + 0.37, 2 * np.pi) - np.pi)
+    P2.copy_(torch.remainder(P2 - 0.11, 2 * np.pi) - np.pi)
+    b1.run_packed(P1, c1, f1_ref)
+    b2.run_packed(P2, c2_ref, f2)
+    chain.run_packed([(P1, c1, f1), (P2, c2, f2)])
+    torch.cuda.synchronize()
+    assert rel_l2(f1.cpu().numpy(), f1_ref.cpu().numpy()) < 1e-5
+    assert rel_l2(c2.cpu().numpy(), c2_ref.cpu().numpy()) < 1e-5
+    del chain
