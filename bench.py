@@ -663,8 +663,9 @@ def measure_plain2d(dev, steps, warmup, cpu=True):
 def measure_type3(dev, steps, warmup):
     """3D type-3, M=1e6 sources U[-pi,pi)^3, N=1e6 targets U[-64,64)^3, in
     complex64 at eps=1e-6 and complex128 at eps=1e-12: forward, and forward
-    plus the vjp with respect to strengths and source points (torch API);
-    errors against the FP64 direct sum on 500 random targets."""
+    plus the vjp with respect to strengths and source points (torch API; the
+    fused adjoint on the forward's plan); errors against the FP64 direct sum
+    on 500 random targets, and the fused vjp against the stacked rules."""
     import torch
 
     import jax_finufft_gb300 as jf
@@ -710,6 +711,18 @@ def measure_type3(dev, steps, warmup):
         f = fwd()
         truth = direct_type3_subset(c, src, tgt, tidx, -1)
         res["rel_l2_vs_fp64_direct_500_targets"] = rel_err(f[tidx], truth)
+        # the fused vjp (one adjoint pass on the forward's plan) against the
+        # stacked rules of the reference at full size
+        from jax_finufft_gb300.options import Opts
+
+        gf = fwd_bwd()
+        b = [t.detach().clone().requires_grad_(True) for t in a]
+        r = jf.nufft3(b[0], *b[1:], *tgt, eps=eps, iflag=-1, opts=Opts(gpu_fused_adjoint=False))
+        gs = torch.autograd.grad(r, b, grad_outputs=gbar)
+        res["vjp_fused_vs_stacked_rel_l2"] = {
+            n: float(torch.linalg.norm((u - v).reshape(-1)) / torch.linalg.norm(v.reshape(-1)))
+            for n, u, v in zip(("c", "x", "y", "z"), gf, gs)}
+        del b, r, gs, gf
         out[name] = res
         del a, c, src, tgt, gbar, f
         torch.cuda.empty_cache()

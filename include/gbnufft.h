@@ -168,6 +168,20 @@ GBN_API int gbn_debug_fold(gbn_plan plan, int64_t* i0_out, double* delta_out);
  * NULL to skip an axis).  The coordinate terms and (type 1) the strength
  * gradient come from one batched cuFFT of the stacked k-weighted grids and
  * one interpolation pass with shared kernel weights, on the given point set.
+ *
+ * Type-3 plans take pts = NULL: they work on their own points (the last
+ * gbn_setpts: sources sorted for the spreading grid, rescaled targets sorted
+ * for the inner type 2).  gbn_execute_points with dir = -1 is the adjoint,
+ * cotangents f (ntr, N targets) to c (ntr, M sources).  gbn_grad (f = A c,
+ * src = c, g (ntr, N)) gives
+ *     grad_src = A^H g;
+ *     grad_x[d][j] = sum_t Re(c_tj conj(dH_tj / dx_d)),  H_t = A^H g_t,
+ * from one adjoint pass whose gather on the sources also differentiates the
+ * interpolant (the derivative of the kernel's polynomial pieces) -- one
+ * inner FFT per transform where the reference's rules issue d + 1.  The
+ * derivative of the interpolant amplifies its aliasing error by a small
+ * factor: the source gradients carry a few times eps.  Target gradients are
+ * not part of it.
  */
 typedef struct gbn_points_s* gbn_points;
 GBN_API int gbn_points_create(gbn_plan plan, int64_t M, const void* x, const void* y,

@@ -242,6 +242,27 @@ cudaError_t wait_flag_setup();
 bool wait_flag_take();
 void wait_flag_raise();
 
+// Type-3 gradient request: the outer gather of the adjoint also
+// differentiates along the sources (interp_t3grad_kernel).  c: forward
+// strengths (ntr, M, data precision) or null; pre: pre-phase factors (M,
+// compute precision); grad_c: strength gradient (ntr, M) or null; gx: per
+// backend axis M reals (data precision, accumulated) or null; D, scale: the
+// plan's target centres and source scales per backend axis; t0: first
+// transform of the launch in the c/grad_c arrays.
+struct T3Grad {
+  const void* c;
+  const void* pre;
+  void* grad_c;
+  void* gx[3];
+  double D[3], scale[3];
+  int iflag, t0;
+};
+template <typename TC, typename TD>
+cudaError_t launch_interp_t3grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                                 const SortState& st, const void* fine, int nb,
+                                 const T3Grad& tg, cudaStream_t s,
+                                 const CUtensorMap* tmap = nullptr);
+
 // Interpolate ntr transforms: fine -> c (ntr, M).
 template <typename TC, typename TD>
 cudaError_t launch_interp(const Geom& g, const KerSpec<TC>& ks, int method, int64_t M,
@@ -374,9 +395,10 @@ cudaError_t launch_interp_queue(int dim, int group, const BatchProb<TC>* probs, 
                                 const int64_t* item_start, int* counter, int T,
                                 const void* arena, void* c, size_t smem, cudaStream_t s);
 
-// out[t, j] = in[t, j] * fac[j] (complex), ntr transforms of length n.
+// out[t, j] = in[t, j] * fac[j] (complex; conj(fac[j]) with conj), ntr
+// transforms of length n.
 template <typename TI, typename TO, typename TF>
 cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, void* out,
-                        cudaStream_t s);
+                        cudaStream_t s, bool conj = false);
 
 }  // namespace gbn

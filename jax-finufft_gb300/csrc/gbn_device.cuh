@@ -35,6 +35,8 @@ __device__ __forceinline__ void load_coef(T (&co)[NCO], const KerSpec<T>& ks, in
 
 __device__ __forceinline__ float bessel_i0_dev(float x) { return cyl_bessel_i0f(x); }
 __device__ __forceinline__ double bessel_i0_dev(double x) { return cyl_bessel_i0(x); }
+__device__ __forceinline__ float bessel_i1_dev(float x) { return cyl_bessel_i1f(x); }
+__device__ __forceinline__ double bessel_i1_dev(double x) { return cyl_bessel_i1(x); }
 
 // Kernel value of piece `piece` at offset delta in [0, 1): Horner in
 // u = 2*delta - 1, or the direct formula: exp(beta*(sqrt(1-z^2)-1)), or

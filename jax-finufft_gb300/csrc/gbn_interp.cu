@@ -141,32 +141,17 @@ struct GradEpi {
   }
 };
 
-// One subproblem of ntb <= TB grids t, t+1, ..., executed by the whole block
-// (shared by the per-subproblem kernel, the work-queue kernel of batched
-// plans and the fused gradient kernel).  Grid t+k is fine + (t+k)*nftot and
-// is staged in tile k (shared memory, each tile padded to 128 bytes); a
-// point's record and kernel values are computed once for all its grids, and
-// its value from grid slot k goes through epi(k, input index, re, im).
-// tmap (or null): TMA map of the grids; t_map = grid t's index in it.
-template <typename TC, typename TD, int DIM, int G, int TB, typename Epi>
-__device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
-                                                const PtRec<TC, DIM>* __restrict__ recs,
-                                                const SubArgs& sa, int sub, int t, int ntb,
-                                                const cplx_t<TC>* __restrict__ fine,
-                                                const Epi& epi, int64_t nftot,
-                                                unsigned char* smem_raw,
-                                                const CUtensorMap* tmap = nullptr,
-                                                int t_map = 0) {
-  constexpr int NCO = GroupCfg<G>::NCO;
-  constexpr int PPW = 32 / G;
-  constexpr int NWARP = kThreads / 32;
-  int start, cnt, bin;
-  if (!sub_range(sa, g, M, sub, start, cnt, bin)) return;
-  const int w = g.w;
-  const Tile<DIM> tl(g, bin);
+// Stage the bin tile of grids t .. t+ntb-1 into shared memory (tile k at
+// tiles + k*tile_c): one bulk tensor copy per grid when the tile does not wrap
+// (FP32, 2D/3D, with a map), else a cell loop with periodic wrap.  False when
+// a bounded wait gave up and the copies never completed: the block must then
+// write no output.
+template <typename TC, int DIM>
+__device__ __forceinline__ bool stage_tiles(const Geom& g, const Tile<DIM>& tl,
+                                            cplx_t<TC>* tiles, int tile_c, int t, int ntb,
+                                            const cplx_t<TC>* __restrict__ fine, int64_t nftot,
+                                            const CUtensorMap* tmap, int t_map) {
   const int ncell = tl.ncell;
-  const int tile_c = (int)(interp_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4) / sizeof(cplx_t<TC>));
-  cplx_t<TC>* tiles = reinterpret_cast<cplx_t<TC>*>(smem_raw);  // tile k at tiles + k*tile_c
   bool staged = false;
   if constexpr (sizeof(TC) == 4 && DIM > 1) {
     if (tmap != nullptr && tl.interior(g) && (smem_addr(tiles) & 127u) == 0 &&
@@ -196,7 +181,7 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
         }
         // wait (bounded again) for the copies in flight; a tile that still
         // has not arrived is never read and the block writes no output
-        if (__syncthreads_or(!mbar_wait_bounded(&s_bar, 0, kWaitPolls))) return;
+        if (__syncthreads_or(!mbar_wait_bounded(&s_bar, 0, kWaitPolls))) return false;
       }
       staged = true;
     }
@@ -215,6 +200,36 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
       }
     }
   }
+  return true;
+}
+
+// One subproblem of ntb <= TB grids t, t+1, ..., executed by the whole block
+// (shared by the per-subproblem kernel, the work-queue kernel of batched
+// plans and the fused gradient kernel).  Grid t+k is fine + (t+k)*nftot and
+// is staged in tile k (shared memory, each tile padded to 128 bytes); a
+// point's record and kernel values are computed once for all its grids, and
+// its value from grid slot k goes through epi(k, input index, re, im).
+// tmap (or null): TMA map of the grids; t_map = grid t's index in it.
+template <typename TC, typename TD, int DIM, int G, int TB, typename Epi>
+__device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                                                const PtRec<TC, DIM>* __restrict__ recs,
+                                                const SubArgs& sa, int sub, int t, int ntb,
+                                                const cplx_t<TC>* __restrict__ fine,
+                                                const Epi& epi, int64_t nftot,
+                                                unsigned char* smem_raw,
+                                                const CUtensorMap* tmap = nullptr,
+                                                int t_map = 0) {
+  constexpr int NCO = GroupCfg<G>::NCO;
+  constexpr int PPW = 32 / G;
+  constexpr int NWARP = kThreads / 32;
+  int start, cnt, bin;
+  if (!sub_range(sa, g, M, sub, start, cnt, bin)) return;
+  const int w = g.w;
+  const Tile<DIM> tl(g, bin);
+  const int ncell = tl.ncell;
+  const int tile_c = (int)(interp_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4) / sizeof(cplx_t<TC>));
+  cplx_t<TC>* tiles = reinterpret_cast<cplx_t<TC>*>(smem_raw);  // tile k at tiles + k*tile_c
+  if (!stage_tiles<TC, DIM>(g, tl, tiles, tile_c, t, ntb, fine, nftot, tmap, t_map)) return;
   const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
   TC co[NCO];
   load_coef<TC, NCO>(co, ks, gl, w);
@@ -302,6 +317,178 @@ __device__ __forceinline__ void interp_sm_block(const Geom& g, const KerSpec<TC>
       ai *= kx;
       group_reduce<TC, G>(ar, ai);
       if (valid && gl == 0) epi(k, out_idx, ar, ai);
+    }
+  }
+}
+
+// Kernel value and its derivative with respect to delta (the Horner
+// polynomial and its derivative together, or the direct formula).
+template <typename T, int NCO>
+__device__ __forceinline__ T kerval_d(const T (&co)[NCO], const KerSpec<T>& ks, T delta,
+                                      int piece, int w, T& dval) {
+  if (ks.meth == 0) {
+    dval = T(0);
+    if (piece >= w) return T(0);
+    const T t = (T)piece - T(0.5) * (T)w + delta;
+    const T z = t * (T(2) / (T)w);
+    const T s2 = T(1) - z * z;
+    if (!(s2 > T(0))) return T(0);
+    const T sq = sqrt(s2);
+    const T dsq = -z / sq * (T(2) / (T)w);  // d sqrt(1 - z^2) / dt, dt/d delta = 1
+    if (ks.shape == 1) {
+      dval = bessel_i1_dev(ks.beta * sq) * ks.beta * dsq * ks.inv_i0b;
+      return bessel_i0_dev(ks.beta * sq) * ks.inv_i0b;
+    }
+    const T v = exp(ks.beta * (sq - T(1)));
+    dval = v * ks.beta * dsq;
+    return v;
+  }
+  const T u = T(2) * delta - T(1);
+  T v = T(0), dv = T(0);
+#pragma unroll
+  for (int n = NCO - 1; n >= 0; --n) {
+    dv = fma(dv, u, v);
+    v = fma(v, u, co[n]);
+  }
+  dval = T(2) * dv;  // du / d delta = 2
+  return v;
+}
+
+// Type-3 gradient gather on the outer grid of the adjoint (see t3_adjoint in
+// the plan code): for each source point j and transform t, the value I and
+// its derivatives J_a along the grid coordinate X_a of the adjoint grid, then
+//   H = conj(pre_j) I                      (the strength gradient, stored)
+//   dH_a = conj(pre_j) (-i iflag D_a I + scale_a J_a)
+//   grad_x_a[j] += Re(c_tj conj(dH_a))     (atomic: summed over transforms)
+// with X_a = (x_a - C_a) scale_a + nf_a/2 and pre_j = exp(i iflag D.(x_j - C)).
+template <typename TC, typename TD>
+struct T3GradArgs {
+  const cplx_t<TD>* c;     // forward strengths (ntr, M), null when no gx is asked
+  const cplx_t<TC>* pre;   // pre-phase factor of each source (M)
+  cplx_t<TD>* grad_c;      // (ntr, M) or null
+  TD* gx[3];               // per backend axis: M reals, accumulated, or null
+  TC D[3], scale[3];
+  int iflag, t0;
+};
+
+template <typename TC, typename TD, int DIM, int G>
+__global__ void __launch_bounds__(kThreads)
+    interp_t3grad_kernel(Geom g, KerSpec<TC> ks, int64_t M,
+                         const PtRec<TC, DIM>* __restrict__ recs, SubArgs sa,
+                         const cplx_t<TC>* __restrict__ fine, int64_t nftot,
+                         T3GradArgs<TC, TD> ga, const __grid_constant__ CUtensorMap tmap,
+                         int use_tma, int t_map0) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  constexpr int NCO = GroupCfg<G>::NCO;
+  constexpr int PPW = 32 / G;
+  constexpr int NWARP = kThreads / 32;
+  int start, cnt, bin;
+  if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
+  const int t = blockIdx.y;  // transform within this launch
+  const int w = g.w;
+  const Tile<DIM> tl(g, bin);
+  const int tile_c = (int)(interp_tile_bytes(DIM, g.bs, w, sizeof(TC) == 4) / sizeof(cplx_t<TC>));
+  cplx_t<TC>* tile = reinterpret_cast<cplx_t<TC>*>(smem_raw);
+  if (!stage_tiles<TC, DIM>(g, tl, tile, tile_c, t, 1, fine, nftot, use_tma ? &tmap : nullptr,
+                            t_map0 + t))
+    return;
+  const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, warp = threadIdx.x >> 5;
+  TC co[NCO];
+  load_coef<TC, NCO>(co, ks, gl, w);
+  __syncthreads();
+  const bool lane_on = gl < w;
+  const int T0 = tl.T[0];
+  const int plane = T0 * tl.T[1];
+  const int tg = ga.t0 + t;  // transform index in the caller's arrays
+  for (int pb = warp * PPW; pb < cnt; pb += NWARP * PPW) {
+    const int pi = pb + grp;
+    const bool valid = pi < cnt && grp < PPW;
+    const int js = start + (valid ? pi : 0);
+    const PtRec<TC, DIM> r = recs[js];
+    const int j = sa.perm ? sa.perm[js] : js;
+    TC dkx;
+    const TC kx = kerval_d<TC, NCO>(co, ks, r.d[0], gl, w, dkx);
+    TC kyr[G], dkyr[G];
+    TC kz = TC(0), dkz = TC(0);
+    if (DIM > 1) {
+      TC dky;
+      const TC ky = kerval_d<TC, NCO>(co, ks, r.d[1], gl, w, dky);
+#pragma unroll
+      for (int i = 0; i < G; ++i) {
+        kyr[i] = __shfl_sync(0xffffffffu, ky, grp * G + i);
+        dkyr[i] = __shfl_sync(0xffffffffu, dky, grp * G + i);
+      }
+    }
+    if (DIM > 2) kz = kerval_d<TC, NCO>(co, ks, r.d[2], gl, w, dkz);
+    const int l0 = r.i[0] - tl.org[0] + gl;
+    const int cell0 = DIM == 1 ? l0
+                      : DIM == 2 ? (r.i[1] - tl.org[1]) * T0 + l0
+                                 : ((r.i[2] - tl.org[2]) * tl.T[1] + (r.i[1] - tl.org[1])) * T0 +
+                                       l0;
+    // a: sum over the lane's rows weighted by ky kz; b: by dky kz; e: by ky dkz
+    TC ar = 0, ai = 0, br = 0, bi = 0, er = 0, ei = 0;
+    if (DIM == 1) {
+      if (lane_on) {
+        const cplx_t<TC> v = tile[cell0];
+        ar = v.x;
+        ai = v.y;
+      }
+    } else {
+      const cplx_t<TC>* zrow = tile + cell0;
+      for (int iz = 0; iz < (DIM > 2 ? w : 1); ++iz) {
+        const TC kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, grp * G + iz) : TC(1);
+        const TC dkzv = DIM > 2 ? __shfl_sync(0xffffffffu, dkz, grp * G + iz) : TC(0);
+        TC yr = 0, yi = 0, dyr = 0, dyi = 0;
+#pragma unroll
+        for (int iy = 0; iy < G; ++iy) {
+          if (iy < w && lane_on) {
+            const cplx_t<TC> v = zrow[iy * T0];
+            yr = fma(v.x, kyr[iy], yr);
+            yi = fma(v.y, kyr[iy], yi);
+            dyr = fma(v.x, dkyr[iy], dyr);
+            dyi = fma(v.y, dkyr[iy], dyi);
+          }
+        }
+        ar = fma(yr, kzv, ar);
+        ai = fma(yi, kzv, ai);
+        br = fma(dyr, kzv, br);
+        bi = fma(dyi, kzv, bi);
+        er = fma(yr, dkzv, er);
+        ei = fma(yi, dkzv, ei);
+        zrow += plane;
+      }
+    }
+    // value and the derivatives along backend axes 0, 1, 2 (w.r.t. delta)
+    TC vr = ar * kx, vi = ai * kx;
+    TC d0r = ar * dkx, d0i = ai * dkx;
+    TC d1r = br * kx, d1i = bi * kx;
+    TC d2r = er * kx, d2i = ei * kx;
+    group_reduce<TC, G>(vr, vi);
+    group_reduce<TC, G>(d0r, d0i);
+    if (DIM > 1) group_reduce<TC, G>(d1r, d1i);
+    if (DIM > 2) group_reduce<TC, G>(d2r, d2i);
+    if (!(valid && gl == 0)) continue;
+    const cplx_t<TC> pre = ga.pre[j];
+    const TC pr = pre.x, pi_ = -pre.y;  // conj(pre)
+    if (ga.grad_c) {
+      cplx_t<TD> o;
+      o.x = (TD)(pr * vr - pi_ * vi);
+      o.y = (TD)(pr * vi + pi_ * vr);
+      ga.grad_c[(int64_t)tg * M + j] = o;
+    }
+    if (!ga.c) continue;
+    const cplx_t<TD> cv = ga.c[(int64_t)tg * M + j];
+    const TC cr = (TC)cv.x, ci = (TC)cv.y;
+    const TC sg = (TC)ga.iflag;
+    const TC dr[3] = {d0r, d1r, d2r}, di[3] = {d0i, d1i, d2i};
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      if (!ga.gx[a]) continue;
+      // q = -i iflag D_a I + scale_a J_a, J_a = -(derivative w.r.t. delta)
+      const TC qr = sg * ga.D[a] * vi - ga.scale[a] * dr[a];
+      const TC qi = -sg * ga.D[a] * vr - ga.scale[a] * di[a];
+      const TC hr = pr * qr - pi_ * qi, hi = pr * qi + pi_ * qr;  // dH_a
+      atomicAdd(&ga.gx[a][j], (TD)(cr * hr + ci * hi));          // Re(c conj(dH_a))
     }
   }
 }
@@ -570,6 +757,84 @@ template cudaError_t launch_interp<float, double>(const Geom&, const KerSpec<flo
 template cudaError_t launch_interp<double, double>(const Geom&, const KerSpec<double>&, int,
                                                    int64_t, const SortState&, const void*,
                                                    void*, int, cudaStream_t, const CUtensorMap*);
+
+template <typename TC, typename TD>
+cudaError_t launch_interp_t3grad(const Geom& g, const KerSpec<TC>& ks, int64_t M,
+                                 const SortState& st, const void* fine, int nb,
+                                 const T3Grad& tg, cudaStream_t s,
+                                 const CUtensorMap* tmap) {
+  if (M == 0 || nb == 0) return cudaSuccess;
+  SubArgs sa;
+  sa.sub_bin = st.sub_bin;
+  sa.sub_off = st.sub_off;
+  sa.n_sub = st.n_sub;
+  sa.bin_start = st.bin_start;
+  sa.bin_count = st.bin_count;
+  sa.perm = st.perm;
+  sa.sorted = st.perm != nullptr;
+  const int64_t nblk = sa.sorted ? st.max_sub : (M + g.maxsub - 1) / g.maxsub;
+  int64_t nftot = 1;
+  for (int d = 0; d < g.dim; ++d) nftot *= g.nf[d];
+  T3GradArgs<TC, TD> ga;
+  ga.c = (const cplx_t<TD>*)tg.c;
+  ga.pre = (const cplx_t<TC>*)tg.pre;
+  ga.grad_c = (cplx_t<TD>*)tg.grad_c;
+  for (int a = 0; a < 3; ++a) {
+    ga.gx[a] = (TD*)tg.gx[a];
+    ga.D[a] = (TC)tg.D[a];
+    ga.scale[a] = (TC)tg.scale[a];
+  }
+  ga.iflag = tg.iflag;
+  ga.t0 = tg.t0;
+  const size_t smem = interp_tile_bytes(g.dim, g.bs, g.w, sizeof(TC) == 4);
+  CUtensorMap m;
+  memset(&m, 0, sizeof(m));
+  const int use = tmap != nullptr && sizeof(TC) == 4;
+  if (use) m = *tmap;
+  const int G = g.w > 8 ? 16 : g.w > 6 ? 8 : 6;
+  for (int t0 = 0; t0 < nb; t0 += 65535) {
+    dim3 grid((unsigned)nblk, (unsigned)std::min(nb - t0, 65535));
+    const cplx_t<TC>* ft = (const cplx_t<TC>*)fine + (int64_t)t0 * nftot;
+    T3GradArgs<TC, TD> gb = ga;
+    gb.t0 = ga.t0 + t0;
+    cudaError_t e = cudaSuccess;
+#define GBN_T3G(DIM, GG)                                                                        \
+  {                                                                                             \
+    auto kern = interp_t3grad_kernel<TC, TD, DIM, GG>;                                          \
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+    if (e == cudaSuccess) {                                                                     \
+      kern<<<grid, kThreads, smem, s>>>(g, ks, M, (const PtRec<TC, DIM>*)st.recs, sa, ft,       \
+                                        nftot, gb, m, use, t0);                                 \
+      note_launch();                                                                            \
+    }                                                                                           \
+  }
+    if (g.dim == 1) {
+      if (G == 16) GBN_T3G(1, 16) else if (G == 8) GBN_T3G(1, 8) else GBN_T3G(1, 6)
+    } else if (g.dim == 2) {
+      if (G == 16) GBN_T3G(2, 16) else if (G == 8) GBN_T3G(2, 8) else GBN_T3G(2, 6)
+    } else {
+      if (G == 16) GBN_T3G(3, 16) else if (G == 8) GBN_T3G(3, 8) else GBN_T3G(3, 6)
+    }
+#undef GBN_T3G
+    if (e != cudaSuccess) return e;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+template cudaError_t launch_interp_t3grad<float, float>(const Geom&, const KerSpec<float>&,
+                                                        int64_t, const SortState&, const void*,
+                                                        int, const T3Grad&,
+                                                        cudaStream_t, const CUtensorMap*);
+template cudaError_t launch_interp_t3grad<float, double>(const Geom&, const KerSpec<float>&,
+                                                         int64_t, const SortState&, const void*,
+                                                         int, const T3Grad&,
+                                                         cudaStream_t, const CUtensorMap*);
+template cudaError_t launch_interp_t3grad<double, double>(const Geom&, const KerSpec<double>&,
+                                                          int64_t, const SortState&,
+                                                          const void*, int,
+                                                          const T3Grad&,
+                                                          cudaStream_t, const CUtensorMap*);
 
 namespace {
 

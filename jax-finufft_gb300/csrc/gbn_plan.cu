@@ -1055,11 +1055,16 @@ void ev_record(cudaEvent_t* ev, int i, cudaStream_t s) {
 // transform; dir = -1 its adjoint with the opposite exponent sign (a type-1
 // plan maps modes f to strengths c like a type-2 transform, a type-2 plan
 // maps c to f like a type-1 transform), reusing the same sort.
+// Adjoint of a type-3 plan on its current points: the cotangents f (ntr, N
+// targets) to c (ntr, M sources); with grad the outer gather also
+// differentiates along the sources (interp_t3grad_kernel).
+int t3_adjoint(gbn_plan_s* p, void* c, const void* f, int ntr, const T3Grad* grad);
+
 int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int dir) {
   if (!ps.set) return fail(GBN_ERR_STATE, "execute called before setpts");
   if (p->type != 3 && !points_match(p, ps))
     return fail(GBN_ERR_ARGS, "point set was sorted for a different plan geometry");
-  if (p->type == 3 && dir != 1) return fail(GBN_ERR_ARGS, "type-3 plans have no adjoint execute");
+  if (p->type == 3 && dir != 1) return t3_adjoint(p, c, f, ntr, nullptr);
   cudaStream_t s = p->stream;
   const size_t dsz = cplx_size(p->data_single);
   const size_t csz = cplx_size(p->comp_single);
@@ -1136,6 +1141,96 @@ int execute_ntr(gbn_plan_s* p, gbn_points_s& ps, void* c, void* f, int ntr, int 
   }
   GBN_CUDA(cudaGetLastError());
   return GBN_OK;
+}
+
+int t3_adjoint(gbn_plan_s* p, void* c, const void* f, int ntr, const T3Grad* grad) {
+  gbn_points_s& ps = p->own;
+  if (!ps.set) return fail(GBN_ERR_STATE, "adjoint called before setpts");
+  if (ntr < 1) return fail(GBN_ERR_ARGS, "ntr must be >= 1");
+  cudaStream_t s = p->stream;
+  const size_t dsz = cplx_size(p->data_single), csz = cplx_size(p->comp_single);
+  GBN_CUDA(p->fine.ensure((size_t)p->batch * p->nftot * csz, s));
+  GBN_CUDA(p->t3_obuf.ensure((size_t)p->batch * std::max<int64_t>(p->Nt, 1) * csz, s));
+  if (!grad)
+    GBN_CUDA(p->t3_cbuf.ensure((size_t)p->batch * std::max<int64_t>(ps.M, 1) * csz, s));
+  for (int t0 = 0; t0 < ntr; t0 += p->batch) {
+    const int nb = std::min(p->batch, ntr - t0);
+    const char* fb = (const char*)f + (size_t)t0 * p->Nt * dsz;
+    // cotangents times conj(post): the adjoint of the post-phase/deconvolution
+    cudaError_t e;
+    if (p->comp_single)
+      e = p->data_single
+              ? launch_cmul<float, float, float>(p->Nt, nb, fb, p->t3_post.p, p->t3_obuf.p, s, true)
+              : launch_cmul<double, float, float>(p->Nt, nb, fb, p->t3_post.p, p->t3_obuf.p, s,
+                                                  true);
+    else
+      e = launch_cmul<double, double, double>(p->Nt, nb, fb, p->t3_post.p, p->t3_obuf.p, s, true);
+    GBN_CUDA(e);
+    // the inner type 2's adjoint (a type 1 on the rescaled targets) onto the
+    // spreading grid, on the forward's sorted targets
+    GBN_TRY(execute_ntr(p->inner.get(), p->inner->own, p->t3_obuf.p, p->fine.p, nb, -1));
+    CUtensorMap map;
+    const CUtensorMap* tm = grid_map(p, ps, p->fine.p, nb, &map);
+    if (grad) {  // gather the strength and source gradients on the forward's sort
+      T3Grad tg = *grad;
+      tg.t0 = t0;
+      if (p->comp_single)
+        e = p->data_single ? launch_interp_t3grad<float, float>(p->geom, ker_spec<float>(p),
+                                                               ps.M, ps.st, p->fine.p, nb, tg, s,
+                                                               tm)
+                           : launch_interp_t3grad<float, double>(p->geom, ker_spec<float>(p),
+                                                                ps.M, ps.st, p->fine.p, nb, tg,
+                                                                s, tm);
+      else
+        e = launch_interp_t3grad<double, double>(p->geom, ker_spec<double>(p), ps.M, ps.st,
+                                                 p->fine.p, nb, tg, s);
+      GBN_CUDA(e);
+      continue;
+    }
+    // gather on the sources, then times conj(pre)
+    char* cb = (char*)c + (size_t)t0 * ps.M * dsz;
+    if (p->comp_single) {
+      GBN_CUDA((launch_interp<float, float>(p->geom, ker_spec<float>(p), p->method, ps.M, ps.st,
+                                            p->fine.p, p->t3_cbuf.p, nb, s, tm)));
+      e = p->data_single
+              ? launch_cmul<float, float, float>(ps.M, nb, p->t3_cbuf.p, p->t3_pre.p, cb, s, true)
+              : launch_cmul<float, double, float>(ps.M, nb, p->t3_cbuf.p, p->t3_pre.p, cb, s,
+                                                  true);
+    } else {
+      GBN_CUDA((launch_interp<double, double>(p->geom, ker_spec<double>(p), p->method, ps.M,
+                                              ps.st, p->fine.p, p->t3_cbuf.p, nb, s)));
+      e = launch_cmul<double, double, double>(ps.M, nb, p->t3_cbuf.p, p->t3_pre.p, cb, s, true);
+    }
+    GBN_CUDA(e);
+  }
+  GBN_CUDA(cudaGetLastError());
+  return GBN_OK;
+}
+
+// Type-3 gradients on the plan's current points (see gbn_grad): one adjoint
+// pass of the ntr cotangents whose outer gather also differentiates along
+// the sources.
+int t3_grad(gbn_plan_s* p, int ntr, const void* src, const void* g, void* grad_src,
+            void* const* gx) {
+  const size_t rsz = p->data_single ? 4 : 8;
+  T3Grad tg{};
+  bool any = false;
+  for (int d = 0; d < p->dim; ++d) {
+    tg.gx[d] = gx ? gx[d] : nullptr;
+    if (tg.gx[d]) {
+      any = true;
+      if (p->own.M > 0) GBN_CUDA(cudaMemsetAsync(tg.gx[d], 0, (size_t)p->own.M * rsz, p->stream));
+    }
+    tg.D[d] = p->t3_cs[d];
+    tg.scale[d] = p->t3_scale[d];
+  }
+  if (!any && !grad_src) return GBN_OK;
+  tg.c = any ? src : nullptr;
+  tg.pre = p->t3_pre.p;
+  tg.grad_c = grad_src;
+  tg.iflag = p->iflag;
+  if (p->own.M == 0) return GBN_OK;
+  return t3_adjoint(p, grad_src, g, ntr, &tg);
 }
 
 // Gradients of a type-1 or type-2 plan on point set ps (see gbn_grad).
@@ -1565,17 +1660,25 @@ int gbn_points_destroy(gbn_points pts) {
 }
 
 int gbn_execute_points(gbn_plan plan, gbn_points pts, int ntr, int dir, void* c, void* f) {
-  if (!plan || !pts) return fail(GBN_ERR_ARGS, "NULL plan or point set");
+  if (!plan) return fail(GBN_ERR_ARGS, "NULL plan");
+  if ((plan->type == 3) != (pts == nullptr))
+    return fail(GBN_ERR_ARGS, "type-3 plans take their own points (pts = NULL); types 1 and 2 "
+                              "a point set");
   if (dir != 1 && dir != -1) return fail(GBN_ERR_ARGS, "dir must be +1 or -1");
   if (ntr < 1) return fail(GBN_ERR_ARGS, "ntr must be >= 1");
   if (int r = check_waits(GBN_OK)) return r;
-  return check_waits(execute_ntr(plan, *pts, c, f, ntr, dir));
+  return check_waits(execute_ntr(plan, pts ? *pts : plan->own, c, f, ntr, dir));
 }
 
 int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void* g,
              void* grad_src, void* const* grad_x) {
-  if (!plan || !pts || !src || !g) return fail(GBN_ERR_ARGS, "NULL argument");
+  if (!plan || !src || !g) return fail(GBN_ERR_ARGS, "NULL argument");
+  if ((plan->type == 3) != (pts == nullptr))
+    return fail(GBN_ERR_ARGS, "type-3 plans take their own points (pts = NULL); types 1 and 2 "
+                              "a point set");
+  if (ntr < 1) return fail(GBN_ERR_ARGS, "ntr must be >= 1");
   if (int r = check_waits(GBN_OK)) return r;
+  if (plan->type == 3) return check_waits(t3_grad(plan, ntr, src, g, grad_src, grad_x));
   return check_waits(plan_grad(plan, *pts, ntr, src, g, grad_src, grad_x));
 }
 

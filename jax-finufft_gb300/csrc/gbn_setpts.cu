@@ -691,10 +691,12 @@ __global__ void t3_post_table_kernel(int dim, int64_t N, Ptrs3 s, double cx0, do
 
 template <typename TI, typename TO, typename TF>
 __global__ void cmul_kernel(int64_t n, int ntr, const cplx_t<TI>* __restrict__ in,
-                            const cplx_t<TF>* __restrict__ fac, cplx_t<TO>* __restrict__ out) {
+                            const cplx_t<TF>* __restrict__ fac, cplx_t<TO>* __restrict__ out,
+                            int conj) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const cplx_t<TF> f = fac[j];
+  cplx_t<TF> f = fac[j];
+  if (conj) f.y = -f.y;
   for (int t = 0; t < ntr; ++t) {
     const cplx_t<TI> v = in[(int64_t)t * n + j];
     const TF vr = (TF)v.x, vi = (TF)v.y;
@@ -1124,11 +1126,11 @@ cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, cons
 
 template <typename TI, typename TO, typename TF>
 cudaError_t launch_cmul(int64_t n, int ntr, const void* in, const void* fac, void* out,
-                        cudaStream_t s) {
+                        cudaStream_t s, bool conj) {
   if (n == 0 || ntr == 0) return cudaSuccess;
   cmul_kernel<TI, TO, TF><<<grid1(n, 256), 256, 0, s>>>(n, ntr, (const cplx_t<TI>*)in,
                                                         (const cplx_t<TF>*)fac,
-                                                        (cplx_t<TO>*)out);
+                                                        (cplx_t<TO>*)out, conj ? 1 : 0);
   note_launch();
   return cudaGetLastError();
 }
@@ -1188,7 +1190,7 @@ GBN_INST_T3(double, float)
 GBN_INST_T3(double, double)
 #define GBN_INST_CMUL(TI, TO, TF)                                                             \
   template cudaError_t launch_cmul<TI, TO, TF>(int64_t, int, const void*, const void*, void*, \
-                                               cudaStream_t);
+                                               cudaStream_t, bool);
 GBN_INST_CMUL(float, float, float)
 GBN_INST_CMUL(double, float, float)
 GBN_INST_CMUL(float, double, float)

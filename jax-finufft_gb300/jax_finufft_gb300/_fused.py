@@ -181,3 +181,120 @@ def _backward_calls(lib, plan, state, n_tot, n_transf, n_j, dim, src, g, grad_sr
                                    ctypes.c_void_p(src.data_ptr() + idx * per_src),
                                    ctypes.c_void_p(g.data_ptr() + idx * per_g),
                                    ctypes.c_void_p(gs) if gs else None, gx), "grad")
+
+
+# -- type 3 ------------------------------------------------------------------------
+# A type-3 plan holds its point sets (sources sorted for the spreading grid,
+# rescaled targets sorted for the inner type 2) and its phase factors, so a
+# differentiable forward keeps whole plans (one per n_tot index) for the
+# backward.  Idle plans are pooled per key; setpts reuses a plan's inner
+# type-2 plan while the grid size stays the same.
+_t3_pool = {}
+_T3_POOL_MAX = 4
+
+
+def _t3_take(key):
+    with _lock:
+        idle = _t3_pool.get(key)
+        if idle:
+            return idle.pop()
+    lib = _native.load()
+    dim, single, iflag, ntr, eps, nopts, stream = key[:7]
+    native = to_native_from_key(nopts)
+    plan = ctypes.c_void_p()
+    mk = lib.gbnf_makeplan if single else lib.gbn_makeplan
+    _native.check(mk(3, dim, None, iflag, ntr, eps, ctypes.byref(plan), ctypes.byref(native),
+                     ctypes.c_void_p(stream or None)), "makeplan")
+    return plan
+
+
+def _t3_give(key, plans):
+    lib = _native.load()
+    extra = []
+    with _lock:
+        idle = _t3_pool.setdefault(key, [])
+        for p in plans:
+            (idle if len(idle) < _T3_POOL_MAX else extra).append(p)
+    for p in extra:
+        lib.gbn_destroy(p)
+
+
+class T3State:
+    """A type-3 forward's plans (one per n_tot index), returned to the pool
+    when the state goes away."""
+
+    def __init__(self, key, plans):
+        self.key = key
+        self.plans = plans
+
+    def __del__(self):
+        try:
+            _t3_give(self.key, self.plans)
+        except Exception:  # interpreter shutdown
+            pass
+        self.plans = []
+
+
+def t3_forward(source, points, iflag, eps, opts, out, single, dim):
+    """Type-3 forward keeping its plans; returns a T3State."""
+    lib = _native.load()
+    dev = source.device
+    n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
+    n_j = int(points[0].shape[1])
+    n_k = int(points[dim].shape[1])
+    eps_v = float(np.float32(eps)) if single else float(eps)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    native = to_native(unpack_opts(opts, 3, True) or Opts())
+    key = (dim, bool(single), int(iflag), n_transf, eps_v, _opts_key(native), int(stream),
+           str(dev))
+    src = source.contiguous()
+    xs = [p.contiguous() for p in points[:dim]][::-1]  # backend order
+    ss = [p.contiguous() for p in points[dim:]][::-1]
+    esz = src.element_size()
+    psz = xs[0].element_size()
+    setpts = lib.gbnf_setpts if single else lib.gbn_setpts
+    plans = []
+    try:
+        for idx in range(n_tot):
+            plan = _t3_take(key)
+            plans.append(plan)
+            xp = [ctypes.c_void_p(p.data_ptr() + idx * n_j * psz) for p in xs] + [None] * (3 - dim)
+            sp = [ctypes.c_void_p(p.data_ptr() + idx * n_k * psz) for p in ss] + [None] * (3 - dim)
+            _native.check(setpts(plan, n_j, *xp, n_k, *sp), "setpts")
+            _native.check(lib.gbn_execute(
+                plan, ctypes.c_void_p(src.data_ptr() + idx * n_j * n_transf * esz),
+                ctypes.c_void_p(out.data_ptr() + idx * n_k * n_transf * esz)), "execute")
+    except Exception:
+        _t3_give(key, plans)
+        raise
+    return T3State(key, plans)
+
+
+def t3_backward(state, source, points, g, need_src, need_pts):
+    """Fused type-3 gradients for the strengths and the source points (one
+    adjoint pass per n_tot index whose gather also differentiates along the
+    sources); target gradients are not part of it."""
+    lib = _native.load()
+    dim = len(points) // 2
+    n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
+    n_j = int(points[0].shape[1])
+    src = source.contiguous()
+    g = g.contiguous()
+    esz = src.element_size()
+    grad_src = torch.empty_like(src) if need_src else None
+    grads = [torch.empty(points[u].shape, dtype=points[u].dtype, device=src.device)
+             if need_pts[u] else None for u in range(dim)]
+    psz = points[0].element_size()
+    per_src = src[0].numel() * esz
+    per_g = g[0].numel() * esz
+    for idx in range(n_tot):
+        gx = (ctypes.c_void_p * 3)()
+        for u in range(dim):
+            if grads[u] is not None:
+                gx[dim - 1 - u] = grads[u].data_ptr() + idx * n_j * psz
+        gs = grad_src.data_ptr() + idx * per_src if grad_src is not None else None
+        _native.check(lib.gbn_grad(state.plans[idx], None, n_transf,
+                                   ctypes.c_void_p(src.data_ptr() + idx * per_src),
+                                   ctypes.c_void_p(g.data_ptr() + idx * per_g),
+                                   ctypes.c_void_p(gs) if gs else None, gx), "grad")
+    return grad_src, grads

@@ -14,9 +14,12 @@ Reverse mode, when a type-1/2 input requires grad, runs the fused adjoint:
 the forward keeps its sorted point sets and the backward calls gbn_grad,
 which builds the d+1 k-weighted grids in one pass, transforms them with one
 batched cuFFT and gathers the strength gradient and every coordinate
-gradient in a single interpolation pass on the forward's sort
-(``Opts(gpu_fused_adjoint=False)`` selects the stacked-transform rules of the
-reference instead; type 3 always uses them).
+gradient in a single interpolation pass on the forward's sort.  For type 3
+(strengths and source points) the forward keeps its plans and the backward
+is one adjoint pass on the same sorted sources and targets whose gather also
+differentiates along the sources.  ``Opts(gpu_fused_adjoint=False)`` selects
+the stacked-transform rules of the reference instead; so do gradients with
+respect to type-3 targets.
 """
 import threading
 
@@ -106,12 +109,23 @@ def _freq_tensor(n, modeord, dim, ndim, like):
 
 
 def _execute_fused(nufft_type, source, points, output_shape, iflag, eps, opts):
-    """Type-1/2 forward that keeps its sorted point sets for the backward."""
+    """Forward that keeps its sorted point sets (types 1/2) or its plans
+    (type 3) for the backward."""
     single = check_canonical(source, points, nufft_type)
     dev = source.device
     if dev.type != "cuda" or any(p.device != dev for p in points):
         raise RuntimeError("jax_finufft_gb300 runs on CUDA tensors only (all inputs on one "
                            "device); got %s" % ([str(dev)] + [str(p.device) for p in points]))
+    if nufft_type == 3:
+        ndim = len(points) // 2
+        n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
+        out = torch.empty((n_tot, n_transf, int(points[ndim].shape[1])), dtype=source.dtype,
+                          device=dev)
+        if out.numel() == 0 or source.numel() == 0 or int(points[0].shape[1]) == 0:
+            return _execute(nufft_type, source, points, output_shape, iflag, eps, opts), None
+        with torch.cuda.device(dev):
+            state = _fused.t3_forward(source, points, iflag, eps, opts, out, single, ndim)
+        return out, state
     ndim = len(points)
     n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
     n_j = int(points[0].shape[1])
@@ -129,11 +143,16 @@ def _execute_fused(nufft_type, source, points, output_shape, iflag, eps, opts):
 
 
 def _wants_fused(nufft_type, opts, source, points):
-    if nufft_type == 3 or not torch.is_grad_enabled():
+    if not torch.is_grad_enabled():
         return False
     fwd = unpack_opts(opts, nufft_type, True)
     if fwd is not None and not getattr(fwd, "gpu_fused_adjoint", True):
         return False
+    if nufft_type == 3:
+        # strengths and sources only: target gradients take the stacked rules
+        nd = len(points) // 2
+        if any(p.requires_grad for p in points[nd:]):
+            return False
     return bool(source.requires_grad or any(p.requires_grad for p in points))
 
 
@@ -172,8 +191,13 @@ class _Nufft(torch.autograd.Function):
             # one fused adjoint on the forward's sort (not differentiable again:
             # a graph of the backward takes the stacked path below)
             with torch.cuda.device(source.device):
-                grad_src, gpts = _fused.backward(ctx.fused_state, nufft_type, source, points, g,
-                                                 need_src, need_pts)
+                if nufft_type == 3:
+                    grad_src, gpts = _fused.t3_backward(ctx.fused_state, source, points, g,
+                                                        need_src, need_pts)
+                    gpts = gpts + [None] * ndim
+                else:
+                    grad_src, gpts = _fused.backward(ctx.fused_state, nufft_type, source,
+                                                     points, g, need_src, need_pts)
             return (grad_src, None, None, None, None, None, None, *gpts)
         grads_pts = [None] * len(points)
         grad_src = None
@@ -374,5 +398,6 @@ def nufft3(source, *points, iflag=-1, eps=1e-6, opts=None):
     if not 1 <= ndim <= 3:
         raise ValueError("Only 1-, 2-, and 3-dimensions are supported")
     index, source, *points = broadcast_and_flatten_inputs(3, None, source, *points)
-    result = _Nufft.apply(source, 3, None, iflag, eps, opts, False, *points)
+    fused = _wants_fused(3, opts, source, points)
+    result = _Nufft.apply(source, 3, None, iflag, eps, opts, fused, *points)
     return index.unflatten(result)

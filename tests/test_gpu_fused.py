@@ -123,3 +123,73 @@ def test_fused_path_sorts_once(jf):
     fused = launches(Opts(gpu_fused_adjoint=True))
     stacked = launches(Opts(gpu_fused_adjoint=False))
     assert fused < stacked
+
+
+def _grads3(jf, args, ndim, opts, eps, iflag):
+    a = [t.detach().clone().requires_grad_(i <= ndim) for i, t in enumerate(args)]
+    out = jf.nufft3(a[0], *a[1:], eps=eps, iflag=iflag, opts=opts)
+    w = torch.randn(out.shape, dtype=out.dtype, device=DEV,
+                    generator=torch.Generator(DEV).manual_seed(3))
+    loss = torch.real(torch.sum(torch.conj(w) * out))
+    return torch.autograd.grad(loss, a[:ndim + 1])
+
+
+@pytest.mark.parametrize("ndim, single", list(product([1, 2, 3], [True, False])))
+def test_fused_type3_matches_stacked(jf, ndim, single):
+    """Type-3 strength and source gradients from one adjoint pass on the
+    forward's plans against the stacked rules (ops.py:238-260, 280-314).
+    The source gradients differentiate the adjoint's interpolant, whose
+    aliasing error the derivative amplifies by about the ratio of the grid
+    frequency to the signal's: they agree to a few times eps."""
+    from jax_finufft_gb300.options import Opts
+
+    rng = np.random.default_rng(70 + ndim)
+    rdt = torch.float32 if single else torch.float64
+    cdt = torch.complex64 if single else torch.complex128
+    eps = 1e-6 if single else 1e-11
+    M, Nt, T, B = 3000, 800, 2, 2
+    x = [torch.tensor(rng.uniform(-np.pi, np.pi, (B, 1, M)), dtype=rdt, device=DEV)
+         for _ in range(ndim)]
+    s = [torch.tensor(rng.uniform(-25, 25, (B, 1, Nt)), dtype=rdt, device=DEV)
+         for _ in range(ndim)]
+    c = torch.tensor(rng.normal(size=(B, T, M)) + 1j * rng.normal(size=(B, T, M)), dtype=cdt,
+                     device=DEV)
+    for iflag in (-1, 1):
+        g_f = _grads3(jf, [c] + x + s, ndim, Opts(gpu_fused_adjoint=True), eps, iflag)
+        g_s = _grads3(jf, [c] + x + s, ndim, Opts(gpu_fused_adjoint=False), eps, iflag)
+        assert rel_l2(g_f[0].cpu().numpy(), g_s[0].cpu().numpy()) < (2e-5 if single else 1e-9)
+        for a, b in zip(g_f[1:], g_s[1:]):
+            assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < (1e-4 if single else 1e-8)
+
+
+def test_fused_type3_finite_differences(jf):
+    """Float64 type-3 loss sum |nufft3(c; x) - d|^2 (3D): the fused strength
+    and source gradients against central finite differences (h = 1e-6) along
+    random directions."""
+    rng = np.random.default_rng(77)
+    M, Nt = 600, 300
+    x0 = [rng.uniform(-np.pi, np.pi, M) for _ in range(3)]
+    s = [torch.tensor(rng.uniform(-12, 12, Nt), device=DEV) for _ in range(3)]
+    c0 = rng.normal(size=M) + 1j * rng.normal(size=M)
+    d = torch.tensor(rng.normal(size=Nt) + 1j * rng.normal(size=Nt), device=DEV)
+
+    def loss(c, xs):
+        r = jf.nufft3(c, *xs, *s, eps=1e-12, iflag=1) - d
+        return torch.sum(torch.real(r) ** 2 + torch.imag(r) ** 2)
+
+    c = torch.tensor(c0, device=DEV, requires_grad=True)
+    xs = [torch.tensor(v, device=DEV, requires_grad=True) for v in x0]
+    grads = torch.autograd.grad(loss(c, xs), [c] + xs)
+    h = 1e-6
+    for k in range(4):
+        dc = rng.normal(size=M) + 1j * rng.normal(size=M)
+        dx = [rng.normal(size=M) for _ in range(3)]
+        with torch.no_grad():
+            lp = loss(torch.tensor(c0 + h * dc, device=DEV),
+                      [torch.tensor(v + h * e, device=DEV) for v, e in zip(x0, dx)])
+            lm = loss(torch.tensor(c0 - h * dc, device=DEV),
+                      [torch.tensor(v - h * e, device=DEV) for v, e in zip(x0, dx)])
+        fd = float((lp - lm) / (2 * h))
+        an = float(torch.sum(torch.real(torch.conj(grads[0]) * torch.tensor(dc, device=DEV))))
+        an += sum(float(torch.sum(gx * torch.tensor(e, device=DEV))) for gx, e in zip(grads[1:], dx))
+        assert abs(an - fd) <= 1e-6 * max(1.0, abs(fd)), (k, an, fd)
