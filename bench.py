@@ -353,7 +353,12 @@ def run_ours(args):
                                     barrier, job_max, opts.gpu_kernel)
     accuracy = round_trip_errors(dev, pts_h, f, c, g, N)
     rate = ctypes.c_double()
-    _native.check(lib.gbn_probe_smem_atomics(sp, min(w.value, 8), ctypes.byref(rate)), "probe")
+    probe = ctypes.CDLL(os.path.join(REPO, "jax-finufft_gb300", "jax_finufft_gb300", "_lib",
+                                     "libgbnprobe.so"))
+    probe.gbn_probe_smem_atomics.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_double)]
+    if probe.gbn_probe_smem_atomics(sp, min(w.value, 8), ctypes.byref(rate)) != 0:
+        raise RuntimeError("shared-memory atomic probe failed")
     updates = M * w.value ** 3  # grid cells touched per transform
     ceiling = rate.value / 2  # two int32 atomics per complex update
     peak, peak_kind = measured_peak()
@@ -401,7 +406,7 @@ def run_ours(args):
             "spread_frac_of_ceiling": updates / (spread_ms * 1e-3) / ceiling,
             "note": "M w^3 complex cell updates per transform; the shared-memory spread "
                     "issues two int32 atomics per update, so its ceiling is half the "
-                    "probed atomic rate (gbn_probe_smem_atomics, same access pattern)"},
+                    "probed atomic rate (libgbnprobe.so, bench.py's own probe, same access pattern)"},
     }
     lib.gbn_destroy(p1)
     lib.gbn_destroy(p2)

@@ -283,11 +283,6 @@ GBN_API int gbn_wait_timeouts(long long* count, int reset);
  * the error path above can be exercised without stalling a GPU. */
 GBN_API void gbn_debug_raise_wait_timeout(void);
 
-/* Measurement aid (no counterpart in the reference): int32 shared-memory
- * atomic adds per second over the whole GPU with the access pattern of the
- * fixed-point spread (w lanes x w rows per point, 8-lane groups), the
- * ceiling its point phase is held against.  Synchronises `stream`. */
-GBN_API int gbn_probe_smem_atomics(void* stream, int w, double* atomics_per_s);
 
 /* Thread-local message describing the last non-zero status. */
 GBN_API const char* gbn_last_error(void);

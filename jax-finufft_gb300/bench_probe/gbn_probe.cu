@@ -1,18 +1,13 @@
 // gbn_probe.cu -- shared-memory atomic throughput with the spread's access
 // pattern, the ceiling the shared-memory spreading kernels are held against.
+// A measurement aid of bench.py, built into its own library (libgbnprobe.so)
+// and not part of libgbnufft.so.
 //
 // Each 8-lane group stands for one point: lane gl < w adds into x offset gl
 // of w rows of a 32 KB shared tile (row pitch 24 words, random row origin
 // per point), exactly the int32 red.shared pattern of the fixed-point spread.
 // The result is int32 atomic adds per second over the whole GPU.
 #include <cuda_runtime.h>
-
-#include <string>
-
-#include "../../include/gbnufft.h"
-#include "gbn_common.cuh"
-
-namespace gbn {
 
 namespace {
 
@@ -45,12 +40,13 @@ __global__ void __launch_bounds__(256) smem_atomic_probe_kernel(int iters, int w
 
 }  // namespace
 
-}  // namespace gbn
-
-extern "C" int gbn_probe_smem_atomics(void* stream, int w, double* atomics_per_s) {
-  using namespace gbn;
-  if (!atomics_per_s || w < 1 || w > 8)
-    return set_error(GBN_ERR_ARGS, "gbn_probe_smem_atomics: w must be 1..8");
+// int32 shared-memory atomic adds per second over the whole GPU with the
+// access pattern of the fixed-point spread (w lanes x w rows per point,
+// 8-lane groups).  Synchronises `stream`.  Returns 0, -1 for bad arguments,
+// or the CUDA error code.
+extern "C" __attribute__((visibility("default"))) int gbn_probe_smem_atomics(
+    void* stream, int w, double* atomics_per_s) {
+  if (!atomics_per_s || w < 1 || w > 8) return -1;
   cudaStream_t s = (cudaStream_t)stream;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -65,7 +61,6 @@ extern "C" int gbn_probe_smem_atomics(void* stream, int w, double* atomics_per_s
   for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
     cudaEventRecord(e0, s);
     smem_atomic_probe_kernel<<<blocks, 256, 0, s>>>(iters, w, sink);
-    note_launch();
     cudaEventRecord(e1, s);
     e = cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -75,9 +70,8 @@ extern "C" int gbn_probe_smem_atomics(void* stream, int w, double* atomics_per_s
   if (sink) cudaFreeAsync(sink, s);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
-  if (e != cudaSuccess)
-    return set_error(GBN_ERR_CUDA, std::string("gbn_probe_smem_atomics: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return (int)e;
   const double atomics = (double)blocks * (256 / 8) * iters * w * w;
   *atomics_per_s = best > 0.f ? atomics / (best * 1e-3) : 0.0;
-  return GBN_OK;
+  return 0;
 }

@@ -24,7 +24,10 @@ BUILD_DIR = os.path.join(OUT_DIR, "obj")
 LIB_NAME = "libgbnufft.so"
 
 SOURCES = ["gbn_setpts.cu", "gbn_spread.cu", "gbn_interp.cu", "gbn_grad.cu", "gbn_plan.cu",
-           "gbn_fft.cu", "gbn_tune.cu", "gbn_probe.cu", "gbn_noalloc.cu"]
+           "gbn_fft.cu", "gbn_tune.cu", "gbn_noalloc.cu"]
+# bench.py's shared-memory atomic probe: a library of its own
+PROBE_SRC = os.path.join(HERE, "bench_probe", "gbn_probe.cu")
+PROBE_LIB = "libgbnprobe.so"
 HEADERS = ["gbn_common.cuh", "gbn_device.cuh", "gbn_fold.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -56,11 +59,17 @@ def library_path():
     return os.path.join(OUT_DIR, LIB_NAME)
 
 
+def probe_library_path():
+    return os.path.join(OUT_DIR, PROBE_LIB)
+
+
 def _stamp():
     h = hashlib.sha256()
     for name in SOURCES + HEADERS:
         with open(os.path.join(CSRC, name), "rb") as f:
             h.update(name.encode() + f.read())
+    with open(PROBE_SRC, "rb") as f:
+        h.update(f.read())
     with open(os.path.join(INCLUDE, "gbnufft.h"), "rb") as f:
         h.update(f.read())
     h.update(" ".join(NVCC_FLAGS).encode())
@@ -70,7 +79,8 @@ def _stamp():
 
 def up_to_date():
     stamp = os.path.join(OUT_DIR, "stamp.txt")
-    if not (os.path.exists(library_path()) and os.path.exists(stamp)):
+    if not (os.path.exists(library_path()) and os.path.exists(stamp) and
+            os.path.exists(probe_library_path())):
         return False
     with open(stamp) as f:
         return f.read().strip() == _stamp()
@@ -94,8 +104,20 @@ def build(verbose=False, force=False):
             print(r.stderr, file=sys.stderr, flush=True)  # warnings
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    def build_probe():
+        tmp = probe_library_path() + ".tmp%d" % os.getpid()
+        cmd = [exe] + ARCH + ["-O3", "-Xcompiler", "-fPIC", "-shared", PROBE_SRC, "-o", tmp]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for the probe:\n%s%s" % (r.stdout, r.stderr))
+        os.replace(tmp, probe_library_path())
+
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
+        probe = ex.submit(build_probe)
         objs = list(ex.map(compile_one, SOURCES))
+        probe.result()
     libdir = cuda_lib_dir()
     tmp = library_path() + ".tmp%d" % os.getpid()
     cmd = [exe] + ARCH + ["-shared", "-o", tmp] + objs + [
