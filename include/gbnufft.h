@@ -376,9 +376,11 @@ GBN_API int gbn_nufft3d3(GBN_ONESHOT_ARGS_D, const void* source, const double* x
  * fixed device array of GBN_NOALLOC_SCRATCH_BYTES inside the library, held
  * by every GPU that loads the library until the process exits; M above
  * GBN_NOALLOC_MAX_POINTS or more than GBN_NOALLOC_MAX_BINS bins is rejected
- * with GBN_ERR_ARGS.  The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress, with that device current); make that
- * first call before any stream capture.  All calls share the array: calls
+ * with GBN_ERR_ARGS.  Every call looks up the array's device address in the
+ * current context (cudaGetSymbolAddress; nothing is cached, so a device reset
+ * or another context leaves no stale address); the first call on each
+ * device, and the first after a reset, loads the library's module, so make
+ * it before any stream capture.  All calls share the array: calls
  * whose work overlaps on the GPU race.  Enqueued on `stream`; no host sync.
  */
 #define GBN_NOALLOC_MAX_POINTS 262144

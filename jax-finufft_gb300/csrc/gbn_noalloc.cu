@@ -12,15 +12,17 @@
 // That array is a file-scope __device__ variable, so every GPU that loads
 // the library holds its kNoallocBytes until the process exits.  Host code
 // cannot use the array's name as a device address (in host code it names a
-// host-side stand-in); the first call on each device looks the address up
-// with cudaGetSymbolAddress while that device is current and caches it.
+// host-side stand-in); every call looks the address up with
+// cudaGetSymbolAddress on the current device.  Nothing is cached, so a
+// device reset or a new context (the module loads again, possibly at another
+// address) leaves no stale pointer; the first lookup after a load loads the
+// module, which is why the first call per device goes before stream capture.
 // Every call shares the array and it keeps the previous call's contents, so
 // whatever must start at zero is cleared by the call itself, and two calls
 // whose work overlaps on the GPU (different streams, or the same array on
 // the same device concurrently) race on it.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/gbnufft.h"
@@ -41,27 +43,8 @@ static_assert(kRankBytes + kRecBytes + kStartBytes + 64 * 1024 <= kNoallocBytes,
 
 static __device__ __align__(256) unsigned char g_scratch[kNoallocBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Address of g_scratch on the current device (looked up once per device).
-cudaError_t scratch_on_current_device(void** out, int* dev_out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  *dev_out = dev;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = p;
-  }
-  *out = g_scratch_ptr[dev];
-  return cudaSuccess;
-}
+// Address of g_scratch in the current device's context.
+cudaError_t scratch_on_current_device(void** out) { return cudaGetSymbolAddress(out, g_scratch); }
 
 __global__ void noalloc_scatter_kernel(int64_t M, const int* __restrict__ bins,
                                        const int* __restrict__ rank,
@@ -145,8 +128,7 @@ extern "C" int gbn_binsort_noalloc(void* stream, int dim, int single, int64_t M,
     return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: NULL point or output array");
   if (!counts) return set_error(GBN_ERR_ARGS, "gbn_binsort_noalloc: NULL counts");
   void* scratch = nullptr;
-  int dev = 0;
-  cudaError_t e = scratch_on_current_device(&scratch, &dev);
+  cudaError_t e = scratch_on_current_device(&scratch);
   if (e != cudaSuccess)
     return set_error(GBN_ERR_CUDA, std::string("gbn_binsort_noalloc: scratch lookup failed: ") +
                                        cudaGetErrorString(e));

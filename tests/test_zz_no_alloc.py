@@ -110,3 +110,60 @@ def test_noalloc_rejects_oversize():
     rc = lib.gbn_binsort_noalloc(None, 2, 1, 10, None, None, None, nf, bs, 7, None, None, None)
     assert rc == 2
     assert "bins exceed" in _native.last_error()
+
+
+def _edge_coords(rng, M):
+    """Uniform draws with the fold's edge values planted at the front: the
+    period ends +-pi, 0, +-2pi, values many periods out, the float32 neighbours
+    of pi, and non-finite entries (which fold as 0)."""
+    v = rng.uniform(-np.pi, np.pi, M)
+    f32pi = float(np.float32(np.pi))
+    edges = [np.pi, -np.pi, 0.0, -0.0, 2 * np.pi, -2 * np.pi, 1e6, -1e6, f32pi,
+             float(np.nextafter(np.float32(np.pi), np.float32(0))),
+             float(np.nextafter(np.float32(-np.pi), np.float32(0))),
+             np.nan, np.inf, -np.inf]
+    v[: len(edges)] = edges
+    return v
+
+
+@pytest.mark.parametrize("single", [True, False])
+def test_noalloc_at_limits_matches_oracle(single):
+    """M = GBN_NOALLOC_MAX_POINTS points into GBN_NOALLOC_MAX_BINS bins (a
+    512 x 512 fine grid in 1 x 1 bins), with edge and non-finite coordinates:
+    every bin equals the oracle fold's bin (oracle/nufft_oracle.c
+    orc_fold_points; the FP32 coordinates are exact in FP64, and the library
+    folds both precisions on the FP64 chain), counts are the bins' histogram,
+    and perm is a permutation in bin order."""
+    from jax_finufft_gb300 import _native
+    from oracle import cpu_nufft as cn
+
+    lib = _native.load()
+    rng = np.random.default_rng(23)
+    M, nf, bs, w = 262144, [512, 512, 1], [1, 1, 1], 7
+    dt = torch.float32 if single else torch.float64
+    npdt = np.float32 if single else np.float64
+    coords = [_edge_coords(rng, M).astype(npdt), _edge_coords(rng, M)[::-1].astype(npdt)]
+    pts = [torch.tensor(np.ascontiguousarray(v), device="cuda") for v in coords]
+    assert pts[0].dtype == dt
+    bins, counts, perm = _noalloc(lib, _native, 2, single, pts, nf, bs, w, 512 * 512)
+    _, _, _, ref_bins = cn.fold_points([v.astype(np.float64) for v in coords], nf[:2], w, bs[:2])
+    np.testing.assert_array_equal(bins.astype(np.int64), ref_bins)
+    np.testing.assert_array_equal(counts, np.bincount(ref_bins, minlength=512 * 512))
+    assert np.array_equal(np.sort(perm), np.arange(M))
+    assert np.all(np.diff(bins[perm]) >= 0)
+
+
+def test_noalloc_no_points_clears_counts():
+    """M = 0: the point and per-point output arrays may be NULL; counts is
+    still written (all zeros)."""
+    from jax_finufft_gb300 import _native
+
+    lib = _native.load()
+    counts = torch.full((64 * 8,), -7, dtype=torch.int32, device="cuda")
+    nf = (ctypes.c_int64 * 3)(64, 64, 1)
+    bs = (ctypes.c_int * 3)(8, 1, 1)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _native.check(lib.gbn_binsort_noalloc(stream, 2, 0, 0, None, None, None, nf, bs, 5, None,
+                                          ctypes.c_void_p(counts.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert torch.count_nonzero(counts).item() == 0
