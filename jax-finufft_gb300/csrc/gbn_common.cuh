@@ -64,6 +64,7 @@ struct Geom {
   int maxsub;
   int stash;  // spread: a subproblem's strengths are staged in shared memory after the tile
   int rows;   // sort keys per bin: > 1 orders a bin's points by tile row (y, z), 0/1 by bin
+  int coarse_round;  // FP32 fixed-point spread: tolerance >= 1e-5 allows 2^22-bounded rounding
 };
 
 // Shared-memory tile of one bin: bs + w - 1 cells per axis from the bin's

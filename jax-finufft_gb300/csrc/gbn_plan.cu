@@ -475,6 +475,11 @@ void setup_geom(gbn_plan_s* p) {
     const int64_t r = p->dim == 2 ? bs[1] : (int64_t)bs[1] * bs[2];
     if (r > 1 && g.nbins * r < ((int64_t)1 << 30)) g.rows = (int)r;
   }
+  // the FP32 fixed-point spread may round every contribution on the FMA pipe
+  // (absolute resolution 2^-22 of the largest strength of a subproblem, a
+  // relative error near 1e-6 of the output) where the tolerance leaves room
+  // (1e-5 as float32, 9.99999975e-6, counts as 1e-5)
+  g.coarse_round = p->eps >= 9.99e-6;
   // stage each subproblem's strengths in shared memory when it still fits
   g.stash = method == 2 && spread_smem_bytes(p->dim, bs, p->w, p->comp_single, g.maxsub, true) <=
                                smem_limit;

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "gbn_common.cuh"
@@ -296,6 +297,288 @@ __global__ void __launch_bounds__(kThreads)
                                       smem_raw, use_tma ? &tmap : nullptr, t_base + t);
 }
 
+// ---------------------------------------------------------------------------
+// Row-owned spread: 3D, FP32 compute, bin-sorted points, Horner kernel
+// values, kernel widths 4..8, bins 16 x 16 x bz.
+//
+// Same fixed-point tile as spread_sm_block (int32 re/im pairs, cell (x, y, z)
+// at x + PY y + PZ z with PY = tile_x(16, w) = 16 + WV, WV = w rounded up to
+// even, PZ = PY (15 + w)), but a warp adds ONE point at a time: lane = (part,
+// r, gl) with part = lane / 16 selecting the real or imaginary word, r < R =
+// 16 / WV a row of the point's support and gl < WV an x offset.  One atomic
+// instruction covers R rows of one z-plane; a point takes ceil(w / R) row
+// chunks times w planes of them.  The lane's word is 2 (gl + PY r) + part
+// past the point's base, and PY = 16 + WV is congruent to WV modulo 16, so
+// gl + PY r is distinct modulo 16 over the active lanes and every instruction
+// reaches 32 distinct banks (points spread G lanes at a time collide on most
+// of their shared-memory wavefronts).
+// Contributions become integers with one FFMA each where the precision
+// allows: for |v| < 2^22, fma(a, kz, 1.5 * 2^23) carries round(a kz) in its
+// low bits, offset by the bit pattern of 1.5 * 2^23 (the FP32-to-int32
+// conversion instruction runs at a quarter of the FMA rate and bounded the
+// G-lane kernel).  The block's scale s = 0.999 * 2^31 / sum_j max|c_j| keeps
+// every final cell sum inside int32 (partial sums may wrap: two's-complement
+// addition is exact modulo 2^32); FFMA rounding also caps it at 0.999 * 2^22
+// / max_j max|c_j|.
+// Kernel values: the 3w pieces of a point are evaluated once (one Horner
+// evaluation per lane) into a per-warp table, from which every lane reads its
+// x value, the w z values and the y values of its rows.
+// ---------------------------------------------------------------------------
+template <int W>
+struct RowCfg {
+  static constexpr int WV = (W + 1) & ~1;          // lanes per row
+  static constexpr int R = 16 / WV;                 // rows per instruction
+  static constexpr int NCH = (W + R - 1) / R;       // row chunks per z plane
+  static constexpr int PY = 16 + WV;                // = tile_x(16, W)
+  static constexpr int PZ = PY * (15 + W);          // cells per tile plane
+  static constexpr int NCO = W <= 6 ? 9 : 11;       // Horner coefficients held
+};
+
+constexpr float kRoundMagic = 12582912.0f;   // 1.5 * 2^23
+constexpr int kRoundMagicBits = 0x4B400000;  // its bit pattern
+
+template <int NCO>
+__device__ __forceinline__ float horner_piece(const float (&co)[NCO], float delta) {
+  const float u = 2.f * delta - 1.f;
+  float v = 0.f;
+#pragma unroll
+  for (int n = NCO - 1; n >= 0; --n) v = fmaf(v, u, co[n]);
+  return v;
+}
+
+// Whether spread_rows_kernel serves this geometry (the host checks the rest:
+// FP32, 3D, sorted, Horner values).
+inline bool rows_spread_fits(const Geom& g, int deg) {
+  if (g.dim != 3 || g.bs[0] != 16 || g.bs[1] != 16 || g.w < 4 || g.w > 8) return false;
+  return deg + 1 <= (g.w <= 6 ? 9 : 11);
+}
+
+// One point's contributions: R rows per atomic instruction, NCH row chunks
+// times W planes.  Every lane adds on every instruction; a lane without a
+// cell of the point in this chunk (row >= W, x offset >= W, or a lane past
+// the R rows) adds an exact zero (its multiplier is selected, not multiplied,
+// so that unwritten table entries never reach the sum).  Its cell is the one
+// its lane position names: within the tile's rows, or at most two rows past
+// the tile's last plane, inside the staged strengths that follow the tile in
+// shared memory (an atomic add of zero leaves them unchanged), and still on a
+// bank of its own.
+template <int W, bool MAGIC>
+__device__ __forceinline__ void rows_add(int* tp, float a0, const float (&ky)[8],
+                                         const float (&kz)[8], int r,
+                                         const bool (&on)[RowCfg<W>::NCH]) {
+  using C = RowCfg<W>;
+#pragma unroll
+  for (int ch = 0; ch < C::NCH; ++ch) {
+    float kyv = ky[ch * C::R];
+#pragma unroll
+    for (int rr = 1; rr < C::R; ++rr)
+      if (r == rr) kyv = ky[(ch * C::R + rr) & 7];
+    const float a = on[ch] ? a0 * kyv : 0.f;
+#pragma unroll
+    for (int iz = 0; iz < W; ++iz) {
+      const int v = MAGIC ? __float_as_int(fmaf(a, kz[iz], kRoundMagic)) - kRoundMagicBits
+                          : __float2int_rn(a * kz[iz]);
+      atomicAdd(tp + 2 * (ch * C::R * C::PY + iz * C::PZ), v);
+    }
+  }
+}
+
+// The point loop of spread_rows_kernel: this warp's points p = warp,
+// warp + NWARP, ... of the subproblem, two per iteration, their records
+// loaded one iteration ahead.  Kernel values: one Horner evaluation per lane
+// and point -- lane (part 0, q < w): z piece q; (part 0, w <= q < 2w): x
+// piece q - w; (part 1, q < w): y piece q -- into a per-warp table [z 0..7 |
+// y 8..15 | x 16..23] per point, read back after one warp barrier.
+// MAGIC: contributions rounded by the FFMA above (|v| < 2^22 guaranteed by
+// the scale); otherwise by the FP32 to int32 conversion (|v| < 2^31).
+template <int W, bool MAGIC>
+__device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ recs, int start,
+                                            int cnt, const float2* cst, float scale,
+                                            const float (&co)[RowCfg<W>::NCO], int* lbase,
+                                            unsigned org_cell, float (*tab)[2][24], int warp,
+                                            int hp, int q, int gl, int r,
+                                            const bool (&on)[RowCfg<W>::NCH]) {
+  using C = RowCfg<W>;
+  constexpr int NWARP = kThreads / 32;
+  constexpr int STEP = 2 * NWARP;
+  // this lane's table entry: axis of its Horner evaluation and slot
+  const int axis = hp ? 1 : (q < W ? 2 : 0);
+  const bool writes = hp ? q < W : q < 2 * W;
+  const int slot = hp ? 8 + q : (q < W ? q : 16 + q - W);
+  int buf = 0;
+  PtRec<float, 3> na, nb;
+  if (warp < cnt) {
+    na = recs[start + warp];
+    nb = recs[start + (warp + NWARP < cnt ? warp + NWARP : warp)];
+  }
+#pragma unroll 2
+  for (int p = warp; p < cnt; p += STEP) {
+    const bool two = p + NWARP < cnt;  // warp-uniform
+    const PtRec<float, 3> ra = na, rb = nb;
+    if (p + STEP < cnt) {
+      na = recs[start + p + STEP];
+      nb = recs[start + (p + STEP + NWARP < cnt ? p + STEP + NWARP : p + STEP)];
+    }
+    const float2 ca = cst[p], cb = cst[two ? p + NWARP : p];
+    const float da = axis == 0 ? ra.d[0] : axis == 1 ? ra.d[1] : ra.d[2];
+    const float db = axis == 0 ? rb.d[0] : axis == 1 ? rb.d[1] : rb.d[2];
+    const float tva = horner_piece(co, da);
+    const float tvb = horner_piece(co, db);
+    float(*tb)[24] = tab[buf];
+    if (writes) {
+      tb[0][slot] = tva;
+      tb[1][slot] = tvb;
+    }
+    __syncwarp();
+    buf ^= 1;
+    {
+      const float4* t4 = reinterpret_cast<const float4*>(tb[0]);
+      const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
+      const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+      const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+      const float kx = tb[0][16 + (gl < W ? gl : 0)];
+      int* tp = lbase + 2 * (int)((unsigned)ra.i[0] + C::PY * (unsigned)ra.i[1] +
+                                  C::PZ * (unsigned)ra.i[2] - org_cell);
+      rows_add<W, MAGIC>(tp, (hp ? ca.y : ca.x) * scale * kx, ky, kz, r, on);
+    }
+    if (two) {
+      const float4* t4 = reinterpret_cast<const float4*>(tb[1]);
+      const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
+      const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+      const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+      const float kx = tb[1][16 + (gl < W ? gl : 0)];
+      int* tp = lbase + 2 * (int)((unsigned)rb.i[0] + C::PY * (unsigned)rb.i[1] +
+                                  C::PZ * (unsigned)rb.i[2] - org_cell);
+      rows_add<W, MAGIC>(tp, (hp ? cb.y : cb.x) * scale * kx, ky, kz, r, on);
+    }
+  }
+}
+
+template <typename TD, int W>
+__global__ void __launch_bounds__(kThreads)
+    spread_rows_kernel(Geom g, KerSpec<float> ks, int64_t M,
+                       const PtRec<float, 3>* __restrict__ recs, SubArgs sa,
+                       const cplx_t<TD>* __restrict__ c, cplx_t<float>* __restrict__ fine,
+                       int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
+                       int t_base) {
+  using C = RowCfg<W>;
+  constexpr int NWARP = kThreads / 32;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ float s_sum[NWARP], s_max[NWARP];
+  __shared__ __align__(16) float s_tab[NWARP][2][2][24];  // [warp][buffer][point][z | y | x]
+  __shared__ int s_org[3];
+  int start, cnt, bin;
+  if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
+  const int t = blockIdx.y;
+  // the tile origin (three integer divisions) by one thread, read after the
+  // first barrier; the extents are the same for every bin
+  if (threadIdx.x == 0) {
+    const Tile<3> t0(g, bin);
+    s_org[0] = t0.org[0];
+    s_org[1] = t0.org[1];
+    s_org[2] = t0.org[2];
+  }
+  const size_t tile_b = spread_tile_bytes(3, g.bs, W, true);
+  int* sacc = reinterpret_cast<int*>(smem_raw);
+  {
+    int4* z4 = reinterpret_cast<int4*>(smem_raw);
+    for (int i = threadIdx.x; i < (int)(tile_b / 16); i += kThreads) z4[i] = make_int4(0, 0, 0, 0);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // stage the strengths; sum and maximum of max(|Re c|, |Im c|)
+  float2* cst = reinterpret_cast<float2*>(smem_raw + tile_b);
+  const cplx_t<TD>* ct = c + (int64_t)t * M;
+  float psum = 0.f, pmax = 0.f;
+  for (int p = threadIdx.x; p < cnt; p += kThreads) {
+    float re, im;
+    load_c<TD, float>(ct + sa.perm[start + p], re, im);
+    cst[p] = make_float2(re, im);
+    const float m = fmaxf(fabsf(re), fabsf(im));
+    psum += m;
+    pmax = fmaxf(pmax, m);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    psum += __shfl_xor_sync(0xffffffffu, psum, o);
+    pmax = fmaxf(pmax, __shfl_xor_sync(0xffffffffu, pmax, o));
+  }
+  if (lane == 0) {
+    s_sum[warp] = psum;
+    s_max[warp] = pmax;
+  }
+  const int hp = lane >> 4, q = lane & 15, gl = q % C::WV, r = q / C::WV;
+  // coefficients of the piece this lane evaluates (see rows_points)
+  float co[C::NCO];
+  load_coef<float, C::NCO>(co, ks, q < W ? q : q - W, W);
+  __syncthreads();  // tile cleared, strengths staged, partial sums written
+  float B = 0.f, Mx = 0.f;
+#pragma unroll
+  for (int i = 0; i < NWARP; ++i) {
+    B += s_sum[i];
+    Mx = fmaxf(Mx, s_max[i]);
+  }
+  // Scale: every final cell sum stays below 2^31 in magnitude; with FFMA
+  // rounding also every contribution below 2^22.  The FFMA rounding is used
+  // where the tolerance allows its resolution (2^-22 of the largest strength)
+  // or where it costs nothing (sum >= 512 x largest: the 2^31 bound is the
+  // tighter one).  B == 0 (or denormal): nothing to spread, the tile stays zero.
+  const bool magic = g.coarse_round != 0 || B >= 512.f * Mx;
+  float scale = 0.f;
+  if (B > 1e-30f) {
+    scale = 0.999f * 2147483648.f / B;
+    if (magic) scale = fminf(scale, 0.999f * 4194304.f / Mx);
+  }
+  const float inv = scale > 0.f ? 1.f / scale : 0.f;
+  bool on[C::NCH];
+#pragma unroll
+  for (int ch = 0; ch < C::NCH; ++ch) on[ch] = r < C::R && gl < W && ch * C::R + r < W;
+  int* const lbase = sacc + 2 * (gl + C::PY * r) + hp;
+  const int org[3] = {s_org[0], s_org[1], s_org[2]};
+  const int T2 = g.bs[2] + W - 1, ncell = C::PZ * T2;
+  // cell index of the tile origin, modulo 2^32 (the cell offsets of the
+  // points from it are small; the absolute indices need not fit an int)
+  const unsigned org_cell = (unsigned)org[0] + C::PY * (unsigned)org[1] + C::PZ * (unsigned)org[2];
+  if (magic)
+    rows_points<W, true>(recs, start, cnt, cst, scale, co, lbase, org_cell, s_tab[warp], warp,
+                         hp, q, gl, r, on);
+  else
+    rows_points<W, false>(recs, start, cnt, cst, scale, co, lbase, org_cell, s_tab[warp], warp,
+                          hp, q, gl, r, on);
+  __syncthreads();
+
+  const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
+  const bool interior = org[0] >= 0 && org[0] + C::PY <= nf0 && org[1] >= 0 &&
+                        org[1] + 15 + W <= nf1 && org[2] >= 0 && org[2] + T2 <= nf2;
+  if (use_tma && interior && (smem_addr(sacc) & 127u) == 0 && (tile_b & 127u) == 0) {
+    // fixed point -> float in place (four words per access; the padded tile
+    // is a whole number of 16-byte words), then one bulk reduce-add
+    int4* s4 = reinterpret_cast<int4*>(sacc);
+    for (int i = threadIdx.x; i < (2 * ncell + 3) / 4; i += kThreads) {
+      const int4 v = s4[i];
+      s4[i] = make_int4(__float_as_int((float)v.x * inv), __float_as_int((float)v.y * inv),
+                        __float_as_int((float)v.z * inv), __float_as_int((float)v.w * inv));
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_reduce_add_3d(&tmap, sacc, 2 * org[0], org[1], org[2] + (t_base + t) * nf2);
+      bulk_commit();
+      bulk_wait_read();  // the tile stays allocated until the copy has read it
+    }
+    return;
+  }
+  cplx_t<float>* ft = fine + (int64_t)t * nftot;
+  CellWalk cw(threadIdx.x, kThreads, C::PY, 15 + W);
+  for (int i = threadIdx.x; i < ncell; i += kThreads, cw.next()) {
+    const int ar = sacc[2 * i], ai = sacc[2 * i + 1];
+    if (ar == 0 && ai == 0) continue;
+    const int g0 = wrap_i32(org[0] + cw.c0, nf0);
+    const int g1 = wrap_i32(org[1] + cw.c1, nf1);
+    const int g2 = wrap_i32(org[2] + cw.c2, nf2);
+    atomic_add_c(&ft[(g2 * nf1 + g1) * nf0 + g0], (float)ar * inv, (float)ai * inv);
+  }
+}
+
 template <typename TC, typename TD, int DIM, int G>
 __global__ void __launch_bounds__(kThreads)
     spread_gm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
@@ -428,8 +711,13 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
   // the block's shared memory stays within 100 KB)
   const bool sm = method == 2 && sa.sorted;
   const size_t smem1 = spread_smem_bytes(DIM, g.bs, g.w, sizeof(TC) == 4, g.maxsub, g.stash != 0);
+  // the row-owned kernel (one transform per block) where it applies
+  // (GBN_DISABLE_ROW_SPREAD=1: the G-lane kernel everywhere)
+  static const bool no_rows = std::getenv("GBN_DISABLE_ROW_SPREAD") != nullptr;
+  const bool rows = DIM == 3 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 && !no_rows &&
+                    rows_spread_fits(g, ks.deg);
   int TB = 1;
-  if (sm && sizeof(TC) == 4 && G <= 8 && g.stash) {
+  if (sm && !rows && sizeof(TC) == 4 && G <= 8 && g.stash) {
     if (ntr >= 4 && 4 * smem1 <= 100 * 1024)
       TB = 4;
     else if (ntr >= 2 && 2 * smem1 <= 100 * 1024)
@@ -455,6 +743,40 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
         return cudaSuccess;
       };
       cudaError_t e;
+      if constexpr (DIM == 3 && sizeof(TC) == 4) {
+        if (rows) {
+          auto go_rows = [&](auto kern) -> cudaError_t {
+            cudaError_t er = cudaFuncSetAttribute(
+                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+            if (er != cudaSuccess) return er;
+            kern<<<grid, kThreads, smem1, s>>>(g, ks, M, (const PtRec<float, 3>*)recs, sa, ct,
+                                               (cplx_t<float>*)ft, nftot, m, use, t0);
+            note_launch();
+            return cudaSuccess;
+          };
+          switch (g.w) {
+            case 4:
+              e = go_rows(spread_rows_kernel<TD, 4>);
+              break;
+            case 5:
+              e = go_rows(spread_rows_kernel<TD, 5>);
+              break;
+            case 6:
+              e = go_rows(spread_rows_kernel<TD, 6>);
+              break;
+            case 7:
+              e = go_rows(spread_rows_kernel<TD, 7>);
+              break;
+            default:
+              e = go_rows(spread_rows_kernel<TD, 8>);
+              break;
+          }
+          if (e != cudaSuccess) return e;
+          e = cudaGetLastError();
+          if (e != cudaSuccess) return e;
+          continue;
+        }
+      }
       if constexpr (sizeof(TC) == 4 && G <= 8) {
         e = TB == 4   ? go(spread_sm_kernel<TC, TD, DIM, G, 4>, 4)
             : TB == 2 ? go(spread_sm_kernel<TC, TD, DIM, G, 2>, 2)
