@@ -13,7 +13,9 @@ Metric: NU points/s/transform = 2*M / t_step.  `value` is measured with all
 inputs resident in HBM (plan API: gbn_setpts + gbn_execute); `e2e` goes
 through the reference-facing C-ABI entry points (gbn_nufft3d2f,
 gbn_nufft3d1f) with pinned host buffers, the host->device copies of points
-and modes and the device->host copy of the result inside the timed region.
+and modes and the device->host copy of the result of every step inside the
+timed region (copies of consecutive steps overlap the compute on two side
+streams, device buffers double-buffered).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -386,7 +388,10 @@ def run_ours(args):
                 "path": ("gbn_nufft3d2f + gbn_nufft3d1f (C ABI), pinned host buffers"
                          if opts.gpu_kernel == 0 else
                          "gbn_run (C ABI one-shot call, type 2 then type 1, gpu_kernel=%d), "
-                         "pinned host buffers" % opts.gpu_kernel)},
+                         "pinned host buffers" % opts.gpu_kernel)
+                        + "; each step's H2D copies and D2H read overlap the neighbouring "
+                          "steps' compute on two side streams (double-buffered device inputs "
+                          "and outputs)"},
         "gpu_launches": int(launches),
         "accuracy": dict(accuracy, bar=ERR_BAR,
                          met=max(accuracy.values()) <= ERR_BAR),
@@ -427,7 +432,16 @@ def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, job_max, 
     """Same round trip through the one-shot C-ABI calls with host buffers:
     gbn_nufft3d2f/gbn_nufft3d1f (the reference-named entry points, whose
     attributes select the default kernel) or, for another kernel shape,
-    gbn_run with the same attributes plus gpu_kernel."""
+    gbn_run with the same attributes plus gpu_kernel.
+
+    Every step copies its points and modes from pinned host memory and reads
+    its result back to pinned host memory.  The copies of consecutive steps
+    overlap the compute: inputs and outputs are double-buffered on the
+    device, the host-to-device copies of step i+1 run on one side stream and
+    the device-to-host read of step i-1 on another while step i computes on
+    the main stream (events order each buffer's reuse).  The timed region
+    runs from before the first step's input copies to after the last step's
+    result read."""
     import torch
 
     from jax_finufft_gb300 import _native
@@ -438,37 +452,60 @@ def run_e2e(args, lib, sp, stream, dev, pts_h, f_h, c, g, ws, barrier, job_max, 
     pin_pts = torch.from_numpy(pts_h).pin_memory()
     pin_f = torch.from_numpy(f_h).pin_memory()
     pin_out = torch.empty((N, N, N), dtype=torch.complex64).pin_memory()
-    d_pts = torch.empty((3, M), dtype=torch.float32, device=dev)
-    d_f = torch.empty((N, N, N), dtype=torch.complex64, device=dev)
+    d_pts = [torch.empty((3, M), dtype=torch.float32, device=dev) for _ in range(2)]
+    d_f = [torch.empty((N, N, N), dtype=torch.complex64, device=dev) for _ in range(2)]
+    d_g = [g, torch.empty_like(g)]
+    s_in = torch.cuda.Stream(device=dev)
+    s_out = torch.cuda.Stream(device=dev)
+    ev_in = [torch.cuda.Event() for _ in range(2)]    # inputs of buffer b copied
+    ev_used = [torch.cuda.Event() for _ in range(2)]  # compute on buffer b done
+    ev_read = [torch.cuda.Event() for _ in range(2)]  # result of buffer b read back
+    for b in range(2):  # every event recorded once, so that the first waits pass
+        ev_used[b].record(stream)
+        ev_read[b].record(stream)
 
-    def e2e_step():
-        d_pts.copy_(pin_pts, non_blocking=True)
-        d_f.copy_(pin_f, non_blocking=True)
-        px = [ctypes.c_void_p(d_pts[d].data_ptr()) for d in range(3)]
+    def e2e_step(i):
+        b = i % 2
+        with torch.cuda.stream(s_in):
+            s_in.wait_event(ev_used[b])
+            d_pts[b].copy_(pin_pts, non_blocking=True)
+            d_f[b].copy_(pin_f, non_blocking=True)
+            ev_in[b].record(s_in)
+        stream.wait_event(ev_in[b])
+        stream.wait_event(ev_read[b])
+        px = [ctypes.c_void_p(d_pts[b][d].data_ptr()) for d in range(3)]
         if kernel == 0:
             common = (sp, ctypes.c_float(EPS))
             _native.check(lib.gbn_nufft3d2f(*common, -1, 1, 1, M, N, N, N, 0, 2.0, 0, 1, 1, 0, 0,
-                                            ctypes.c_void_p(d_f.data_ptr()), *px,
+                                            ctypes.c_void_p(d_f[b].data_ptr()), *px,
                                             ctypes.c_void_p(c.data_ptr())))
             _native.check(lib.gbn_nufft3d1f(*common, 1, 1, 1, M, N, N, N, 0, 2.0, 0, 1, 1, 0, 0,
                                             ctypes.c_void_p(c.data_ptr()), *px,
-                                            ctypes.c_void_p(g.data_ptr())))
+                                            ctypes.c_void_p(d_g[b].data_ptr())))
         else:
             _native.run(2, 3, True, stream.cuda_stream, float(np.float32(EPS)), -1, 1, 1, M,
-                        (N, N, N), opts, d_f.data_ptr(), [p.value for p in px], [], c.data_ptr())
+                        (N, N, N), opts, d_f[b].data_ptr(), [p.value for p in px], [],
+                        c.data_ptr())
             _native.run(1, 3, True, stream.cuda_stream, float(np.float32(EPS)), 1, 1, 1, M,
-                        (N, N, N), opts, c.data_ptr(), [p.value for p in px], [], g.data_ptr())
-        pin_out.copy_(g, non_blocking=True)
+                        (N, N, N), opts, c.data_ptr(), [p.value for p in px], [],
+                        d_g[b].data_ptr())
+        ev_used[b].record(stream)
+        with torch.cuda.stream(s_out):
+            s_out.wait_event(ev_used[b])
+            pin_out.copy_(d_g[b], non_blocking=True)
+            ev_read[b].record(s_out)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    for i in range(max(1, args.warmup)):
+        e2e_step(i)
     torch.cuda.synchronize()
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    s_in.wait_event(e0)
+    for i in range(args.steps):
+        e2e_step(i)
+    stream.wait_stream(s_out)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()

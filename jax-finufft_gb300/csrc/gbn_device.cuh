@@ -60,6 +60,46 @@ __device__ __forceinline__ T kerval(const T (&co)[NCO], const KerSpec<T>& ks, T 
   return v;
 }
 
+// Lane layout of the row-owned spread kernel (3D, FP32 compute, bins
+// 16 x 16 x bz, kernel widths 4..8).  Sixteen lanes serve one point: lane
+// q = (r, gl) with gl = q % WV an x offset and r = q / WV one of R rows, WV =
+// w rounded up to even.  The tile's row pitch is PY = tile_x(16, w) = 16 + WV
+// cells, congruent to WV modulo 16, so the cells gl + PY r of the sixteen
+// lanes fall on distinct 8-byte bank pairs; a point takes NCH = ceil(w / R)
+// row chunks times w planes of such accesses.
+template <int W>
+struct RowCfg {
+  static constexpr int WV = (W + 1) & ~1;          // lanes per row
+  static constexpr int R = 16 / WV;                 // rows per access
+  static constexpr int NCH = (W + R - 1) / R;       // row chunks per z plane
+  static constexpr int PY = 16 + WV;                // = tile_x(16, W)
+  static constexpr int PZ = PY * (15 + W);          // cells per tile plane
+  static constexpr int NCO = W <= 6 ? 9 : 11;       // Horner coefficients held
+};
+
+// Shared-memory atomic add by 32-bit shared-window byte address (constant
+// offsets fold into the instruction's immediate; no value returned).
+__device__ __forceinline__ void red_add_shared_s32(uint32_t addr, int v) {
+  asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+// Horner evaluation of one piece (coefficients in registers) at offset delta.
+template <int NCO>
+__device__ __forceinline__ float horner_piece(const float (&co)[NCO], float delta) {
+  const float u = 2.f * delta - 1.f;
+  float v = 0.f;
+#pragma unroll
+  for (int n = NCO - 1; n >= 0; --n) v = fmaf(v, u, co[n]);
+  return v;
+}
+
+// Whether the row-owned spread serves this geometry (the caller checks the
+// rest: FP32 compute, sorted points, Horner kernel values).
+inline bool rows_fit(const Geom& g, int deg) {
+  if (g.dim != 3 || g.bs[0] != 16 || g.bs[1] != 16 || g.w < 4 || g.w > 8) return false;
+  return deg + 1 <= (g.w <= 6 ? 9 : 11);
+}
+
 // Periodic wrap for indices in [-n, 3n).
 __device__ __forceinline__ int64_t wrap_idx(int64_t i, int64_t n) {
   if (i < 0) i += n;

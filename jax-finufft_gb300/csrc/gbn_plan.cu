@@ -429,6 +429,10 @@ void setup_geom(gbn_plan_s* p) {
   g.w = p->w;
   int bs[3];
   default_bins(p->dim, p->comp_single, bs);
+  // type-1 3D FP32 at w <= 6 (the row-owned spread): bins 12 planes deep
+  // halve the per-bin tile overhead of sparse bins for 1.5x the tile
+  // (2.19 -> 2.06 ms on 1e7 mixed points, 512^3 grid; interp prefers 8)
+  if (p->type == 1 && p->dim == 3 && p->comp_single && p->w <= 6) bs[2] = 12;
   const int user[3] = {p->opts.gpu_binsizex, p->opts.gpu_binsizey, p->opts.gpu_binsizez};
   for (int d = 0; d < 3; ++d) {
     if (d < p->dim && user[d] > 0) bs[d] = user[d];

@@ -324,46 +324,21 @@ __global__ void __launch_bounds__(kThreads)
 // evaluation per lane) into a per-warp table, from which every lane reads its
 // x value, the w z values and the y values of its rows.
 // ---------------------------------------------------------------------------
-template <int W>
-struct RowCfg {
-  static constexpr int WV = (W + 1) & ~1;          // lanes per row
-  static constexpr int R = 16 / WV;                 // rows per instruction
-  static constexpr int NCH = (W + R - 1) / R;       // row chunks per z plane
-  static constexpr int PY = 16 + WV;                // = tile_x(16, W)
-  static constexpr int PZ = PY * (15 + W);          // cells per tile plane
-  static constexpr int NCO = W <= 6 ? 9 : 11;       // Horner coefficients held
-};
-
 constexpr float kRoundMagic = 12582912.0f;   // 1.5 * 2^23
 constexpr int kRoundMagicBits = 0x4B400000;  // its bit pattern
 
-template <int NCO>
-__device__ __forceinline__ float horner_piece(const float (&co)[NCO], float delta) {
-  const float u = 2.f * delta - 1.f;
-  float v = 0.f;
-#pragma unroll
-  for (int n = NCO - 1; n >= 0; --n) v = fmaf(v, u, co[n]);
-  return v;
-}
-
-// Whether spread_rows_kernel serves this geometry (the host checks the rest:
-// FP32, 3D, sorted, Horner values).
-inline bool rows_spread_fits(const Geom& g, int deg) {
-  if (g.dim != 3 || g.bs[0] != 16 || g.bs[1] != 16 || g.w < 4 || g.w > 8) return false;
-  return deg + 1 <= (g.w <= 6 ? 9 : 11);
-}
-
 // One point's contributions: R rows per atomic instruction, NCH row chunks
-// times W planes.  Every lane adds on every instruction; a lane without a
-// cell of the point in this chunk (row >= W, x offset >= W, or a lane past
-// the R rows) adds an exact zero (its multiplier is selected, not multiplied,
-// so that unwritten table entries never reach the sum).  Its cell is the one
-// its lane position names: within the tile's rows, or at most two rows past
-// the tile's last plane, inside the staged strengths that follow the tile in
-// shared memory (an atomic add of zero leaves them unchanged), and still on a
-// bank of its own.
+// times W planes, to the point's cells from shared-memory byte address a (the
+// lane's word of the point's first cell).  Every lane adds on every
+// instruction; a lane without a cell of the point in this chunk (row >= W, x
+// offset >= W, or a lane past the R rows) adds an exact zero (its multiplier
+// is selected, not multiplied, so that unwritten table entries never reach
+// the sum).  Its cell is the one its lane position names: within the tile's
+// rows, or at most two rows past the tile's last plane, inside the staged
+// strengths that follow the tile in shared memory (an atomic add of zero
+// leaves them unchanged), and still on a bank of its own.
 template <int W, bool MAGIC>
-__device__ __forceinline__ void rows_add(int* tp, float a0, const float (&ky)[8],
+__device__ __forceinline__ void rows_add(uint32_t a, float a0, const float (&ky)[8],
                                          const float (&kz)[8], int r,
                                          const bool (&on)[RowCfg<W>::NCH]) {
   using C = RowCfg<W>;
@@ -373,84 +348,113 @@ __device__ __forceinline__ void rows_add(int* tp, float a0, const float (&ky)[8]
 #pragma unroll
     for (int rr = 1; rr < C::R; ++rr)
       if (r == rr) kyv = ky[(ch * C::R + rr) & 7];
-    const float a = on[ch] ? a0 * kyv : 0.f;
+    const float av = on[ch] ? a0 * kyv : 0.f;
 #pragma unroll
     for (int iz = 0; iz < W; ++iz) {
-      const int v = MAGIC ? __float_as_int(fmaf(a, kz[iz], kRoundMagic)) - kRoundMagicBits
-                          : __float2int_rn(a * kz[iz]);
-      atomicAdd(tp + 2 * (ch * C::R * C::PY + iz * C::PZ), v);
+      const int v = MAGIC ? __float_as_int(fmaf(av, kz[iz], kRoundMagic)) - kRoundMagicBits
+                          : __float2int_rn(av * kz[iz]);
+      red_add_shared_s32(a + 8u * (ch * C::R * C::PY + iz * C::PZ), v);
     }
   }
 }
 
+// Lane roles in the per-warp kernel-value table of rows_points: one Horner
+// evaluation per lane and point -- lane (part 0, q < w): z piece q; (part 0,
+// w <= q < 2w): x piece q - w; (part 1, q < w): y piece q -- into the
+// table [z 0..7 | y 8..15 | x 16..23] of the point.
+struct RowTab {
+  int axis, slot;
+  bool writes;
+  __device__ __forceinline__ RowTab(int hp, int q, int W) {
+    axis = hp ? 1 : (q < W ? 2 : 0);
+    writes = hp ? q < W : q < 2 * W;
+    slot = hp ? 8 + q : (q < W ? q : 16 + q - W);
+  }
+};
+
+// Two points of the warp (p and p + NWARP when `two`): their kernel values
+// through one table round trip, then their contributions.
+template <int W, bool MAGIC>
+__device__ __forceinline__ void rows_pair(const PtRec<float, 3>& ra, const PtRec<float, 3>& rb,
+                                          bool two, int p, const float2* cst, float scale,
+                                          const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
+                                          unsigned org_cell, float (*tb)[24], const RowTab& rt,
+                                          int hp, int gl, int r,
+                                          const bool (&on)[RowCfg<W>::NCH]) {
+  using C = RowCfg<W>;
+  constexpr int NWARP = kThreads / 32;
+  const float2 ca = cst[p], cb = cst[two ? p + NWARP : p];
+  const float da = rt.axis == 0 ? ra.d[0] : rt.axis == 1 ? ra.d[1] : ra.d[2];
+  const float db = rt.axis == 0 ? rb.d[0] : rt.axis == 1 ? rb.d[1] : rb.d[2];
+  const float tva = horner_piece(co, da);
+  const float tvb = horner_piece(co, db);
+  const uint32_t aa =
+      lbase + 8u * ((unsigned)ra.i[0] + C::PY * (unsigned)ra.i[1] + C::PZ * (unsigned)ra.i[2] -
+                    org_cell);
+  const uint32_t ab =
+      lbase + 8u * ((unsigned)rb.i[0] + C::PY * (unsigned)rb.i[1] + C::PZ * (unsigned)rb.i[2] -
+                    org_cell);
+  if (rt.writes) {
+    tb[0][rt.slot] = tva;
+    tb[1][rt.slot] = tvb;
+  }
+  __syncwarp();
+  const int xs = 16 + (gl < W ? gl : 0);
+  {
+    const float4* t4 = reinterpret_cast<const float4*>(tb[0]);
+    const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
+    const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+    const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+    rows_add<W, MAGIC>(aa, (hp ? ca.y : ca.x) * scale * tb[0][xs], ky, kz, r, on);
+  }
+  if (two) {
+    const float4* t4 = reinterpret_cast<const float4*>(tb[1]);
+    const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
+    const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+    const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+    rows_add<W, MAGIC>(ab, (hp ? cb.y : cb.x) * scale * tb[1][xs], ky, kz, r, on);
+  }
+}
+
 // The point loop of spread_rows_kernel: this warp's points p = warp,
-// warp + NWARP, ... of the subproblem, two per iteration, their records
-// loaded one iteration ahead.  Kernel values: one Horner evaluation per lane
-// and point -- lane (part 0, q < w): z piece q; (part 0, w <= q < 2w): x
-// piece q - w; (part 1, q < w): y piece q -- into a per-warp table [z 0..7 |
-// y 8..15 | x 16..23] per point, read back after one warp barrier.
-// MAGIC: contributions rounded by the FFMA above (|v| < 2^22 guaranteed by
-// the scale); otherwise by the FP32 to int32 conversion (|v| < 2^31).
+// warp + NWARP, ... of the subproblem, two per step, with the records of the
+// next step loaded during the current one into a second register set (the
+// loop body is written out twice, alternating the sets, so no record is
+// copied).  MAGIC: contributions rounded by the FFMA above (|v| < 2^22
+// guaranteed by the scale); otherwise by the FP32 to int32 conversion
+// (|v| < 2^31).
 template <int W, bool MAGIC>
 __device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ recs, int start,
                                             int cnt, const float2* cst, float scale,
-                                            const float (&co)[RowCfg<W>::NCO], int* lbase,
+                                            const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
                                             unsigned org_cell, float (*tab)[2][24], int warp,
                                             int hp, int q, int gl, int r,
                                             const bool (&on)[RowCfg<W>::NCH]) {
-  using C = RowCfg<W>;
   constexpr int NWARP = kThreads / 32;
   constexpr int STEP = 2 * NWARP;
-  // this lane's table entry: axis of its Horner evaluation and slot
-  const int axis = hp ? 1 : (q < W ? 2 : 0);
-  const bool writes = hp ? q < W : q < 2 * W;
-  const int slot = hp ? 8 + q : (q < W ? q : 16 + q - W);
-  int buf = 0;
-  PtRec<float, 3> na, nb;
-  if (warp < cnt) {
-    na = recs[start + warp];
-    nb = recs[start + (warp + NWARP < cnt ? warp + NWARP : warp)];
-  }
-#pragma unroll 2
-  for (int p = warp; p < cnt; p += STEP) {
-    const bool two = p + NWARP < cnt;  // warp-uniform
-    const PtRec<float, 3> ra = na, rb = nb;
+  const RowTab rt(hp, q, W);
+  const PtRec<float, 3>* rp = recs + start;
+  auto jc = [&](int p) { return p < cnt ? p : cnt - 1; };
+  int p = warp;
+  if (p >= cnt) return;
+  PtRec<float, 3> xa = rp[p], xb = rp[jc(p + NWARP)], ya, yb;
+  for (;;) {
     if (p + STEP < cnt) {
-      na = recs[start + p + STEP];
-      nb = recs[start + (p + STEP + NWARP < cnt ? p + STEP + NWARP : p + STEP)];
+      ya = rp[p + STEP];
+      yb = rp[jc(p + STEP + NWARP)];
     }
-    const float2 ca = cst[p], cb = cst[two ? p + NWARP : p];
-    const float da = axis == 0 ? ra.d[0] : axis == 1 ? ra.d[1] : ra.d[2];
-    const float db = axis == 0 ? rb.d[0] : axis == 1 ? rb.d[1] : rb.d[2];
-    const float tva = horner_piece(co, da);
-    const float tvb = horner_piece(co, db);
-    float(*tb)[24] = tab[buf];
-    if (writes) {
-      tb[0][slot] = tva;
-      tb[1][slot] = tvb;
+    rows_pair<W, MAGIC>(xa, xb, p + NWARP < cnt, p, cst, scale, co, lbase, org_cell, tab[0], rt,
+                        hp, gl, r, on);
+    p += STEP;
+    if (p >= cnt) break;
+    if (p + STEP < cnt) {
+      xa = rp[p + STEP];
+      xb = rp[jc(p + STEP + NWARP)];
     }
-    __syncwarp();
-    buf ^= 1;
-    {
-      const float4* t4 = reinterpret_cast<const float4*>(tb[0]);
-      const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
-      const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
-      const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-      const float kx = tb[0][16 + (gl < W ? gl : 0)];
-      int* tp = lbase + 2 * (int)((unsigned)ra.i[0] + C::PY * (unsigned)ra.i[1] +
-                                  C::PZ * (unsigned)ra.i[2] - org_cell);
-      rows_add<W, MAGIC>(tp, (hp ? ca.y : ca.x) * scale * kx, ky, kz, r, on);
-    }
-    if (two) {
-      const float4* t4 = reinterpret_cast<const float4*>(tb[1]);
-      const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
-      const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
-      const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-      const float kx = tb[1][16 + (gl < W ? gl : 0)];
-      int* tp = lbase + 2 * (int)((unsigned)rb.i[0] + C::PY * (unsigned)rb.i[1] +
-                                  C::PZ * (unsigned)rb.i[2] - org_cell);
-      rows_add<W, MAGIC>(tp, (hp ? cb.y : cb.x) * scale * kx, ky, kz, r, on);
-    }
+    rows_pair<W, MAGIC>(ya, yb, p + NWARP < cnt, p, cst, scale, co, lbase, org_cell, tab[1], rt,
+                        hp, gl, r, on);
+    p += STEP;
+    if (p >= cnt) break;
   }
 }
 
@@ -532,7 +536,7 @@ __global__ void __launch_bounds__(kThreads)
   bool on[C::NCH];
 #pragma unroll
   for (int ch = 0; ch < C::NCH; ++ch) on[ch] = r < C::R && gl < W && ch * C::R + r < W;
-  int* const lbase = sacc + 2 * (gl + C::PY * r) + hp;
+  const uint32_t lbase = smem_addr(sacc) + 4u * (2 * (gl + C::PY * r) + hp);
   const int org[3] = {s_org[0], s_org[1], s_org[2]};
   const int T2 = g.bs[2] + W - 1, ncell = C::PZ * T2;
   // cell index of the tile origin, modulo 2^32 (the cell offsets of the
@@ -715,7 +719,7 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
   // (GBN_DISABLE_ROW_SPREAD=1: the G-lane kernel everywhere)
   static const bool no_rows = std::getenv("GBN_DISABLE_ROW_SPREAD") != nullptr;
   const bool rows = DIM == 3 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 && !no_rows &&
-                    rows_spread_fits(g, ks.deg);
+                    rows_fit(g, ks.deg);
   int TB = 1;
   if (sm && !rows && sizeof(TC) == 4 && G <= 8 && g.stash) {
     if (ntr >= 4 && 4 * smem1 <= 100 * 1024)
