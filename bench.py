@@ -359,10 +359,10 @@ def run_ours(args):
                                      "libgbnprobe.so"))
     probe.gbn_probe_smem_atomics.argtypes = [ctypes.c_void_p, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_double)]
-    if probe.gbn_probe_smem_atomics(sp, min(w.value, 8), ctypes.byref(rate)) != 0:
+    if probe.gbn_probe_smem_atomics(sp, min(max(w.value, 4), 8), ctypes.byref(rate)) != 0:
         raise RuntimeError("shared-memory atomic probe failed")
     updates = M * w.value ** 3  # grid cells touched per transform
-    ceiling = rate.value / 2  # two int32 atomics per complex update
+    ceiling = rate.value  # complex updates/s of the row-owned spread's atomic pattern
     peak, peak_kind = measured_peak()
     alg = algorithmic_bytes(M, nf_total)
     spread_ms, interp_ms = t1[0], t2[0]
@@ -406,12 +406,12 @@ def run_ours(args):
         "grid_updates": {
             "spread_per_s": updates / (spread_ms * 1e-3),
             "interp_per_s": updates / (interp_ms * 1e-3),
-            "smem_int32_atomics_per_s": rate.value,
             "spread_ceiling_per_s": ceiling,
             "spread_frac_of_ceiling": updates / (spread_ms * 1e-3) / ceiling,
-            "note": "M w^3 complex cell updates per transform; the shared-memory spread "
-                    "issues two int32 atomics per update, so its ceiling is half the "
-                    "probed atomic rate (libgbnprobe.so, bench.py's own probe, same access pattern)"},
+            "note": "M w^3 complex cell updates per transform; the ceiling is the rate of "
+                    "the row-owned spread's shared-memory atomic pattern alone (int32 "
+                    "red.shared, 2 ceil(w/R) w instructions per point, conflict-free "
+                    "banks), measured by bench.py's own probe (libgbnprobe.so)"},
     }
     lib.gbn_destroy(p1)
     lib.gbn_destroy(p2)
