@@ -77,11 +77,6 @@ struct RowCfg {
   static constexpr int NCO = W <= 6 ? 9 : 11;       // Horner coefficients held
 };
 
-// Shared-memory atomic add by 32-bit shared-window byte address (constant
-// offsets fold into the instruction's immediate; no value returned).
-__device__ __forceinline__ void red_add_shared_s32(uint32_t addr, int v) {
-  asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
-}
 
 // Horner evaluation of one piece (coefficients in registers) at offset delta.
 template <int NCO>

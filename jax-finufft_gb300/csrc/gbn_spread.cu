@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <utility>
 
 #include "gbn_common.cuh"
 #include "gbn_device.cuh"
@@ -324,8 +325,30 @@ __global__ void __launch_bounds__(kThreads)
 // evaluation per lane) into a per-warp table, from which every lane reads its
 // x value, the w z values and the y values of its rows.
 // ---------------------------------------------------------------------------
+// threads per row-owned spread block (three blocks per SM; 512-thread
+// blocks, two per SM, measured slower: 2.07 -> 2.34 ms on the headline)
+constexpr int kRowThreads = 256;
+
 constexpr float kRoundMagic = 12582912.0f;   // 1.5 * 2^23
 constexpr int kRoundMagicBits = 0x4B400000;  // its bit pattern
+
+// One contribution, rounded as the block's scale requires, added at
+// shared-memory byte address a + OFF (OFF a compile-time immediate).
+template <int OFF, bool MAGIC>
+__device__ __forceinline__ void red_at(uint32_t a, float av, float kz) {
+  const int v = MAGIC ? __float_as_int(fmaf(av, kz, kRoundMagic)) - kRoundMagicBits
+                      : __float2int_rn(av * kz);
+  asm volatile("red.shared.add.s32 [%0+%2], %1;" ::"r"(a), "r"(v), "n"(OFF) : "memory");
+}
+
+template <int W, bool MAGIC, int... K>
+__device__ __forceinline__ void rows_add_all(uint32_t a, const float (&av)[RowCfg<W>::NCH],
+                                             const float (&kz)[8],
+                                             std::integer_sequence<int, K...>) {
+  using C = RowCfg<W>;
+  // instruction k: row chunk k / W, plane k % W
+  (red_at<8 * ((K / W) * C::R * C::PY + (K % W) * C::PZ), MAGIC>(a, av[K / W], kz[K % W]), ...);
+}
 
 // One point's contributions: R rows per atomic instruction, NCH row chunks
 // times W planes, to the point's cells from shared-memory byte address a (the
@@ -342,20 +365,16 @@ __device__ __forceinline__ void rows_add(uint32_t a, float a0, const float (&ky)
                                          const float (&kz)[8], int r,
                                          const bool (&on)[RowCfg<W>::NCH]) {
   using C = RowCfg<W>;
+  float av[C::NCH];
 #pragma unroll
   for (int ch = 0; ch < C::NCH; ++ch) {
     float kyv = ky[ch * C::R];
 #pragma unroll
     for (int rr = 1; rr < C::R; ++rr)
       if (r == rr) kyv = ky[(ch * C::R + rr) & 7];
-    const float av = on[ch] ? a0 * kyv : 0.f;
-#pragma unroll
-    for (int iz = 0; iz < W; ++iz) {
-      const int v = MAGIC ? __float_as_int(fmaf(av, kz[iz], kRoundMagic)) - kRoundMagicBits
-                          : __float2int_rn(av * kz[iz]);
-      red_add_shared_s32(a + 8u * (ch * C::R * C::PY + iz * C::PZ), v);
-    }
+    av[ch] = on[ch] ? a0 * kyv : 0.f;
   }
+  rows_add_all<W, MAGIC>(a, av, kz, std::make_integer_sequence<int, C::NCH * W>{});
 }
 
 // Lane roles in the per-warp kernel-value table of rows_points: one Horner
@@ -382,7 +401,7 @@ __device__ __forceinline__ void rows_pair(const PtRec<float, 3>& ra, const PtRec
                                           int hp, int gl, int r,
                                           const bool (&on)[RowCfg<W>::NCH]) {
   using C = RowCfg<W>;
-  constexpr int NWARP = kThreads / 32;
+  constexpr int NWARP = kRowThreads / 32;
   const float2 ca = cst[p], cb = cst[two ? p + NWARP : p];
   const float da = rt.axis == 0 ? ra.d[0] : rt.axis == 1 ? ra.d[1] : ra.d[2];
   const float db = rt.axis == 0 ? rb.d[0] : rt.axis == 1 ? rb.d[1] : rb.d[2];
@@ -430,7 +449,7 @@ __device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ 
                                             unsigned org_cell, float (*tab)[2][24], int warp,
                                             int hp, int q, int gl, int r,
                                             const bool (&on)[RowCfg<W>::NCH]) {
-  constexpr int NWARP = kThreads / 32;
+  constexpr int NWARP = kRowThreads / 32;
   constexpr int STEP = 2 * NWARP;
   const RowTab rt(hp, q, W);
   const PtRec<float, 3>* rp = recs + start;
@@ -459,14 +478,14 @@ __device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ 
 }
 
 template <typename TD, int W>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kRowThreads)
     spread_rows_kernel(Geom g, KerSpec<float> ks, int64_t M,
                        const PtRec<float, 3>* __restrict__ recs, SubArgs sa,
                        const cplx_t<TD>* __restrict__ c, cplx_t<float>* __restrict__ fine,
                        int64_t nftot, const __grid_constant__ CUtensorMap tmap, int use_tma,
                        int t_base) {
   using C = RowCfg<W>;
-  constexpr int NWARP = kThreads / 32;
+  constexpr int NWARP = kRowThreads / 32;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ float s_sum[NWARP], s_max[NWARP];
   __shared__ __align__(16) float s_tab[NWARP][2][2][24];  // [warp][buffer][point][z | y | x]
@@ -486,14 +505,14 @@ __global__ void __launch_bounds__(kThreads)
   int* sacc = reinterpret_cast<int*>(smem_raw);
   {
     int4* z4 = reinterpret_cast<int4*>(smem_raw);
-    for (int i = threadIdx.x; i < (int)(tile_b / 16); i += kThreads) z4[i] = make_int4(0, 0, 0, 0);
+    for (int i = threadIdx.x; i < (int)(tile_b / 16); i += kRowThreads) z4[i] = make_int4(0, 0, 0, 0);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // stage the strengths; sum and maximum of max(|Re c|, |Im c|)
   float2* cst = reinterpret_cast<float2*>(smem_raw + tile_b);
   const cplx_t<TD>* ct = c + (int64_t)t * M;
   float psum = 0.f, pmax = 0.f;
-  for (int p = threadIdx.x; p < cnt; p += kThreads) {
+  for (int p = threadIdx.x; p < cnt; p += kRowThreads) {
     float re, im;
     load_c<TD, float>(ct + sa.perm[start + p], re, im);
     cst[p] = make_float2(re, im);
@@ -557,7 +576,7 @@ __global__ void __launch_bounds__(kThreads)
     // fixed point -> float in place (four words per access; the padded tile
     // is a whole number of 16-byte words), then one bulk reduce-add
     int4* s4 = reinterpret_cast<int4*>(sacc);
-    for (int i = threadIdx.x; i < (2 * ncell + 3) / 4; i += kThreads) {
+    for (int i = threadIdx.x; i < (2 * ncell + 3) / 4; i += kRowThreads) {
       const int4 v = s4[i];
       s4[i] = make_int4(__float_as_int((float)v.x * inv), __float_as_int((float)v.y * inv),
                         __float_as_int((float)v.z * inv), __float_as_int((float)v.w * inv));
@@ -572,8 +591,8 @@ __global__ void __launch_bounds__(kThreads)
     return;
   }
   cplx_t<float>* ft = fine + (int64_t)t * nftot;
-  CellWalk cw(threadIdx.x, kThreads, C::PY, 15 + W);
-  for (int i = threadIdx.x; i < ncell; i += kThreads, cw.next()) {
+  CellWalk cw(threadIdx.x, kRowThreads, C::PY, 15 + W);
+  for (int i = threadIdx.x; i < ncell; i += kRowThreads, cw.next()) {
     const int ar = sacc[2 * i], ai = sacc[2 * i + 1];
     if (ar == 0 && ai == 0) continue;
     const int g0 = wrap_i32(org[0] + cw.c0, nf0);
@@ -753,7 +772,7 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
             cudaError_t er = cudaFuncSetAttribute(
                 kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
             if (er != cudaSuccess) return er;
-            kern<<<grid, kThreads, smem1, s>>>(g, ks, M, (const PtRec<float, 3>*)recs, sa, ct,
+            kern<<<grid, kRowThreads, smem1, s>>>(g, ks, M, (const PtRec<float, 3>*)recs, sa, ct,
                                                (cplx_t<float>*)ft, nftot, m, use, t0);
             note_launch();
             return cudaSuccess;
