@@ -1,0 +1,68 @@
+"""The row-owned 3D FP32 spread at every width it serves, against the oracle.
+
+spread_rows_kernel serves 3D FP32 type-1 plans with bins 16 x 16 x bz and
+kernel widths 4..8 (one template instance per width), rounding each
+contribution to the fixed-point tile either by one FFMA (tolerance >= 1e-5,
+or a subproblem whose strengths sum to >= 512 times the largest) or by the
+FP32-to-int32 conversion.  Each case runs a type-1 transform through the
+library on complex64 data and compares it with the FP64 oracle
+(oracle/cpu_nufft.py) in relative l2 within 5 max(eps, 1e-6), the bound of
+the other GPU parity tests.  Points: half uniform, half in a tight cluster,
+so that tiles inside the grid (bulk reduce-add), tiles that wrap (per-cell
+atomics), sparse and dense subproblems all occur.
+"""
+import numpy as np
+import pytest
+import torch
+
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SHAPE = (40, 36, 44)  # fine grid 80 x 72 x 88: bins 16 x 16 x 12 cover it with interior and wrapping tiles
+
+
+def _inputs(seed, M, unit_strengths=False):
+    rng = np.random.default_rng(seed)
+    h = M // 2
+    x = [np.concatenate([rng.uniform(-np.pi, np.pi, h), rng.normal(0.3, 0.05, M - h)])
+         for _ in range(3)]
+    if unit_strengths:
+        c = np.exp(2j * np.pi * rng.uniform(size=M))
+    else:
+        c = rng.normal(size=M) + 1j * rng.normal(size=M)
+    return x, c
+
+
+@pytest.mark.parametrize("eps", [1e-3, 1e-4, 1e-5, 1e-6, 1e-7])
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_row_spread_widths_match_oracle(eps, kernel):
+    import jax_finufft_gb300 as jf
+    from jax_finufft_gb300.options import Opts
+    from oracle import cpu_nufft as cn
+
+    x, c = _inputs(17, 40000)
+    out = jf.nufft1(SHAPE, torch.tensor(c.astype(np.complex64), device="cuda"),
+                    *[torch.tensor(v.astype(np.float32), device="cuda") for v in x],
+                    eps=eps, iflag=1, opts=Opts(gpu_kernel=kernel)).cpu().numpy()
+    ref = cn.nufft1(SHAPE, c, *[v.astype(np.float32).astype(np.float64) for v in x], eps=eps,
+                    iflag=1, kernel=kernel)
+    assert np.isfinite(out).all()
+    assert rel_l2(out, ref) < 5 * max(eps, 1e-6), rel_l2(out, ref)
+
+
+def test_row_spread_dense_unit_strengths():
+    """eps 1e-6 (conversion rounding by default) with unit-modulus strengths
+    in a dense cluster: full subproblems sum to 1024 times their largest
+    strength, so they take the FFMA rounding; sparse ones the conversion."""
+    import jax_finufft_gb300 as jf
+    from oracle import cpu_nufft as cn
+
+    x, c = _inputs(29, 60000, unit_strengths=True)
+    eps = 1e-6
+    out = jf.nufft1(SHAPE, torch.tensor(c.astype(np.complex64), device="cuda"),
+                    *[torch.tensor(v.astype(np.float32), device="cuda") for v in x],
+                    eps=eps, iflag=-1).cpu().numpy()
+    ref = cn.nufft1(SHAPE, c, *[v.astype(np.float32).astype(np.float64) for v in x], eps=eps,
+                    iflag=-1)
+    assert rel_l2(out, ref) < 5 * max(eps, 1e-6), rel_l2(out, ref)
