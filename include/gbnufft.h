@@ -7,7 +7,8 @@
  * Every entry point takes plain pointers and sizes.  Device pointers are
  * expected unless a function says otherwise; work is enqueued on the given
  * CUDA stream and never synchronises the host except where noted
- * (type-3 setpts reads the point extents back to size its grid).
+ * (type-3 setpts reads the point extents back to size its grid, unless
+ * they were declared with gbn_set_t3_extents).
  *
  * Return codes follow the reference's convention (lib/kernels.cc.cu:52-55,
  * 70-79): 0 success, 1 warning (tolerance not reachable, clamped; results
@@ -108,6 +109,20 @@ GBN_API int gbn_setpts(gbn_plan plan, int64_t M, const double* x, const double* 
                int64_t N, const double* s, const double* t, const double* u);
 GBN_API int gbnf_setpts(gbn_plan plan, int64_t M, const float* x, const float* y, const float* z,
                 int64_t N, const float* s, const float* t, const float* u);
+
+/* Type 3: declare the extents of the sources (x_lo[d] <= x <= x_hi[d]) and
+ * targets (s_lo[d] <= s <= s_hi[d]) per backend axis (host arrays of dim
+ * doubles) for the following setpts calls.  setpts then sizes the grid from
+ * them instead of measuring the points, so it does not synchronise the host
+ * and is stream-ordered (with unchanged extents and sizes, the inner plan
+ * and buffers are reused, so setpts and execute can be captured into a CUDA
+ * graph after a first call).  Wider extents give a larger grid, same
+ * accuracy.  A finite coordinate outside its declared extent is detected on
+ * the device and makes the next API call on that device return
+ * GBN_ERR_ARGS (the outputs since the previous check are invalid).  All four
+ * pointers NULL: measure the extents again (the default). */
+GBN_API int gbn_set_t3_extents(gbn_plan plan, const double* x_lo, const double* x_hi,
+                               const double* s_lo, const double* s_hi);
 
 /* Execute ntransf transforms.  Type 1: c (ntransf, M) -> f (ntransf, N...).
  * Type 2: f -> c.  Type 3: c (ntransf, M) -> f (ntransf, N). */

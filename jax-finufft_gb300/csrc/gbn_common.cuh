@@ -242,6 +242,18 @@ cudaError_t read_wait_timeouts(unsigned* out, bool reset);
 cudaError_t wait_flag_setup();
 bool wait_flag_take();
 void wait_flag_raise();
+// The second word of that memory: type-3 points found outside the extents a
+// caller declared (gbn_set_t3_extents).  extent_flag_device: its device
+// pointer for the check kernel (null before setup); extent_flag_take: true
+// if raised on the current device since the last take, and clears it.
+unsigned* extent_flag_device();
+bool extent_flag_take();
+
+// Raise *flag (mapped host memory) if any finite coordinate of the n points
+// lies outside [lo[d], hi[d]] on an axis d < dim.
+template <typename TX>
+cudaError_t launch_extent_check(int dim, int64_t n, const TX* const* a, const double* lo,
+                                const double* hi, unsigned* flag, cudaStream_t s);
 
 // Type-3 gradient request: the outer gather of the adjoint also
 // differentiates along the sources (interp_t3grad_kernel).  c: forward
@@ -328,11 +340,24 @@ cudaError_t launch_t3_prephase_factors(int dim, int64_t M, const TX* const* x, c
 // With tau_max > 0 (a bound on |tau|), psihat comes from a piecewise
 // Chebyshev fit checked on the host against the quadrature (relative 1e-14
 // in FP64, 1e-9 in FP32), else from the quadrature per target.
+// A fitted psihat table kept on the device across setpts calls (type-3 plans
+// with declared extents): refitted on the host and uploaded only when its
+// parameters change, so that later setpts calls make no host copy and can be
+// captured into a CUDA graph.  dev is freed by the owner (cudaFree).
+struct T3PsihatCache {
+  double* dev = nullptr;
+  size_t cap = 0;  // doubles allocated at dev
+  bool fitted = false;
+  double tau_max = -1.0, beta = 0.0, h = 0.0;
+  int w = 0, shape = -1, single = -1, P = 0;
+};
+
 template <typename TX, typename TC>
 cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
                                    const double* const* tau, int iflag, int w, double beta,
                                    int shape,
-                                   void* fac, cudaStream_t s, double tau_max = 0.0);
+                                   void* fac, cudaStream_t s, double tau_max = 0.0,
+                                   T3PsihatCache* cache = nullptr);
 
 // Gradient grids: for every transform, E fine grids from its modes `in`
 // (ntr, N): grid e < base holds mode/psihat, grid e >= base holds

@@ -976,10 +976,13 @@ GBN_INST_IGS(float, double)
 GBN_INST_IGS(double, double)
 
 namespace {
+// Per device: two words of mapped pinned host memory, [0] bounded waits that
+// gave up, [1] type-3 points outside declared extents; host and device views.
 struct WaitFlag {
   std::once_flag once;
   cudaError_t err = cudaSuccess;
   volatile unsigned* host = nullptr;
+  unsigned* dev = nullptr;
 };
 constexpr int kMaxDevices = 64;
 WaitFlag g_flags[kMaxDevices];
@@ -997,9 +1000,10 @@ cudaError_t wait_flag_setup() {
   if (!f) return cudaErrorInvalidDevice;
   std::call_once(f->once, [f]() {
     void* h = nullptr;
-    f->err = cudaHostAlloc(&h, sizeof(unsigned), cudaHostAllocMapped | cudaHostAllocPortable);
+    f->err = cudaHostAlloc(&h, 2 * sizeof(unsigned), cudaHostAllocMapped | cudaHostAllocPortable);
     if (f->err != cudaSuccess) return;
-    *(volatile unsigned*)h = 0u;
+    ((volatile unsigned*)h)[0] = 0u;
+    ((volatile unsigned*)h)[1] = 0u;
     void* d = nullptr;
     f->err = cudaHostGetDevicePointer(&d, h, 0);
     if (f->err == cudaSuccess) f->err = cudaMemcpyToSymbol(g_wait_host, &d, sizeof(d));
@@ -1008,6 +1012,7 @@ cudaError_t wait_flag_setup() {
       return;
     }
     f->host = (volatile unsigned*)h;
+    f->dev = (unsigned*)d;
   });
   return f->err;
 }
@@ -1022,6 +1027,18 @@ bool wait_flag_take() {
 void wait_flag_raise() {
   WaitFlag* f = flag_of_current();
   if (f && f->host) *f->host += 1u;
+}
+
+unsigned* extent_flag_device() {
+  WaitFlag* f = flag_of_current();
+  return f && f->dev ? f->dev + 1 : nullptr;
+}
+
+bool extent_flag_take() {
+  WaitFlag* f = flag_of_current();
+  if (!f || !f->host || f->host[1] == 0u) return false;
+  f->host[1] = 0u;
+  return true;
 }
 
 cudaError_t read_wait_timeouts(unsigned* out, bool reset) {

@@ -60,6 +60,10 @@ int check_waits(int r) {
     return fail(GBN_ERR_CUDA,
                 "a bounded device-side wait gave up (tile copy into shared memory): outputs of "
                 "the calls enqueued on this device since the previous check are invalid");
+  if (gbn::extent_flag_take())
+    return fail(GBN_ERR_ARGS,
+                "type-3 points outside the extents given to gbn_set_t3_extents: outputs of the "
+                "calls enqueued on this device since the previous check are invalid");
   return r;
 }
 
@@ -367,6 +371,10 @@ struct gbn_plan_s {
   // type 3
   std::unique_ptr<gbn_plan_s> inner;
   double t3_cx[3] = {0, 0, 0}, t3_cs[3] = {0, 0, 0}, t3_scale[3] = {1, 1, 1};
+  // extents declared by gbn_set_t3_extents: x_lo, x_hi, s_lo, s_hi per axis
+  bool t3_ext = false;
+  double t3_ext_v[4][3] = {};
+  T3PsihatCache t3_tab;  // the psihat table of declared extents, kept on the device
   int64_t Nt = 0;
   DevBuf t3_tau[3], t3_pre, t3_post, t3_cbuf, t3_obuf, t3_minmax;
 
@@ -383,6 +391,7 @@ struct gbn_plan_s {
                       &t3_tau[0], &t3_tau[1], &t3_tau[2], &t3_pre,    &t3_post,   &t3_cbuf,
                       &t3_obuf,   &t3_minmax, &fft_tw[0], &fft_tw[1], &fft_tw[2]};
     for (DevBuf* b : bufs) b->release(stream);
+    if (t3_tab.dev) cudaFree(t3_tab.dev);
     own.stream = stream;
     own.release();
     for (auto& h : ffts) cufftDestroy(h.second);
@@ -847,24 +856,38 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
     const TX* ss[3] = {s, t, u};
     for (int d = 0; d < p->dim; ++d)
       if ((M > 0 && !xs[d]) || (N > 0 && !ss[d])) return fail(GBN_ERR_ARGS, "missing coordinate array");
-    // extents of sources and targets (one host round trip)
-    GBN_CUDA(p->t3_minmax.ensure(sizeof(double) * 12, st));
-    const TX* arrs[6];
-    for (int d = 0; d < p->dim; ++d) {
-      arrs[d] = xs[d];
-      arrs[p->dim + d] = ss[d];
+    // extents of sources and targets: declared (gbn_set_t3_extents; checked
+    // on the device, no host round trip) or measured (one host round trip)
+    double h[12] = {};
+    if (p->t3_ext) {
+      for (int d = 0; d < p->dim; ++d) {
+        h[2 * d] = p->t3_ext_v[0][d];
+        h[2 * d + 1] = p->t3_ext_v[1][d];
+        h[2 * (p->dim + d)] = p->t3_ext_v[2][d];
+        h[2 * (p->dim + d) + 1] = p->t3_ext_v[3][d];
+      }
+      unsigned* flag = extent_flag_device();
+      GBN_CUDA(launch_extent_check<TX>(p->dim, M, xs, p->t3_ext_v[0], p->t3_ext_v[1], flag, st));
+      GBN_CUDA(launch_extent_check<TX>(p->dim, N, ss, p->t3_ext_v[2], p->t3_ext_v[3], flag, st));
+    } else {
+      GBN_CUDA(p->t3_minmax.ensure(sizeof(double) * 12, st));
+      const TX* arrs[6];
+      for (int d = 0; d < p->dim; ++d) {
+        arrs[d] = xs[d];
+        arrs[p->dim + d] = ss[d];
+      }
+      double* mm = p->t3_minmax.as<double>();
+      GBN_CUDA(launch_minmax<TX>(arrs, p->dim, M, mm, st));
+      GBN_CUDA(launch_minmax<TX>(arrs + p->dim, p->dim, N, mm + 2 * p->dim, st));
+      GBN_CUDA(cudaMemcpyAsync(h, mm, sizeof(double) * 4 * p->dim, cudaMemcpyDeviceToHost, st));
+      GBN_CUDA(cudaStreamSynchronize(st));
     }
-    double* mm = p->t3_minmax.as<double>();
-    GBN_CUDA(launch_minmax<TX>(arrs, p->dim, M, mm, st));
-    GBN_CUDA(launch_minmax<TX>(arrs + p->dim, p->dim, N, mm + 2 * p->dim, st));
-    double h[12];
-    GBN_CUDA(cudaMemcpyAsync(h, mm, sizeof(double) * 4 * p->dim, cudaMemcpyDeviceToHost, st));
-    GBN_CUDA(cudaStreamSynchronize(st));
+    const bool have_x = M > 0 || p->t3_ext, have_s = N > 0 || p->t3_ext;
     int64_t nmodes_inner[3] = {1, 1, 1};
     for (int d = 0; d < p->dim; ++d) {
-      const double xmin = M > 0 ? h[2 * d] : 0.0, xmax = M > 0 ? h[2 * d + 1] : 0.0;
-      const double smin = N > 0 ? h[2 * (p->dim + d)] : 0.0;
-      const double smax = N > 0 ? h[2 * (p->dim + d) + 1] : 0.0;
+      const double xmin = have_x ? h[2 * d] : 0.0, xmax = have_x ? h[2 * d + 1] : 0.0;
+      const double smin = have_s ? h[2 * (p->dim + d)] : 0.0;
+      const double smax = have_s ? h[2 * (p->dim + d) + 1] : 0.0;
       p->nf[d] = type3_params(xmin, xmax, smin, smax, p->sigma, p->w, &p->t3_cx[d],
                               &p->t3_cs[d], &p->t3_scale[d]);
       nmodes_inner[d] = p->nf[d];
@@ -872,7 +895,7 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
     for (int d = p->dim; d < 3; ++d) p->nf[d] = 1;
     // bound on |tau| = |s - cs| / scale over the targets (for the psihat fit)
     double tau_max = 0.0;
-    for (int d = 0; d < p->dim && N > 0; ++d) {
+    for (int d = 0; d < p->dim && have_s; ++d) {
       const double smin = h[2 * (p->dim + d)], smax = h[2 * (p->dim + d) + 1];
       const double r = std::max(std::fabs(smin - p->t3_cs[d]), std::fabs(smax - p->t3_cs[d]));
       tau_max = std::max(tau_max, r / p->t3_scale[d]);
@@ -931,7 +954,8 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
                                                        p->iflag, p->t3_pre.p, st)));
       GBN_CUDA((launch_t3_post_factors<TX, float>(p->dim, N, ss, p->t3_cx, ctaus, p->iflag,
                                                    p->w, p->beta, p->opts.gpu_kernel,
-                                                   p->t3_post.p, st, tau_max)));
+                                                   p->t3_post.p, st, tau_max,
+                                                   p->t3_ext ? &p->t3_tab : nullptr)));
     } else {
       GBN_CUDA((launch_t3_prephase_factors<double, double>(p->dim, M, (const double* const*)xs,
                                                            p->t3_cx, p->t3_cs, p->iflag,
@@ -939,7 +963,8 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
       GBN_CUDA((launch_t3_post_factors<double, double>(p->dim, N, (const double* const*)ss,
                                                        p->t3_cx, ctaus, p->iflag, p->w,
                                                        p->beta, p->opts.gpu_kernel,
-                                                       p->t3_post.p, st, tau_max)));
+                                                       p->t3_post.p, st, tau_max,
+                                                       p->t3_ext ? &p->t3_tab : nullptr)));
     }
   }
   if (sev) GBN_CUDA(cudaEventRecord(sev[1], st));
@@ -1694,6 +1719,30 @@ int gbn_grad(gbn_plan plan, gbn_points pts, int ntr, const void* src, const void
 void gbn_clear_cache(void) { cache().clear(); }
 
 long long gbn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int gbn_set_t3_extents(gbn_plan plan, const double* x_lo, const double* x_hi,
+                       const double* s_lo, const double* s_hi) {
+  if (!plan) return fail(GBN_ERR_ARGS, "plan is NULL");
+  if (plan->type != 3) return fail(GBN_ERR_ARGS, "extents are for type-3 plans");
+  if (!x_lo && !x_hi && !s_lo && !s_hi) {
+    plan->t3_ext = false;
+    return GBN_OK;
+  }
+  if (!x_lo || !x_hi || !s_lo || !s_hi)
+    return fail(GBN_ERR_ARGS, "give all four extent arrays, or none to measure the extents");
+  const double* v[4] = {x_lo, x_hi, s_lo, s_hi};
+  for (int d = 0; d < plan->dim; ++d) {
+    for (int k = 0; k < 4; ++k)
+      if (!std::isfinite(v[k][d])) return fail(GBN_ERR_ARGS, "extents must be finite");
+    if (x_lo[d] > x_hi[d] || s_lo[d] > s_hi[d])
+      return fail(GBN_ERR_ARGS, "each extent needs lo <= hi");
+  }
+  GBN_CUDA(wait_flag_setup());
+  for (int k = 0; k < 4; ++k)
+    for (int d = 0; d < 3; ++d) plan->t3_ext_v[k][d] = d < plan->dim ? v[k][d] : 0.0;
+  plan->t3_ext = true;
+  return GBN_OK;
+}
 
 int gbn_wait_timeouts(long long* count, int reset) {
   if (!count) return fail(GBN_ERR_ARGS, "NULL argument");

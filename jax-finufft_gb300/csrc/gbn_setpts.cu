@@ -580,6 +580,9 @@ __global__ void minmax_decode_kernel(const unsigned long long* k, double* out, i
 struct Ptrs3 {
   const void* p[3];
 };
+struct Bounds3 {
+  double lo[3], hi[3];
+};
 struct DPtrs3 {
   double* p[3];
 };
@@ -950,6 +953,44 @@ cudaError_t launch_minmax(const TX* const* arrs, int narr, int64_t n, double* ou
   return cudaGetLastError();
 }
 
+// Declared type-3 extents: a warp with a finite coordinate outside its
+// axis's [lo, hi] raises the flag word once (system-scope atomic on mapped
+// host memory); non-finite coordinates are left to the fold, which treats
+// them as the centre.
+template <typename TX>
+__global__ void extent_check_kernel(int dim, int64_t n, Ptrs3 a, Bounds3 b, unsigned* flag) {
+  bool out = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    for (int d = 0; d < dim; ++d) {
+      const double v = (double)((const TX*)a.p[d])[i];
+      if (isfinite(v) && (v < b.lo[d] || v > b.hi[d])) out = true;
+    }
+  }
+  if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31) == 0) {
+    atomicAdd_system(flag, 1u);
+    __threadfence_system();
+  }
+}
+
+template <typename TX>
+cudaError_t launch_extent_check(int dim, int64_t n, const TX* const* a, const double* lo,
+                                const double* hi, unsigned* flag, cudaStream_t s) {
+  if (n == 0 || flag == nullptr) return cudaSuccess;
+  Ptrs3 ap{};
+  Bounds3 bb{};
+  for (int d = 0; d < dim; ++d) {
+    ap.p[d] = a[d];
+    bb.lo[d] = lo[d];
+    bb.hi[d] = hi[d];
+  }
+  unsigned nb = grid1(n, 256);
+  if (nb > 4096) nb = 4096;
+  extent_check_kernel<TX><<<nb, 256, 0, s>>>(dim, n, ap, bb, flag);
+  note_launch();
+  return cudaGetLastError();
+}
+
 template <typename TX>
 cudaError_t launch_t3_targets(int dim, int64_t N, const TX* const* s, const double* center,
                               const double* scale, double* const* tau, cudaStream_t st) {
@@ -1079,7 +1120,8 @@ bool fit_psihat(const Quad& qd, double tau_max, double rel_tol, int D, std::vect
 template <typename TX, typename TC>
 cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, const double* cx,
                                    const double* const* tau, int iflag, int w, double beta,
-                                   int shape, void* fac, cudaStream_t s, double tau_max) {
+                                   int shape, void* fac, cudaStream_t s, double tau_max,
+                                   T3PsihatCache* cache) {
   if (N == 0) return cudaSuccess;
   const double pi = 3.141592653589793238462643383279502884;
   Quad qd;
@@ -1104,7 +1146,45 @@ cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, cons
   double h = 0.0;
   int P = 0;
   constexpr int D = 20;
-  if (tau_max > 0.0 && fit_psihat(qd, tau_max, sizeof(TC) == 4 ? 1e-9 : 1e-14, D, tab, h, P)) {
+  const int single = sizeof(TC) == 4;
+  if (cache && cache->fitted && cache->tau_max == tau_max && cache->beta == beta &&
+      cache->w == w && cache->shape == shape && cache->single == single) {
+    t3_post_table_kernel<TX, TC><<<grid1(N, 128), 128, 0, s>>>(
+        dim, N, sp, c[0], c[1], c[2], tp, iflag, cache->dev, cache->h, cache->P, D,
+        (cplx_t<TC>*)fac);
+    note_launch();
+    return cudaGetLastError();
+  }
+  if (cache) cache->fitted = false;
+  if (tau_max > 0.0 && fit_psihat(qd, tau_max, single ? 1e-9 : 1e-14, D, tab, h, P)) {
+    if (cache) {
+      // keep the table: a plan-owned device buffer, grown when needed
+      cudaError_t e = cudaSuccess;
+      if (cache->cap < tab.size()) {
+        if (cache->dev) cudaFree(cache->dev);
+        cache->dev = nullptr;
+        cache->cap = 0;
+        e = cudaMalloc(&cache->dev, tab.size() * sizeof(double));
+        if (e != cudaSuccess) return e;
+        cache->cap = tab.size();
+      }
+      // pageable source: the call returns once the host buffer has been consumed
+      e = cudaMemcpyAsync(cache->dev, tab.data(), tab.size() * sizeof(double),
+                          cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) return e;
+      cache->fitted = true;
+      cache->tau_max = tau_max;
+      cache->beta = beta;
+      cache->w = w;
+      cache->shape = shape;
+      cache->single = single;
+      cache->h = h;
+      cache->P = P;
+      t3_post_table_kernel<TX, TC><<<grid1(N, 128), 128, 0, s>>>(
+          dim, N, sp, c[0], c[1], c[2], tp, iflag, cache->dev, h, P, D, (cplx_t<TC>*)fac);
+      note_launch();
+      return cudaGetLastError();
+    }
     double* dtab = nullptr;
     cudaError_t e = cudaMallocAsync(&dtab, tab.size() * sizeof(double), s);
     if (e != cudaSuccess) return e;
@@ -1172,6 +1252,12 @@ template cudaError_t launch_minmax<float>(const float* const*, int, int64_t, dou
                                           cudaStream_t);
 template cudaError_t launch_minmax<double>(const double* const*, int, int64_t, double*,
                                            cudaStream_t);
+template cudaError_t launch_extent_check<float>(int, int64_t, const float* const*,
+                                                const double*, const double*, unsigned*,
+                                                cudaStream_t);
+template cudaError_t launch_extent_check<double>(int, int64_t, const double* const*,
+                                                 const double*, const double*, unsigned*,
+                                                 cudaStream_t);
 template cudaError_t launch_t3_targets<float>(int, int64_t, const float* const*, const double*,
                                               const double*, double* const*, cudaStream_t);
 template cudaError_t launch_t3_targets<double>(int, int64_t, const double* const*,
@@ -1184,7 +1270,7 @@ template cudaError_t launch_t3_targets<double>(int, int64_t, const double* const
   template cudaError_t launch_t3_post_factors<TX, TC>(int, int64_t, const TX* const*,          \
                                                       const double*, const double* const*,     \
                                                       int, int, double, int, void*,            \
-                                                      cudaStream_t, double);
+                                                      cudaStream_t, double, T3PsihatCache*);
 GBN_INST_T3(float, float)
 GBN_INST_T3(double, float)
 GBN_INST_T3(double, double)

@@ -100,6 +100,7 @@ SIGNATURES = {
                                     _vp]),
     "gbn_autotune_clear": (None, [ctypes.c_int]),
     "gbn_wait_timeouts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    "gbn_set_t3_extents": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_double)] * 4),
     "gbn_debug_raise_wait_timeout": (None, []),
     "gbn_binsort_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,
                                            _i64p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
