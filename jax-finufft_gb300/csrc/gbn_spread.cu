@@ -23,6 +23,13 @@
 //     FP64 keeps double atomics.
 //   method 1 (GM): every update is a global atomic; used when the tile would
 //     not fit or when points are not sorted.
+//
+// 3D FP32 plans with bins 16 x 16 x bz and widths 4..8 take the row-owned
+// kernel below (spread_rows_kernel) instead of the G-lane one: the same
+// tile, but one point per warp on lanes laid out so that every atomic
+// instruction reaches distinct banks, contributions rounded by one FFMA
+// where the tolerance allows, and the scale bounded to 0.999 * 2^31 / sum.
+// Batched plans (the work queue) keep the G-lane block.
 #include <cuda_runtime.h>
 
 #include <algorithm>
