@@ -89,9 +89,16 @@ __device__ __forceinline__ float horner_piece(const float (&co)[NCO], float delt
 }
 
 // Whether the row-owned spread serves this geometry (the caller checks the
-// rest: FP32 compute, sorted points, Horner kernel values).
+// rest: FP32 compute, sorted points, Horner kernel values).  Lanes without a
+// cell add zeros up to two tile rows (and one cell) past the last tile; the
+// staged strengths that follow the tiles (maxsub complex values) must cover
+// that reach, so small subproblem sizes take the G-lane kernel.
+inline bool rows_reach_fits(const Geom& g) {
+  return (int64_t)g.maxsub >= 2 * (int64_t)tile_x(g.bs[0], g.w) + 2;
+}
 inline bool rows_fit(const Geom& g, int deg) {
   if (g.dim != 3 || g.bs[0] != 16 || g.bs[1] != 16 || g.w < 4 || g.w > 8) return false;
+  if (!rows_reach_fits(g)) return false;
   return deg + 1 <= (g.w <= 6 ? 9 : 11);
 }
 

@@ -29,7 +29,10 @@
 // tile, but one point per warp on lanes laid out so that every atomic
 // instruction reaches distinct banks, contributions rounded by one FFMA
 // where the tolerance allows, and the scale bounded to 0.999 * 2^31 / sum.
-// Batched plans (the work queue) keep the G-lane block.
+// 2D FP32 plans with bins 16 x 16 or 32 x 32 and widths 4..8 take its 2D
+// counterpart (spread_rows2_kernel: four stacked transforms per block, two
+// points per warp step, integer-product contributions).  Batched plans (the
+// work queue) keep the G-lane block.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -609,6 +612,316 @@ __global__ void __launch_bounds__(kRowThreads)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Row-owned 2D spread: FP32 compute, sorted points, Horner values, widths
+// 4..8, bins BS x BS (BS = 16 or 32), TB stacked transforms per block (one
+// tile each, as spread_sm_block stacks them).  The lane layout of the 3D
+// kernel (RowCfg: part, row r, x offset gl; tile row pitch T0 = tile_x(BS, w)
+// = BS + WV, congruent to WV modulo 16, so every atomic instruction reaches
+// 32 distinct banks), one point per warp at a time: per point and transform
+// ceil(w / R) atomic instructions, at compile-time offsets from one address.
+// Lanes without a cell add an exact zero to the cell their position names:
+// in the tile, at most two rows past its end (inside the next tile or the
+// staged strengths that follow the tiles; zero adds change nothing).
+// Integer products instead of float rounding: the staged strengths become
+// int32, a = round(c S) with S = 0.999 min(2^31 / max, 2^33 / sum) per
+// transform (max and sum of max(|Re c|, |Im c|) over the subproblem), the
+// kernel products Q30 fractions, kq = round(2^30 ky kx) (the y pieces'
+// Horner coefficients carry the 2^30), and a contribution is the high word of
+// the 64-bit a kq + 2^31, round(c S ky kx / 4), by one multiply-add.  Cell
+// sums stay below 2^31 (S sum / 4 < 2^31); the resolution, 4 / S = max(sum /
+// 2^31, max / 2^29) in strength units, is the FP32-to-int32 rounding's
+// sum / 2^31 wherever sum >= 4 max, and finer than an FFMA rounding's
+// max / 2^22 always.
+// ---------------------------------------------------------------------------
+template <int OFF>
+__device__ __forceinline__ void red_imm(uint32_t a, int v) {
+  asm volatile("red.shared.add.s32 [%0+%2], %1;" ::"r"(a), "r"(v), "n"(OFF) : "memory");
+}
+
+// round(a kq / 2^32): the high word of the 64-bit a kq + 2^31
+__device__ __forceinline__ int mul_round_hi(int a, int kq) {
+  int hi;
+  asm("{\n\t.reg .s64 t;\n\t.reg .b32 lo;\n\t"
+      "mad.wide.s32 t, %1, %2, 2147483648;\n\t"
+      "mov.b64 {lo, %0}, t;\n\t}"
+      : "=r"(hi)
+      : "r"(a), "r"(kq));
+  return hi;
+}
+
+template <int W, int BS>
+struct Rows2Cfg {
+  using C = RowCfg<W>;
+  static constexpr int T0 = BS + C::WV;  // = tile_x(BS, W)
+  static constexpr int T1 = BS + W - 1;
+  static constexpr int TILE_B = (T0 * T1 * 8 + 127) & ~127;  // = spread_tile_bytes
+  static constexpr int ROW_B = 8 * C::R * T0;                // one row chunk
+};
+
+// One point's contributions: transform k, row chunk ch at byte offset
+// k TILE_B + ch ROW_B from a.
+template <int W, int BS, int TB, int... I>
+__device__ __forceinline__ void rows2_add(uint32_t a, const int (&ci)[TB],
+                                          const int (&kq)[RowCfg<W>::NCH],
+                                          std::integer_sequence<int, I...>) {
+  using C = RowCfg<W>;
+  using Q = Rows2Cfg<W, BS>;
+  (red_imm<(I / C::NCH) * Q::TILE_B + (I % C::NCH) * Q::ROW_B>(
+       a, mul_round_hi(ci[I / C::NCH], kq[I % C::NCH])),
+   ...);
+}
+
+// One point: kernel values from the warp's table tb ([y 0..7 | x 8..15], y
+// in Q30), integer strengths from the staged ones (word (2 p + part) TB + k).
+template <int W, int BS, int TB>
+__device__ __forceinline__ void rows2_point(const PtRec<float, 2>& rc, int p, const float* tb,
+                                            const int* cint, uint32_t lbase, int org0, int org1,
+                                            int hp, int gl, int r,
+                                            const bool (&on)[RowCfg<W>::NCH]) {
+  using C = RowCfg<W>;
+  using Q = Rows2Cfg<W, BS>;
+  const float4* t4 = reinterpret_cast<const float4*>(tb);
+  const float4 y0 = t4[0], y1 = t4[1];
+  const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+  const float kx = tb[8 + (gl < W ? gl : 0)];
+  int kq[C::NCH];
+#pragma unroll
+  for (int ch = 0; ch < C::NCH; ++ch) {
+    float v = ky[ch * C::R];
+#pragma unroll
+    for (int rr = 1; rr < C::R; ++rr)
+      if (r == rr) v = ky[(ch * C::R + rr) & 7];
+    kq[ch] = on[ch] ? __float2int_rn(v * kx) : 0;
+  }
+  int ci[TB];
+  const int* cp = cint + (2 * p + hp) * TB;
+  if constexpr (TB == 4) {
+    const int4 v = *reinterpret_cast<const int4*>(cp);
+    ci[0] = v.x;
+    ci[1] = v.y;
+    ci[2] = v.z;
+    ci[3] = v.w;
+  } else if constexpr (TB == 2) {
+    const int2 v = *reinterpret_cast<const int2*>(cp);
+    ci[0] = v.x;
+    ci[1] = v.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < TB; ++k) ci[k] = cp[k];
+  }
+  const uint32_t a = lbase + 8u * (uint32_t)((rc.i[0] - org0) + Q::T0 * (rc.i[1] - org1));
+  rows2_add<W, BS, TB>(a, ci, kq, std::make_integer_sequence<int, TB * C::NCH>{});
+}
+
+// The point loop: this warp's points in pairs (p, p + NWARP), p = warp,
+// warp + 2 NWARP, ...; the pair's kernel values by one Horner evaluation per
+// lane (part 0 lanes for the first point, part 1 lanes for the second; lane q
+// < w: y piece q, w <= q < 2w: x piece q - w) into a double-buffered per-warp
+// table, the next pair's records loaded during the current pair.
+template <int W, int BS, int TB, int NT>
+__device__ __forceinline__ void rows2_points(const PtRec<float, 2>* __restrict__ recs, int start,
+                                             int cnt, const int* cint,
+                                             const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
+                                             int org0, int org1, float (*tab)[2][16], int warp,
+                                             int hp, int q, int gl, int r,
+                                             const bool (&on)[RowCfg<W>::NCH]) {
+  constexpr int NWARP = NT / 32;
+  constexpr int STEP = 2 * NWARP;
+  const bool tab_w = q < 2 * W;
+  const int slot = q < W ? q : 8 + q - W;
+  const int axis = q < W ? 1 : 0;
+  const PtRec<float, 2>* rp = recs + start;
+  auto jc = [&](int i) { return i < cnt ? i : cnt - 1; };
+  int buf = 0;
+  PtRec<float, 2> na = rp[warp], nb = rp[jc(warp + NWARP)];
+  for (int p = warp; p < cnt; p += STEP) {
+    const PtRec<float, 2> ra = na, rb = nb;
+    if (p + STEP < cnt) {
+      na = rp[p + STEP];
+      nb = rp[jc(p + STEP + NWARP)];
+    }
+    const PtRec<float, 2>& mine = hp ? rb : ra;
+    const float tv = horner_piece(co, axis ? mine.d[1] : mine.d[0]);
+    if (tab_w) tab[buf][hp][slot] = tv;
+    __syncwarp();
+    rows2_point<W, BS, TB>(ra, p, tab[buf][0], cint, lbase, org0, org1, hp, gl, r, on);
+    if (p + NWARP < cnt)
+      rows2_point<W, BS, TB>(rb, p + NWARP, tab[buf][1], cint, lbase, org0, org1, hp, gl, r,
+                             on);
+    buf ^= 1;
+  }
+}
+
+// Shared memory: TB tiles of TILE_B bytes, then the staged strengths of up to
+// maxsub points (2 TB words each).
+template <typename TD, int W, int BS, int TB, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+    spread_rows2_kernel(Geom g, KerSpec<float> ks, int64_t M,
+                        const PtRec<float, 2>* __restrict__ recs, SubArgs sa,
+                        const cplx_t<TD>* __restrict__ c, cplx_t<float>* __restrict__ fine,
+                        int64_t nftot, int ntr, const __grid_constant__ CUtensorMap tmap,
+                        int use_tma, int t_base) {
+  using C = RowCfg<W>;
+  using Q = Rows2Cfg<W, BS>;
+  constexpr int NWARP = NT / 32;
+  static_assert(NT % (2 * TB) == 0, "a thread converts words of one transform");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ float s_sum[TB][NWARP], s_max[TB][NWARP];
+  __shared__ __align__(16) float s_tab[NWARP][2][2][16];  // [warp][buffer][point][y | x]
+  __shared__ int s_org[2];
+  int start, cnt, bin;
+  if (!sub_range(sa, g, M, blockIdx.x, start, cnt, bin)) return;
+  const int t = TB * (int)blockIdx.y;
+  const int ntb = min(TB, ntr - t);
+  if (threadIdx.x == 0) {
+    const Tile<2> t0(g, bin);
+    s_org[0] = t0.org[0];
+    s_org[1] = t0.org[1];
+  }
+  int* sacc = reinterpret_cast<int*>(smem_raw);
+  {
+    int4* z4 = reinterpret_cast<int4*>(smem_raw);
+    for (int i = threadIdx.x; i < TB * Q::TILE_B / 16; i += NT) z4[i] = make_int4(0, 0, 0, 0);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // stage the strengths (a point's TB gathers in flight together; zeros for
+  // the transforms past ntr) at word (2 p + part) TB + k; per transform the
+  // sum and maximum of max(|Re c|, |Im c|)
+  float* cs = reinterpret_cast<float*>(smem_raw + TB * Q::TILE_B);
+  {
+    float psum[TB], pmax[TB];
+#pragma unroll
+    for (int k = 0; k < TB; ++k) psum[k] = pmax[k] = 0.f;
+    const cplx_t<TD>* ct = c + (int64_t)t * M;
+    for (int p = threadIdx.x; p < cnt; p += NT) {
+      const int64_t j = sa.perm[start + p];
+      float re[TB], im[TB];
+#pragma unroll
+      for (int k = 0; k < TB; ++k) {
+        re[k] = im[k] = 0.f;
+        if (k < ntb) load_c<TD, float>(ct + k * M + j, re[k], im[k]);
+        const float m = fmaxf(fabsf(re[k]), fabsf(im[k]));
+        psum[k] += m;
+        pmax[k] = fmaxf(pmax[k], m);
+      }
+      float* w = cs + 2 * p * TB;
+      if constexpr (TB == 4) {
+        reinterpret_cast<float4*>(w)[0] = make_float4(re[0], re[1], re[2], re[3]);
+        reinterpret_cast<float4*>(w)[1] = make_float4(im[0], im[1], im[2], im[3]);
+      } else if constexpr (TB == 2) {
+        reinterpret_cast<float4*>(w)[0] = make_float4(re[0], re[1], im[0], im[1]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < TB; ++k) {
+          w[k] = re[k];
+          w[TB + k] = im[k];
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < TB; ++k) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        psum[k] += __shfl_xor_sync(0xffffffffu, psum[k], o);
+        pmax[k] = fmaxf(pmax[k], __shfl_xor_sync(0xffffffffu, pmax[k], o));
+      }
+      if (lane == 0) {
+        s_sum[k][warp] = psum[k];
+        s_max[k][warp] = pmax[k];
+      }
+    }
+  }
+  const int hp = lane >> 4, q = lane & 15, gl = q % C::WV, r = q / C::WV;
+  float co[C::NCO];
+  load_coef<float, C::NCO>(co, ks, q < W ? q : q - W, W);  // y piece q, or x piece q - w
+  if (q < W) {
+#pragma unroll
+    for (int n = 0; n < C::NCO; ++n) co[n] *= 1073741824.f;  // y values in Q30
+  }
+  __syncthreads();  // tiles cleared, strengths staged, partial sums written
+  // S (strength -> int32) and 4 / S (tile units -> strength) per transform;
+  // sum == 0 (or denormal): nothing to spread, the tile stays zero
+  float inv[TB], sk = 0.f;
+#pragma unroll
+  for (int k = 0; k < TB; ++k) {
+    float B = 0.f, Mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < NWARP; ++i) {
+      B += s_sum[k][i];
+      Mx = fmaxf(Mx, s_max[k][i]);
+    }
+    float S = 0.f;
+    if (B > 1e-30f) S = fminf(0.999f * 2147483648.f / Mx, 0.999f * 8589934592.f / B);
+    inv[k] = S > 0.f ? 4.f / S : 0.f;
+    if ((int)(threadIdx.x % TB) == k) sk = S;
+  }
+  {
+    int* ci = reinterpret_cast<int*>(cs);
+    for (int i = threadIdx.x; i < 2 * TB * cnt; i += NT) ci[i] = __float2int_rn(cs[i] * sk);
+  }
+  bool on[C::NCH];
+#pragma unroll
+  for (int ch = 0; ch < C::NCH; ++ch) on[ch] = r < C::R && gl < W && ch * C::R + r < W;
+  const uint32_t lbase = smem_addr(sacc) + 4u * (2 * (gl + Q::T0 * r) + hp);
+  const int org0 = s_org[0], org1 = s_org[1];
+  __syncthreads();  // integer strengths written
+  rows2_points<W, BS, TB, NT>(recs, start, cnt, reinterpret_cast<const int*>(cs), co, lbase,
+                              org0, org1, s_tab[warp], warp, hp, q, gl, r, on);
+  __syncthreads();
+
+  const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1];
+  const bool interior =
+      org0 >= 0 && org0 + Q::T0 <= nf0 && org1 >= 0 && org1 + Q::T1 <= nf1;
+  constexpr int ncell = Q::T0 * Q::T1;
+  constexpr int tile_w = Q::TILE_B / 4;
+  if (use_tma && interior && (smem_addr(sacc) & 127u) == 0) {
+    // fixed point -> float in place (four words per access), then one bulk
+    // reduce-add per tile
+    for (int k = 0; k < ntb; ++k) {
+      int4* s4 = reinterpret_cast<int4*>(sacc + k * tile_w);
+      for (int i = threadIdx.x; i < (2 * ncell + 3) / 4; i += NT) {
+        const int4 v = s4[i];
+        s4[i] = make_int4(
+            __float_as_int((float)v.x * inv[k]), __float_as_int((float)v.y * inv[k]),
+            __float_as_int((float)v.z * inv[k]), __float_as_int((float)v.w * inv[k]));
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < ntb; ++k)
+        tma_reduce_add_2d(&tmap, sacc + k * tile_w, 2 * org0, org1 + (t_base + t + k) * nf1);
+      bulk_commit();
+      bulk_wait_read();  // the tiles stay allocated until the copies have read them
+    }
+    return;
+  }
+  for (int k = 0; k < ntb; ++k) {
+    const int* tk = sacc + k * tile_w;
+    cplx_t<float>* ft = fine + (int64_t)(t + k) * nftot;
+    CellWalk cw(threadIdx.x, NT, Q::T0, Q::T1);
+    for (int i = threadIdx.x; i < ncell; i += NT, cw.next()) {
+      const int ar = tk[2 * i], ai = tk[2 * i + 1];
+      if (ar == 0 && ai == 0) continue;
+      const int g0 = wrap_i32(org0 + cw.c0, nf0);
+      const int g1 = wrap_i32(org1 + cw.c1, nf1);
+      atomic_add_c(&ft[g1 * nf0 + g0], (float)ar * inv[k], (float)ai * inv[k]);
+    }
+  }
+}
+
+// Whether spread_rows2_kernel serves this geometry (2D, FP32 compute, sorted,
+// Horner values, widths 4..8, bins 16 x 16 or 32 x 32; the caller checks the
+// rest).
+inline bool rows2_fit(const Geom& g, int deg) {
+  if (g.dim != 2 || g.bs[0] != g.bs[1] || (g.bs[0] != 16 && g.bs[0] != 32) || g.w < 4 ||
+      g.w > 8)
+    return false;
+  if (!rows_reach_fits(g)) return false;
+  return deg + 1 <= (g.w <= 6 ? 9 : 11);
+}
+
 template <typename TC, typename TD, int DIM, int G>
 __global__ void __launch_bounds__(kThreads)
     spread_gm_kernel(Geom g, KerSpec<TC> ks, int64_t M, const PtRec<TC, DIM>* __restrict__ recs,
@@ -746,6 +1059,9 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
   static const bool no_rows = std::getenv("GBN_DISABLE_ROW_SPREAD") != nullptr;
   const bool rows = DIM == 3 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 && !no_rows &&
                     rows_fit(g, ks.deg);
+  // 2D: the row-owned kernel stacks 4 transforms per block or takes one
+  const bool rows2 = DIM == 2 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 && !no_rows &&
+                     rows2_fit(g, ks.deg);
   int TB = 1;
   if (sm && !rows && sizeof(TC) == 4 && G <= 8 && g.stash) {
     if (ntr >= 4 && 4 * smem1 <= 100 * 1024)
@@ -753,6 +1069,7 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     else if (ntr >= 2 && 2 * smem1 <= 100 * 1024)
       TB = 2;
   }
+  if (rows2 && TB == 2) TB = 1;
   for (int t0 = 0; t0 < ntr; t0 += 65535 * TB) {
     const int nt = std::min(ntr - t0, 65535 * TB);
     dim3 grid((unsigned)nblk, (unsigned)((nt + TB - 1) / TB));
@@ -801,6 +1118,49 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
               e = go_rows(spread_rows_kernel<TD, 8>);
               break;
           }
+          if (e != cudaSuccess) return e;
+          e = cudaGetLastError();
+          if (e != cudaSuccess) return e;
+          continue;
+        }
+      }
+      if constexpr (DIM == 2 && sizeof(TC) == 4) {
+        if (rows2) {
+          auto go_rows2 = [&](auto kern, int tb, int nth) -> cudaError_t {
+            const size_t smem = smem1 * tb;
+            cudaError_t er = cudaFuncSetAttribute(
+                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (er != cudaSuccess) return er;
+            dim3 gr((unsigned)nblk, (unsigned)((nt + tb - 1) / tb));
+            kern<<<gr, nth, smem, s>>>(g, ks, M, (const PtRec<float, 2>*)recs, sa, ct,
+                                       (cplx_t<float>*)ft, nftot, nt, m, use, t0);
+            note_launch();
+            return cudaSuccess;
+          };
+          // four stacked transforms: 512-thread blocks (two per SM); one: 256
+#define GBN_ROWS2(W_)                                                                       \
+  e = g.bs[0] == 16 ? (TB == 4 ? go_rows2(spread_rows2_kernel<TD, W_, 16, 4, 512>, 4, 512)       \
+                               : go_rows2(spread_rows2_kernel<TD, W_, 16, 1, 256>, 1, 256))      \
+                    : (TB == 4 ? go_rows2(spread_rows2_kernel<TD, W_, 32, 4, 512>, 4, 512)       \
+                               : go_rows2(spread_rows2_kernel<TD, W_, 32, 1, 256>, 1, 256));
+          switch (g.w) {
+            case 4:
+              GBN_ROWS2(4)
+              break;
+            case 5:
+              GBN_ROWS2(5)
+              break;
+            case 6:
+              GBN_ROWS2(6)
+              break;
+            case 7:
+              GBN_ROWS2(7)
+              break;
+            default:
+              GBN_ROWS2(8)
+              break;
+          }
+#undef GBN_ROWS2
           if (e != cudaSuccess) return e;
           e = cudaGetLastError();
           if (e != cudaSuccess) return e;
