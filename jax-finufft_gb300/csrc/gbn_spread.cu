@@ -623,16 +623,20 @@ __global__ void __launch_bounds__(kRowThreads)
 // Lanes without a cell add an exact zero to the cell their position names:
 // in the tile, at most two rows past its end (inside the next tile or the
 // staged strengths that follow the tiles; zero adds change nothing).
-// Integer products instead of float rounding: the staged strengths become
-// int32, a = round(c S) with S = 0.999 min(2^31 / max, 2^33 / sum) per
-// transform (max and sum of max(|Re c|, |Im c|) over the subproblem), the
-// kernel products Q30 fractions, kq = round(2^30 ky kx) (the y pieces'
-// Horner coefficients carry the 2^30), and a contribution is the high word of
-// the 64-bit a kq + 2^31, round(c S ky kx / 4), by one multiply-add.  Cell
-// sums stay below 2^31 (S sum / 4 < 2^31); the resolution, 4 / S = max(sum /
-// 2^31, max / 2^29) in strength units, is the FP32-to-int32 rounding's
-// sum / 2^31 wherever sum >= 4 max, and finer than an FFMA rounding's
-// max / 2^22 always.
+// Contributions, for all the block's transforms one of:
+//   integer products (RND_IMUL): the staged strengths become int32, a =
+//     round(c S) with S = 0.999 min(2^31 / max, 2^33 / sum) per transform
+//     (max and sum of max(|Re c|, |Im c|) over the subproblem), the kernel
+//     products Q30 fractions, kq = round(2^30 ky kx) (the y pieces' Horner
+//     coefficients carry the 2^30), and a contribution is the high word of
+//     the 64-bit a kq + 2^31, round(c S ky kx / 4), by one multiply-add.
+//     Cell sums stay below 2^31 (S sum / 4 < 2^31); the resolution, 4 / S =
+//     max(sum / 2^31, max / 2^29) in strength units, is the FP32-to-int32
+//     rounding's sum / 2^31 wherever sum >= 4 max;
+//   FFMA rounding (RND_FFMA; tolerance >= 1e-5, or every transform's
+//     strengths sum to >= 512 x their largest): fma(c S 2^-30, 2^30 ky kx,
+//     1.5 2^23) carries round(c S ky kx) in its low bits, with S = 0.999
+//     min(2^31 / sum, 2^22 / max) as in spread_rows_kernel.
 // ---------------------------------------------------------------------------
 template <int OFF>
 __device__ __forceinline__ void red_imm(uint32_t a, int v) {
@@ -660,21 +664,31 @@ struct Rows2Cfg {
 };
 
 // One point's contributions: transform k, row chunk ch at byte offset
-// k TILE_B + ch ROW_B from a.
-template <int W, int BS, int TB, int... I>
-__device__ __forceinline__ void rows2_add(uint32_t a, const int (&ci)[TB],
+// k TILE_B + ch ROW_B from a.  RND_IMUL: integer strengths ci times Q30
+// kernel products kq; RND_FFMA: float strengths cf (times 2^-30) times the
+// same products as floats, rounded by one FFMA each.
+enum { RND_IMUL = 0, RND_FFMA = 1 };
+template <int W, int BS, int TB, int RND, int... I>
+__device__ __forceinline__ void rows2_add(uint32_t a, const int (&ci)[TB], const float (&cf)[TB],
                                           const int (&kq)[RowCfg<W>::NCH],
+                                          const float (&kf)[RowCfg<W>::NCH],
                                           std::integer_sequence<int, I...>) {
   using C = RowCfg<W>;
   using Q = Rows2Cfg<W, BS>;
-  (red_imm<(I / C::NCH) * Q::TILE_B + (I % C::NCH) * Q::ROW_B>(
-       a, mul_round_hi(ci[I / C::NCH], kq[I % C::NCH])),
-   ...);
+  if constexpr (RND == RND_IMUL)
+    (red_imm<(I / C::NCH) * Q::TILE_B + (I % C::NCH) * Q::ROW_B>(
+         a, mul_round_hi(ci[I / C::NCH], kq[I % C::NCH])),
+     ...);
+  else
+    (red_imm<(I / C::NCH) * Q::TILE_B + (I % C::NCH) * Q::ROW_B>(
+         a, __float_as_int(fmaf(cf[I / C::NCH], kf[I % C::NCH], kRoundMagic)) - kRoundMagicBits),
+     ...);
 }
 
 // One point: kernel values from the warp's table tb ([y 0..7 | x 8..15], y
-// in Q30), integer strengths from the staged ones (word (2 p + part) TB + k).
-template <int W, int BS, int TB>
+// in Q30), strengths from the staged ones (word (2 p + part) TB + k: int32
+// for RND_IMUL, float for RND_FFMA).
+template <int W, int BS, int TB, int RND>
 __device__ __forceinline__ void rows2_point(const PtRec<float, 2>& rc, int p, const float* tb,
                                             const int* cint, uint32_t lbase, int org0, int org1,
                                             int hp, int gl, int r,
@@ -686,15 +700,19 @@ __device__ __forceinline__ void rows2_point(const PtRec<float, 2>& rc, int p, co
   const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
   const float kx = tb[8 + (gl < W ? gl : 0)];
   int kq[C::NCH];
+  float kf[C::NCH];
 #pragma unroll
   for (int ch = 0; ch < C::NCH; ++ch) {
     float v = ky[ch * C::R];
 #pragma unroll
     for (int rr = 1; rr < C::R; ++rr)
       if (r == rr) v = ky[(ch * C::R + rr) & 7];
-    kq[ch] = on[ch] ? __float2int_rn(v * kx) : 0;
+    kf[ch] = on[ch] ? v * kx : 0.f;
+    kq[ch] = 0;
+    if constexpr (RND == RND_IMUL) kq[ch] = __float2int_rn(kf[ch]);
   }
   int ci[TB];
+  float cf[TB];
   const int* cp = cint + (2 * p + hp) * TB;
   if constexpr (TB == 4) {
     const int4 v = *reinterpret_cast<const int4*>(cp);
@@ -710,8 +728,10 @@ __device__ __forceinline__ void rows2_point(const PtRec<float, 2>& rc, int p, co
 #pragma unroll
     for (int k = 0; k < TB; ++k) ci[k] = cp[k];
   }
+#pragma unroll
+  for (int k = 0; k < TB; ++k) cf[k] = __int_as_float(ci[k]);
   const uint32_t a = lbase + 8u * (uint32_t)((rc.i[0] - org0) + Q::T0 * (rc.i[1] - org1));
-  rows2_add<W, BS, TB>(a, ci, kq, std::make_integer_sequence<int, TB * C::NCH>{});
+  rows2_add<W, BS, TB, RND>(a, ci, cf, kq, kf, std::make_integer_sequence<int, TB * C::NCH>{});
 }
 
 // The point loop: this warp's points in pairs (p, p + NWARP), p = warp,
@@ -719,7 +739,7 @@ __device__ __forceinline__ void rows2_point(const PtRec<float, 2>& rc, int p, co
 // lane (part 0 lanes for the first point, part 1 lanes for the second; lane q
 // < w: y piece q, w <= q < 2w: x piece q - w) into a double-buffered per-warp
 // table, the next pair's records loaded during the current pair.
-template <int W, int BS, int TB, int NT>
+template <int W, int BS, int TB, int NT, int RND>
 __device__ __forceinline__ void rows2_points(const PtRec<float, 2>* __restrict__ recs, int start,
                                              int cnt, const int* cint,
                                              const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
@@ -745,9 +765,9 @@ __device__ __forceinline__ void rows2_points(const PtRec<float, 2>* __restrict__
     const float tv = horner_piece(co, axis ? mine.d[1] : mine.d[0]);
     if (tab_w) tab[buf][hp][slot] = tv;
     __syncwarp();
-    rows2_point<W, BS, TB>(ra, p, tab[buf][0], cint, lbase, org0, org1, hp, gl, r, on);
+    rows2_point<W, BS, TB, RND>(ra, p, tab[buf][0], cint, lbase, org0, org1, hp, gl, r, on);
     if (p + NWARP < cnt)
-      rows2_point<W, BS, TB>(rb, p + NWARP, tab[buf][1], cint, lbase, org0, org1, hp, gl, r,
+      rows2_point<W, BS, TB, RND>(rb, p + NWARP, tab[buf][1], cint, lbase, org0, org1, hp, gl, r,
                              on);
     buf ^= 1;
   }
@@ -840,34 +860,59 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     for (int n = 0; n < C::NCO; ++n) co[n] *= 1073741824.f;  // y values in Q30
   }
   __syncthreads();  // tiles cleared, strengths staged, partial sums written
-  // S (strength -> int32) and 4 / S (tile units -> strength) per transform;
-  // sum == 0 (or denormal): nothing to spread, the tile stays zero
+  // Rounding for all the block's transforms: one FFMA per contribution
+  // (RND_FFMA) where the tolerance allows its resolution, 2^-22 of the
+  // largest strength, or where every transform's strengths sum to >= 512
+  // times their largest (then the 2^31 sum bound is the tighter one and the
+  // FFMA rounding costs nothing); integer products (RND_IMUL) otherwise.
+  // Per transform: S (strength -> tile units; RND_IMUL: -> int32 strength
+  // units, four of which make a tile unit) and inv (tile units -> strength);
+  // sum == 0 (or denormal): nothing to spread, the tile stays zero.
+  float Bk[TB], Mk[TB];
+  bool ffma = g.coarse_round != 0, dense = true;
+#pragma unroll
+  for (int k = 0; k < TB; ++k) {
+    Bk[k] = Mk[k] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NWARP; ++i) {
+      Bk[k] += s_sum[k][i];
+      Mk[k] = fmaxf(Mk[k], s_max[k][i]);
+    }
+    if (k < ntb && !(Bk[k] >= 512.f * Mk[k])) dense = false;
+  }
+  ffma = ffma || dense;
   float inv[TB], sk = 0.f;
 #pragma unroll
   for (int k = 0; k < TB; ++k) {
-    float B = 0.f, Mx = 0.f;
-#pragma unroll
-    for (int i = 0; i < NWARP; ++i) {
-      B += s_sum[k][i];
-      Mx = fmaxf(Mx, s_max[k][i]);
-    }
     float S = 0.f;
-    if (B > 1e-30f) S = fminf(0.999f * 2147483648.f / Mx, 0.999f * 8589934592.f / B);
-    inv[k] = S > 0.f ? 4.f / S : 0.f;
-    if ((int)(threadIdx.x % TB) == k) sk = S;
+    if (Bk[k] > 1e-30f)
+      S = ffma ? fminf(0.999f * 2147483648.f / Bk[k], 0.999f * 4194304.f / Mk[k])
+               : fminf(0.999f * 2147483648.f / Mk[k], 0.999f * 8589934592.f / Bk[k]);
+    inv[k] = S > 0.f ? (ffma ? 1.f : 4.f) / S : 0.f;
+    // RND_FFMA: the kernel products carry 2^30 (the y coefficients' Q30)
+    if ((int)(threadIdx.x % TB) == k) sk = ffma ? S * (1.f / 1073741824.f) : S;
   }
   {
     int* ci = reinterpret_cast<int*>(cs);
-    for (int i = threadIdx.x; i < 2 * TB * cnt; i += NT) ci[i] = __float2int_rn(cs[i] * sk);
+    if (ffma)
+      for (int i = threadIdx.x; i < 2 * TB * cnt; i += NT) cs[i] *= sk;
+    else
+      for (int i = threadIdx.x; i < 2 * TB * cnt; i += NT) ci[i] = __float2int_rn(cs[i] * sk);
   }
   bool on[C::NCH];
 #pragma unroll
   for (int ch = 0; ch < C::NCH; ++ch) on[ch] = r < C::R && gl < W && ch * C::R + r < W;
   const uint32_t lbase = smem_addr(sacc) + 4u * (2 * (gl + Q::T0 * r) + hp);
   const int org0 = s_org[0], org1 = s_org[1];
-  __syncthreads();  // integer strengths written
-  rows2_points<W, BS, TB, NT>(recs, start, cnt, reinterpret_cast<const int*>(cs), co, lbase,
-                              org0, org1, s_tab[warp], warp, hp, q, gl, r, on);
+  __syncthreads();  // scaled strengths written
+  if (ffma)
+    rows2_points<W, BS, TB, NT, RND_FFMA>(recs, start, cnt, reinterpret_cast<const int*>(cs), co,
+                                          lbase, org0, org1, s_tab[warp], warp, hp, q, gl, r,
+                                          on);
+  else
+    rows2_points<W, BS, TB, NT, RND_IMUL>(recs, start, cnt, reinterpret_cast<const int*>(cs), co,
+                                          lbase, org0, org1, s_tab[warp], warp, hp, q, gl, r,
+                                          on);
   __syncthreads();
 
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1];
