@@ -1890,6 +1890,12 @@ struct gbn_batch_s {
   size_t smem = 0;  // one transform's shared memory (largest problem)
   cudaGraphExec_t gexec = nullptr;
   const void* gkey[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // per-problem stages (sorting, FFTs, deconvolution) of different problems
+  // run on these streams side by side, forked from and joined back to
+  // `stream` (small problems are launch-bound one after another)
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> side_done;
+  cudaEvent_t ev_fork = nullptr;
 
   ~gbn_batch_s() {
     if (stream) cudaStreamSynchronize(stream);
@@ -1901,10 +1907,50 @@ struct gbn_batch_s {
       cudaStreamSynchronize(stream);
       cudaStreamDestroy(stream);
     }
+    for (cudaStream_t t : side) cudaStreamDestroy(t);
+    for (cudaEvent_t e : side_done) cudaEventDestroy(e);
+    if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
   }
 };
+
+namespace {
+
+// Problems in flight side by side in a batch's per-problem stages.
+constexpr int kBatchSideStreams = 8;
+
+// Runs fn(i) for i = 0..n-1, item i with problem sub(i)'s plan on side
+// stream i mod S: the side streams wait for everything already on the
+// batch's stream, and the batch's stream waits for all of them before
+// anything after (also when an item fails, so that a capture stays joined).
+template <typename Sub, typename F>
+int batch_fork(gbn_batch_s* b, int n, Sub sub, F fn) {
+  const int S = (int)b->side.size();
+  if (S == 0 || n < 2) {
+    for (int i = 0; i < n; ++i) GBN_TRY(fn(i));
+    return GBN_OK;
+  }
+  GBN_CUDA(cudaEventRecord(b->ev_fork, b->stream));
+  const int used = std::min(S, n);
+  for (int j = 0; j < used; ++j) GBN_CUDA(cudaStreamWaitEvent(b->side[j], b->ev_fork, 0));
+  int r = GBN_OK;
+  for (int i = 0; i < n && r < 2; ++i) {
+    gbn_plan_s* p = sub(i);
+    p->stream = b->side[i % S];
+    r = fn(i);
+    p->stream = b->stream;
+    p->own.stream = b->stream;
+  }
+  for (int j = 0; j < used; ++j) {
+    const cudaError_t e1 = cudaEventRecord(b->side_done[j], b->side[j]);
+    const cudaError_t e2 = cudaStreamWaitEvent(b->stream, b->side_done[j], 0);
+    if (r < 2 && (e1 != cudaSuccess || e2 != cudaSuccess)) GBN_CUDA(e1 != cudaSuccess ? e1 : e2);
+  }
+  return r;
+}
+
+}  // namespace
 
 namespace {
 
@@ -1926,6 +1972,17 @@ int batch_create(int type, int dim, bool single, int K, const int64_t* nmodes, c
   GBN_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   GBN_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming));
   GBN_CUDA(cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming));
+  if (K >= 2) {
+    GBN_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    for (int j = 0; j < std::min(K, kBatchSideStreams); ++j) {
+      cudaStream_t t = nullptr;
+      cudaEvent_t e = nullptr;
+      GBN_CUDA(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking));
+      b->side.push_back(t);
+      GBN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      b->side_done.push_back(e);
+    }
+  }
   gbn_opts base;
   if (opts)
     base = *opts;
@@ -2036,11 +2093,13 @@ int batch_setpts(gbn_batch_s* b, const TX* x, const TX* y, const TX* z) {
   cudaStream_t s = b->stream;
   FoldSpec fs{};
   fs.mode = 0;
-  for (int k = 0; k < b->K; ++k) {
-    const int64_t o = b->pt_off[k];
-    GBN_TRY(sort_points<TX>(b->sub[k].get(), b->sub[k]->own, b->M[k], x ? x + o : nullptr,
-                            y ? y + o : nullptr, z ? z + o : nullptr, fs));
-  }
+  GBN_TRY(batch_fork(
+      b, b->K, [&](int k) { return b->sub[k].get(); },
+      [&](int k) {
+        const int64_t o = b->pt_off[k];
+        return sort_points<TX>(b->sub[k].get(), b->sub[k]->own, b->M[k], x ? x + o : nullptr,
+                               y ? y + o : nullptr, z ? z + o : nullptr, fs);
+      }));
   if (!b->queue) return GBN_OK;
   std::vector<unsigned char> host;
   if (b->comp_single)
@@ -2085,18 +2144,27 @@ int batch_execute(gbn_batch_s* b, void* c, void* f) {
   const char* no_own = std::getenv("GBN_DISABLE_OWN_FFT");
   const bool own_off = no_own && no_own[0] == '1';
   auto own_k = [&](int k) { return !own_off && b->sub[k]->fft_own; };
+  auto sub_k = [&](int k) { return b->sub[k].get(); };
+  // per problem: the own FFT with the deconvolution fused, or the
+  // deconvolution alone (type 2: before the group FFTs; type 1: after)
+  auto per_problem = [&](int k, bool to_modes) {
+    char* fk = (char*)f + b->f_off[k] * dsz;
+    char* gk = arena + b->grid_off[k] * csz;
+    return own_k(k) ? own_fft(b->sub[k].get(), gk, fk, b->T, b->iflag, to_modes)
+                    : do_deconv(b->sub[k].get(), fk, b->T, to_modes, gk);
+  };
+  // the groups whose problems share one cuFFT pass
+  std::vector<const gbn_batch_s::Group*> cu;
+  for (const auto& g : b->groups)
+    if (!own_k(g.first)) cu.push_back(&g);
+  auto per_group = [&](int i) {
+    const gbn_batch_s::Group& g = *cu[i];
+    return exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag);
+  };
+  auto group_sub = [&](int i) { return b->sub[cu[i]->first].get(); };
   if (b->type == 2) {
-    for (int k = 0; k < b->K; ++k) {
-      char* fk = (char*)f + b->f_off[k] * dsz;
-      char* gk = arena + b->grid_off[k] * csz;
-      if (own_k(k))
-        GBN_TRY(own_fft(b->sub[k].get(), gk, fk, b->T, b->iflag, false));
-      else
-        GBN_TRY(do_deconv(b->sub[k].get(), fk, b->T, false, gk));
-    }
-    for (const auto& g : b->groups)
-      if (!own_k(g.first))
-        GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
+    GBN_TRY(batch_fork(b, b->K, sub_k, [&](int k) { return per_problem(k, false); }));
+    GBN_TRY(batch_fork(b, (int)cu.size(), group_sub, per_group));
     GBN_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(int), s));
     cudaError_t e;
     if (b->comp_single)
@@ -2137,17 +2205,8 @@ int batch_execute(gbn_batch_s* b, void* c, void* f) {
                                               b->item_start.as<int64_t>(), b->counter.as<int>(),
                                               b->T, c, arena, b->smem, s);
     GBN_CUDA(e);
-    for (const auto& g : b->groups)
-      if (!own_k(g.first))
-        GBN_TRY(exec_fft(b->sub[g.first].get(), arena + g.off * csz, g.count * b->T, b->iflag));
-    for (int k = 0; k < b->K; ++k) {
-      char* fk = (char*)f + b->f_off[k] * dsz;
-      char* gk = arena + b->grid_off[k] * csz;
-      if (own_k(k))
-        GBN_TRY(own_fft(b->sub[k].get(), gk, fk, b->T, b->iflag, true));
-      else
-        GBN_TRY(do_deconv(b->sub[k].get(), fk, b->T, true, gk));
-    }
+    GBN_TRY(batch_fork(b, (int)cu.size(), group_sub, per_group));
+    GBN_TRY(batch_fork(b, b->K, sub_k, [&](int k) { return per_problem(k, true); }));
   }
   GBN_CUDA(cudaGetLastError());
   return GBN_OK;
