@@ -686,28 +686,24 @@ __device__ __forceinline__ void rows2_add(uint32_t a, const int (&ci)[TB], const
 }
 
 // One point: kernel values from the warp's table tb ([y 0..7 | x 8..15], y
-// in Q30), strengths from the staged ones (word (2 p + part) TB + k: int32
-// for RND_IMUL, float for RND_FFMA).
+// in Q30; the slots past w hold zeros), strengths from the staged ones (word
+// (2 p + part) TB + k: int32 for RND_IMUL, float for RND_FFMA).  The lane's
+// rows are y slots ch R + r (from its own base tb + r, compile-time offsets),
+// its x value slot xs: a lane without a cell (x offset >= w, row >= w, or r
+// >= R with slot xs a zero) gets zero products without a select.
 template <int W, int BS, int TB, int RND>
 __device__ __forceinline__ void rows2_point(const PtRec<float, 2>& rc, int p, const float* tb,
                                             const int* cint, uint32_t lbase, int org0, int org1,
-                                            int hp, int gl, int r,
-                                            const bool (&on)[RowCfg<W>::NCH]) {
+                                            int hp, int r, int xs) {
   using C = RowCfg<W>;
   using Q = Rows2Cfg<W, BS>;
-  const float4* t4 = reinterpret_cast<const float4*>(tb);
-  const float4 y0 = t4[0], y1 = t4[1];
-  const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-  const float kx = tb[8 + (gl < W ? gl : 0)];
+  const float* ty = tb + r;
+  const float kx = tb[xs];
   int kq[C::NCH];
   float kf[C::NCH];
 #pragma unroll
   for (int ch = 0; ch < C::NCH; ++ch) {
-    float v = ky[ch * C::R];
-#pragma unroll
-    for (int rr = 1; rr < C::R; ++rr)
-      if (r == rr) v = ky[(ch * C::R + rr) & 7];
-    kf[ch] = on[ch] ? v * kx : 0.f;
+    kf[ch] = ty[ch * C::R] * kx;
     kq[ch] = 0;
     if constexpr (RND == RND_IMUL) kq[ch] = __float2int_rn(kf[ch]);
   }
@@ -744,13 +740,23 @@ __device__ __forceinline__ void rows2_points(const PtRec<float, 2>* __restrict__
                                              int cnt, const int* cint,
                                              const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
                                              int org0, int org1, float (*tab)[2][16], int warp,
-                                             int hp, int q, int gl, int r,
-                                             const bool (&on)[RowCfg<W>::NCH]) {
+                                             int hp, int q, int gl, int r) {
+  using C = RowCfg<W>;
   constexpr int NWARP = NT / 32;
   constexpr int STEP = 2 * NWARP;
   const bool tab_w = q < 2 * W;
   const int slot = q < W ? q : 8 + q - W;
   const int axis = q < W ? 1 : 0;
+  // x slot of the lane's value: slot 15 is a zero for w <= 7 (and no lane
+  // needs it at w = 8, where 16 lanes are 2 rows of 8 offsets)
+  const int xs = (gl < W && r < C::R) ? 8 + gl : 15;
+  // zero the warp's tables once: the slots past w are never written
+  {
+    float* t = &tab[0][0][0];
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < 2 * 2 * 16; i += 32) t[i] = 0.f;
+    __syncwarp();
+  }
   const PtRec<float, 2>* rp = recs + start;
   auto jc = [&](int i) { return i < cnt ? i : cnt - 1; };
   int buf = 0;
@@ -765,10 +771,10 @@ __device__ __forceinline__ void rows2_points(const PtRec<float, 2>* __restrict__
     const float tv = horner_piece(co, axis ? mine.d[1] : mine.d[0]);
     if (tab_w) tab[buf][hp][slot] = tv;
     __syncwarp();
-    rows2_point<W, BS, TB, RND>(ra, p, tab[buf][0], cint, lbase, org0, org1, hp, gl, r, on);
+    rows2_point<W, BS, TB, RND>(ra, p, tab[buf][0], cint, lbase, org0, org1, hp, r, xs);
     if (p + NWARP < cnt)
-      rows2_point<W, BS, TB, RND>(rb, p + NWARP, tab[buf][1], cint, lbase, org0, org1, hp, gl, r,
-                             on);
+      rows2_point<W, BS, TB, RND>(rb, p + NWARP, tab[buf][1], cint, lbase, org0, org1, hp, r,
+                                  xs);
     buf ^= 1;
   }
 }
@@ -899,20 +905,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     else
       for (int i = threadIdx.x; i < 2 * TB * cnt; i += NT) ci[i] = __float2int_rn(cs[i] * sk);
   }
-  bool on[C::NCH];
-#pragma unroll
-  for (int ch = 0; ch < C::NCH; ++ch) on[ch] = r < C::R && gl < W && ch * C::R + r < W;
   const uint32_t lbase = smem_addr(sacc) + 4u * (2 * (gl + Q::T0 * r) + hp);
   const int org0 = s_org[0], org1 = s_org[1];
   __syncthreads();  // scaled strengths written
   if (ffma)
     rows2_points<W, BS, TB, NT, RND_FFMA>(recs, start, cnt, reinterpret_cast<const int*>(cs), co,
-                                          lbase, org0, org1, s_tab[warp], warp, hp, q, gl, r,
-                                          on);
+                                          lbase, org0, org1, s_tab[warp], warp, hp, q, gl, r);
   else
     rows2_points<W, BS, TB, NT, RND_IMUL>(recs, start, cnt, reinterpret_cast<const int*>(cs), co,
-                                          lbase, org0, org1, s_tab[warp], warp, hp, q, gl, r,
-                                          on);
+                                          lbase, org0, org1, s_tab[warp], warp, hp, q, gl, r);
   __syncthreads();
 
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1];
