@@ -364,26 +364,20 @@ __device__ __forceinline__ void rows_add_all(uint32_t a, const float (&av)[RowCf
 // times W planes, to the point's cells from shared-memory byte address a (the
 // lane's word of the point's first cell).  Every lane adds on every
 // instruction; a lane without a cell of the point in this chunk (row >= W, x
-// offset >= W, or a lane past the R rows) adds an exact zero (its multiplier
-// is selected, not multiplied, so that unwritten table entries never reach
-// the sum).  Its cell is the one its lane position names: within the tile's
-// rows, or at most two rows past the tile's last plane, inside the staged
-// strengths that follow the tile in shared memory (an atomic add of zero
-// leaves them unchanged), and still on a bank of its own.
+// offset >= W, or a lane past the R rows) adds an exact zero: its y or x
+// kernel value comes from a table slot that holds zero (the table's slots
+// past w are never written).  Its cell is the one its lane position names:
+// within the tile's rows, or at most two rows past the tile's last plane,
+// inside the staged strengths that follow the tile in shared memory (an
+// atomic add of zero leaves them unchanged), and still on a bank of its own.
+// ty: the lane's first row's y value (rows ch R + r at offsets ch R).
 template <int W, bool MAGIC>
-__device__ __forceinline__ void rows_add(uint32_t a, float a0, const float (&ky)[8],
-                                         const float (&kz)[8], int r,
-                                         const bool (&on)[RowCfg<W>::NCH]) {
+__device__ __forceinline__ void rows_add(uint32_t a, float a0, const float* ty,
+                                         const float (&kz)[8]) {
   using C = RowCfg<W>;
   float av[C::NCH];
 #pragma unroll
-  for (int ch = 0; ch < C::NCH; ++ch) {
-    float kyv = ky[ch * C::R];
-#pragma unroll
-    for (int rr = 1; rr < C::R; ++rr)
-      if (r == rr) kyv = ky[(ch * C::R + rr) & 7];
-    av[ch] = on[ch] ? a0 * kyv : 0.f;
-  }
+  for (int ch = 0; ch < C::NCH; ++ch) av[ch] = a0 * ty[ch * C::R];
   rows_add_all<W, MAGIC>(a, av, kz, std::make_integer_sequence<int, C::NCH * W>{});
 }
 
@@ -408,8 +402,7 @@ __device__ __forceinline__ void rows_pair(const PtRec<float, 3>& ra, const PtRec
                                           bool two, int p, const float2* cst, float scale,
                                           const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
                                           unsigned org_cell, float (*tb)[24], const RowTab& rt,
-                                          int hp, int gl, int r,
-                                          const bool (&on)[RowCfg<W>::NCH]) {
+                                          int hp, int r, int xs) {
   using C = RowCfg<W>;
   constexpr int NWARP = kRowThreads / 32;
   const float2 ca = cst[p], cb = cst[two ? p + NWARP : p];
@@ -428,20 +421,17 @@ __device__ __forceinline__ void rows_pair(const PtRec<float, 3>& ra, const PtRec
     tb[1][rt.slot] = tvb;
   }
   __syncwarp();
-  const int xs = 16 + (gl < W ? gl : 0);
   {
     const float4* t4 = reinterpret_cast<const float4*>(tb[0]);
-    const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
+    const float4 z0 = t4[0], z1 = t4[1];
     const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
-    const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-    rows_add<W, MAGIC>(aa, (hp ? ca.y : ca.x) * scale * tb[0][xs], ky, kz, r, on);
+    rows_add<W, MAGIC>(aa, (hp ? ca.y : ca.x) * scale * tb[0][xs], tb[0] + 8 + r, kz);
   }
   if (two) {
     const float4* t4 = reinterpret_cast<const float4*>(tb[1]);
-    const float4 z0 = t4[0], z1 = t4[1], y0 = t4[2], y1 = t4[3];
+    const float4 z0 = t4[0], z1 = t4[1];
     const float kz[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
-    const float ky[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-    rows_add<W, MAGIC>(ab, (hp ? cb.y : cb.x) * scale * tb[1][xs], ky, kz, r, on);
+    rows_add<W, MAGIC>(ab, (hp ? cb.y : cb.x) * scale * tb[1][xs], tb[1] + 8 + r, kz);
   }
 }
 
@@ -457,11 +447,20 @@ __device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ 
                                             int cnt, const float2* cst, float scale,
                                             const float (&co)[RowCfg<W>::NCO], uint32_t lbase,
                                             unsigned org_cell, float (*tab)[2][24], int warp,
-                                            int hp, int q, int gl, int r,
-                                            const bool (&on)[RowCfg<W>::NCH]) {
+                                            int hp, int q, int gl, int r) {
   constexpr int NWARP = kRowThreads / 32;
   constexpr int STEP = 2 * NWARP;
   const RowTab rt(hp, q, W);
+  // x slot of the lane's value: slot 23 is a zero for w <= 7 (and no lane
+  // needs it at w = 8, where 16 lanes are 2 rows of 8 offsets)
+  const int xs = (gl < W && r < RowCfg<W>::R) ? 16 + gl : 23;
+  // zero the warp's tables once: the slots past w are never written
+  {
+    float* t = &tab[0][0][0];
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < 2 * 2 * 24; i += 32) t[i] = 0.f;
+    __syncwarp();
+  }
   const PtRec<float, 3>* rp = recs + start;
   auto jc = [&](int p) { return p < cnt ? p : cnt - 1; };
   int p = warp;
@@ -473,7 +472,7 @@ __device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ 
       yb = rp[jc(p + STEP + NWARP)];
     }
     rows_pair<W, MAGIC>(xa, xb, p + NWARP < cnt, p, cst, scale, co, lbase, org_cell, tab[0], rt,
-                        hp, gl, r, on);
+                        hp, r, xs);
     p += STEP;
     if (p >= cnt) break;
     if (p + STEP < cnt) {
@@ -481,7 +480,7 @@ __device__ __forceinline__ void rows_points(const PtRec<float, 3>* __restrict__ 
       xb = rp[jc(p + STEP + NWARP)];
     }
     rows_pair<W, MAGIC>(ya, yb, p + NWARP < cnt, p, cst, scale, co, lbase, org_cell, tab[1], rt,
-                        hp, gl, r, on);
+                        hp, r, xs);
     p += STEP;
     if (p >= cnt) break;
   }
@@ -562,9 +561,6 @@ __global__ void __launch_bounds__(kRowThreads)
     if (magic) scale = fminf(scale, 0.999f * 4194304.f / Mx);
   }
   const float inv = scale > 0.f ? 1.f / scale : 0.f;
-  bool on[C::NCH];
-#pragma unroll
-  for (int ch = 0; ch < C::NCH; ++ch) on[ch] = r < C::R && gl < W && ch * C::R + r < W;
   const uint32_t lbase = smem_addr(sacc) + 4u * (2 * (gl + C::PY * r) + hp);
   const int org[3] = {s_org[0], s_org[1], s_org[2]};
   const int T2 = g.bs[2] + W - 1, ncell = C::PZ * T2;
@@ -573,10 +569,10 @@ __global__ void __launch_bounds__(kRowThreads)
   const unsigned org_cell = (unsigned)org[0] + C::PY * (unsigned)org[1] + C::PZ * (unsigned)org[2];
   if (magic)
     rows_points<W, true>(recs, start, cnt, cst, scale, co, lbase, org_cell, s_tab[warp], warp,
-                         hp, q, gl, r, on);
+                         hp, q, gl, r);
   else
     rows_points<W, false>(recs, start, cnt, cst, scale, co, lbase, org_cell, s_tab[warp], warp,
-                          hp, q, gl, r, on);
+                          hp, q, gl, r);
   __syncthreads();
 
   const int nf0 = (int)g.nf[0], nf1 = (int)g.nf[1], nf2 = (int)g.nf[2];
