@@ -139,6 +139,39 @@ int64_t fine_size(int64_t n, double sigma, int w) {
   return next235even(m);
 }
 
+// Upsampling factor of a type-3 plan's inner FP32 type-2 transform: a little
+// below 2 where that puts every axis of its fine grid on a power of two
+// (128..1024: the library's own pruned FFT with the deconvolution fused,
+// against cuFFT on the 2,3,5-smooth sizes of sigma = 2) without widening
+// the kernel; sigma = 2 otherwise.  The width and shape parameter follow the
+// published rules for the factor chosen, which hold the tolerance.
+double inner_sigma_pow2(int dim, const int64_t* n, double eps, int shape) {
+  int w2 = 0;
+  double b2 = 0.0;
+  kernel_params(eps, 2.0, shape, &w2, &b2);
+  int64_t P[3] = {1, 1, 1}, nf2[3] = {1, 1, 1};
+  double sig = 2.0;
+  bool already = true;
+  for (int d = 0; d < dim; ++d) {
+    nf2[d] = fine_size(n[d], 2.0, w2);
+    int64_t q = 1;
+    while (q * 2 <= nf2[d]) q *= 2;
+    if (q < 128 || q > 1024 || (double)q < 1.5 * (double)n[d]) return 2.0;
+    P[d] = q;
+    if (q != nf2[d]) already = false;
+    sig = std::min(sig, (double)q / (double)n[d]);
+  }
+  if (already) return 2.0;
+  sig *= 1.0 - 1e-12;  // ceil(sig n) stays at the power of two
+  int w = 0;
+  double b = 0.0;
+  kernel_params(eps, sig, shape, &w, &b);
+  if (w != w2) return 2.0;
+  for (int d = 0; d < dim; ++d)
+    if (fine_size(n[d], sig, w) != P[d]) return 2.0;
+  return fft_pow2_supported(dim, P, 1) ? sig : 2.0;
+}
+
 double kernel_value(double t, int w, double beta, int shape) {
   const double z = 2.0 * t / (double)w;
   const double s = 1.0 - z * z;
@@ -917,6 +950,9 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
       io.gpu_precision = 0;
       io.debug = 0;
       io.gpu_maxbatchsize = p->batch;
+      if (p->comp_single && p->sigma == 2.0)
+        io.upsampfac = inner_sigma_pow2(p->dim, nmodes_inner, std::max(p->eps, 1e-7),
+                                        p->opts.gpu_kernel);
       gbn_plan_s* ip = nullptr;
       int r = plan_create(2, p->dim, nmodes_inner, p->iflag, p->batch, p->eps, p->comp_single,
                           &io, (void*)st, &ip);
