@@ -340,10 +340,11 @@ cudaError_t launch_t3_prephase_factors(int dim, int64_t M, const TX* const* x, c
 // With tau_max > 0 (a bound on |tau|), psihat comes from a piecewise
 // Chebyshev fit checked on the host against the quadrature (relative 1e-14
 // in FP64, 1e-9 in FP32), else from the quadrature per target.
-// A fitted psihat table kept on the device across setpts calls (type-3 plans
-// with declared extents): refitted on the host and uploaded only when its
-// parameters change, so that later setpts calls make no host copy and can be
-// captured into a CUDA graph.  dev is freed by the owner (cudaFree).
+// A fitted psihat table kept on the device across setpts calls of a type-3
+// plan: refitted on the host and uploaded only when the kernel changes or
+// the |tau| bound grows past the one it was fitted for, so that later setpts
+// calls skip the fit (and, with declared extents, make no host copy and can
+// be captured into a CUDA graph).  dev is freed by the owner (cudaFree).
 struct T3PsihatCache {
   double* dev = nullptr;
   size_t cap = 0;  // doubles allocated at dev

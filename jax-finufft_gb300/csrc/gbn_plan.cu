@@ -407,7 +407,7 @@ struct gbn_plan_s {
   // extents declared by gbn_set_t3_extents: x_lo, x_hi, s_lo, s_hi per axis
   bool t3_ext = false;
   double t3_ext_v[4][3] = {};
-  T3PsihatCache t3_tab;  // the psihat table of declared extents, kept on the device
+  T3PsihatCache t3_tab;  // the fitted psihat table, kept on the device across setpts calls
   int64_t Nt = 0;
   DevBuf t3_tau[3], t3_pre, t3_post, t3_cbuf, t3_obuf, t3_minmax;
 
@@ -991,7 +991,7 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
       GBN_CUDA((launch_t3_post_factors<TX, float>(p->dim, N, ss, p->t3_cx, ctaus, p->iflag,
                                                    p->w, p->beta, p->opts.gpu_kernel,
                                                    p->t3_post.p, st, tau_max,
-                                                   p->t3_ext ? &p->t3_tab : nullptr)));
+                                                   &p->t3_tab)));
     } else {
       GBN_CUDA((launch_t3_prephase_factors<double, double>(p->dim, M, (const double* const*)xs,
                                                            p->t3_cx, p->t3_cs, p->iflag,
@@ -1000,7 +1000,7 @@ int plan_setpts(gbn_plan_s* p, int64_t M, const TX* x, const TX* y, const TX* z,
                                                        p->t3_cx, ctaus, p->iflag, p->w,
                                                        p->beta, p->opts.gpu_kernel,
                                                        p->t3_post.p, st, tau_max,
-                                                       p->t3_ext ? &p->t3_tab : nullptr)));
+                                                       &p->t3_tab)));
     }
   }
   if (sev) GBN_CUDA(cudaEventRecord(sev[1], st));

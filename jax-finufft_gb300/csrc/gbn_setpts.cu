@@ -1147,7 +1147,8 @@ cudaError_t launch_t3_post_factors(int dim, int64_t N, const TX* const* sx, cons
   int P = 0;
   constexpr int D = 20;
   const int single = sizeof(TC) == 4;
-  if (cache && cache->fitted && cache->tau_max == tau_max && cache->beta == beta &&
+  // a table fitted for a larger |tau| bound covers this one (same kernel)
+  if (cache && cache->fitted && tau_max <= cache->tau_max && cache->beta == beta &&
       cache->w == w && cache->shape == shape && cache->single == single) {
     t3_post_table_kernel<TX, TC><<<grid1(N, 128), 128, 0, s>>>(
         dim, N, sp, c[0], c[1], c[2], tp, iflag, cache->dev, cache->h, cache->P, D,
