@@ -546,7 +546,19 @@ __global__ void minmax_kernel(const TX* __restrict__ a, int64_t n, unsigned long
     lo = l2 < lo ? l2 : lo;
     hi = h2 > hi ? h2 : hi;
   }
-  if ((threadIdx.x & 31) == 0) {
+  // one atomic pair per block (all blocks' atomics meet at one address)
+  __shared__ unsigned long long s_lo[32], s_hi[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    s_lo[warp] = lo;
+    s_hi[warp] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < nw; ++i) {
+      lo = s_lo[i] < lo ? s_lo[i] : lo;
+      hi = s_hi[i] > hi ? s_hi[i] : hi;
+    }
     atomicMin(&out[0], lo);
     atomicMax(&out[1], hi);
   }
@@ -592,14 +604,40 @@ struct CDPtrs3 {
 
 template <typename TX>
 __global__ void t3_targets_kernel(int dim, int64_t N, Ptrs3 s, double c0, double c1, double c2,
-                                  double sc0, double sc1, double sc2, DPtrs3 tau) {
+                                  double isc0, double isc1, double isc2, DPtrs3 tau) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= N) return;
-  const double c[3] = {c0, c1, c2}, sc[3] = {sc0, sc1, sc2};
+  // isc: reciprocal scales (a multiply where a division would run on the
+  // FP64 pipe's slow path; the result differs by at most an ulp)
+  const double c[3] = {c0, c1, c2}, isc[3] = {isc0, isc1, isc2};
   for (int d = 0; d < dim; ++d) {
     double v = (double)((const TX*)s.p[d])[k];
-    tau.p[d][k] = isfinite(v) ? (v - c[d]) / sc[d] : 0.0;
+    tau.p[d][k] = isfinite(v) ? (v - c[d]) * isc[d] : 0.0;
   }
+}
+
+// e^{i ph} / den into a compute-precision complex.  FP32: the phase is
+// reduced to [-pi, pi] in FP64 (|ph| / 2 pi cycles removed exactly enough:
+// ph - 2 pi k by one FMA) and its sine and cosine taken in FP32, whose
+// rounding matches the FP32 output; FP64 throughout otherwise.
+template <typename TC>
+__device__ __forceinline__ cplx_t<TC> phase_over(double ph, double den) {
+  cplx_t<TC> o;
+  if constexpr (sizeof(TC) == 4) {
+    const double k = rint(ph * 0.15915494309189535);  // 1 / (2 pi)
+    const float pr = (float)fma(-k, 6.283185307179586, ph);
+    float sn, cn;
+    sincosf(pr, &sn, &cn);
+    const float inv = 1.0f / (float)den;
+    o.x = cn * inv;
+    o.y = sn * inv;
+  } else {
+    double sn, cn;
+    sincos(ph, &sn, &cn);
+    o.x = cn / den;
+    o.y = sn / den;
+  }
+  return o;
 }
 
 template <typename TX, typename TC>
@@ -615,12 +653,7 @@ __global__ void t3_pre_kernel(int dim, int64_t M, Ptrs3 x, double cx0, double cx
     if (!isfinite(v)) v = cx[d];
     ph += cs[d] * (v - cx[d]);
   }
-  double sn, cn;
-  sincos((double)iflag * ph, &sn, &cn);
-  cplx_t<TC> o;
-  o.x = (TC)cn;
-  o.y = (TC)sn;
-  fac[j] = o;
+  fac[j] = phase_over<TC>((double)iflag * ph, 1.0);
 }
 
 constexpr int kMaxQuad = 64;
@@ -646,12 +679,7 @@ __global__ void t3_post_kernel(int dim, int64_t N, Ptrs3 s, double cx0, double c
     for (int i = 0; i < qd.q; ++i) acc += qd.f[i] * cos(tv * qd.t[i]);
     den *= acc;
   }
-  double sn, cn;
-  sincos((double)iflag * ph, &sn, &cn);
-  cplx_t<TC> o;
-  o.x = (TC)(cn / den);
-  o.y = (TC)(sn / den);
-  fac[k] = o;
+  fac[k] = phase_over<TC>((double)iflag * ph, den);
 }
 
 // The same factors with psihat from a piecewise Chebyshev table: piece
@@ -684,12 +712,7 @@ __global__ void t3_post_table_kernel(int dim, int64_t N, Ptrs3 s, double cx0, do
     }
     den *= fma(x, b1, c[0] - b2);
   }
-  double sn, cn;
-  sincos((double)iflag * ph, &sn, &cn);
-  cplx_t<TC> o;
-  o.x = (TC)(cn / den);
-  o.y = (TC)(sn / den);
-  fac[k] = o;
+  fac[k] = phase_over<TC>((double)iflag * ph, den);
 }
 
 template <typename TI, typename TO, typename TF>
@@ -943,7 +966,7 @@ cudaError_t launch_minmax(const TX* const* arrs, int narr, int64_t n, double* ou
   minmax_init_kernel<<<1, 32, 0, s>>>(keys, narr);
   note_launch();
   unsigned nb = grid1(n, 256);
-  if (nb > 4096) nb = 4096;
+  if (nb > 1024) nb = 1024;
   if (nb == 0) nb = 1;
   for (int a = 0; a < narr; ++a)
     if (n > 0) minmax_kernel<TX><<<nb, 256, 0, s>>>(arrs[a], n, keys + 2 * a);
@@ -985,7 +1008,7 @@ cudaError_t launch_extent_check(int dim, int64_t n, const TX* const* a, const do
     bb.hi[d] = hi[d];
   }
   unsigned nb = grid1(n, 256);
-  if (nb > 4096) nb = 4096;
+  if (nb > 1024) nb = 1024;
   extent_check_kernel<TX><<<nb, 256, 0, s>>>(dim, n, ap, bb, flag);
   note_launch();
   return cudaGetLastError();
@@ -1002,7 +1025,7 @@ cudaError_t launch_t3_targets(int dim, int64_t N, const TX* const* s, const doub
     sp.p[d] = s[d];
     tp.p[d] = tau[d];
     c[d] = center[d];
-    sc[d] = scale[d];
+    sc[d] = 1.0 / scale[d];
   }
   t3_targets_kernel<TX><<<grid1(N, 256), 256, 0, st>>>(dim, N, sp, c[0], c[1], c[2], sc[0],
                                                        sc[1], sc[2], tp);
