@@ -2,11 +2,12 @@
 
 spread_rows_kernel serves 3D FP32 type-1 plans with bins 16 x 16 x bz and
 kernel widths 4..8 (one template instance per width); spread_rows2_kernel
-2D plans with bins 16 x 16 or 32 x 32, one or four stacked transforms per
-block, with integer-product contributions.  The 3D kernel rounds each
-contribution to the fixed-point tile either by one FFMA (tolerance >= 1e-5,
-or a subproblem whose strengths sum to >= 512 times the largest) or by the
-FP32-to-int32 conversion.  Each case runs a type-1 transform through the
+2D plans with bins 16 x 16 (the type-1 FP32 default) or 32 x 32, one or
+four stacked transforms per block.  Both round each contribution to the
+fixed-point tile by one FFMA where the tolerance is >= 1e-5 or a
+subproblem's strengths sum to >= 512 times the largest; otherwise the 3D
+kernel uses the FP32-to-int32 conversion and the 2D kernel integer products
+(int32 strengths times Q30 kernel products).  Each case runs a type-1 transform through the
 library on complex64 data and compares it with the FP64 oracle
 (oracle/cpu_nufft.py) in relative l2 within 5 max(eps, 1e-6), the bound of
 the other GPU parity tests.  Points: half uniform, half in a tight cluster,
@@ -92,12 +93,12 @@ def test_row_spread_2d_widths_match_oracle(eps, kernel, T):
     assert rel_l2(out, ref) < 5 * max(eps, 1e-6), rel_l2(out, ref)
 
 
-@pytest.mark.parametrize("bins,maxsub", [((16, 16), 0), ((32, 32), 40), ((16, 32), 0)])
+@pytest.mark.parametrize("bins,maxsub", [((32, 32), 0), ((32, 32), 40), ((16, 32), 0)])
 def test_row_spread_2d_bins_and_small_subproblems(bins, maxsub):
-    """Bins 16 x 16 (the narrowest row layout); subproblems too small for the
-    row-owned kernel's zero-add reach (maxsub 40 < 2 * 40 + 2 cells); bins
-    16 x 32, which it does not serve: the last two take the G-lane kernel.
-    All against the oracle."""
+    """Bins 32 x 32 (the wider row layout; type-1 FP32 plans default to
+    16 x 16); subproblems too small for the row-owned kernel's zero-add reach
+    (maxsub 40 < 2 * 40 + 2 cells); bins 16 x 32, which it does not serve:
+    the last two take the G-lane kernel.  All against the oracle."""
     import jax_finufft_gb300 as jf
     from jax_finufft_gb300.options import Opts
     from oracle import cpu_nufft as cn
