@@ -756,6 +756,7 @@ __device__ __forceinline__ void rows2_points(const PtRec<float, 2>* __restrict__
   const PtRec<float, 2>* rp = recs + start;
   auto jc = [&](int i) { return i < cnt ? i : cnt - 1; };
   int buf = 0;
+  if (warp >= cnt) return;  // (no record of this subproblem to load)
   PtRec<float, 2> na = rp[warp], nb = rp[jc(warp + NWARP)];
   for (int p = warp; p < cnt; p += STEP) {
     const PtRec<float, 2> ra = na, rb = nb;
