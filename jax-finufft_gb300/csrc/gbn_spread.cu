@@ -29,10 +29,11 @@
 // tile, but one point per warp on lanes laid out so that every atomic
 // instruction reaches distinct banks, contributions rounded by one FFMA
 // where the tolerance allows, and the scale bounded to 0.999 * 2^31 / sum.
-// 2D FP32 plans with bins 16 x 16 or 32 x 32 and widths 4..8 take its 2D
-// counterpart (spread_rows2_kernel: four stacked transforms per block, two
-// points per warp step, integer-product contributions).  Batched plans (the
-// work queue) keep the G-lane block.
+// 2D FP32 plans of four or more stacked transforms with bins 16 x 16 or
+// 32 x 32 and widths 4..8 take its 2D counterpart (spread_rows2_kernel: four
+// transforms per block, two points per warp step, integer-product
+// contributions below 1e-5).  Batched plans (the work queue) keep the G-lane
+// block.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(kRowThreads)
 // ---------------------------------------------------------------------------
 // Row-owned 2D spread: FP32 compute, sorted points, Horner values, widths
 // 4..8, bins BS x BS (BS = 16 or 32), TB stacked transforms per block (one
-// tile each, as spread_sm_block stacks them).  The lane layout of the 3D
+// tile each, as spread_sm_block stacks them; run_spread launches TB = 4).  The lane layout of the 3D
 // kernel (RowCfg: part, row r, x offset gl; tile row pitch T0 = tile_x(BS, w)
 // = BS + WV, congruent to WV modulo 16, so every atomic instruction reaches
 // 32 distinct banks), one point per warp at a time: per point and transform
@@ -1102,9 +1103,11 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
   static const bool no_rows = std::getenv("GBN_DISABLE_ROW_SPREAD") != nullptr;
   const bool rows = DIM == 3 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 && !no_rows &&
                     rows_fit(g, ks.deg);
-  // 2D: the row-owned kernel stacks 4 transforms per block or takes one
-  const bool rows2 = DIM == 2 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 && !no_rows &&
-                     rows2_fit(g, ks.deg);
+  // 2D: the row-owned kernel where four transforms share each block (with
+  // fewer the G-lane kernel measured faster: one transform of 4e6 points on
+  // a 1024^2 grid, 0.26 against 0.32 ms at eps 1e-6)
+  const bool rows2_fits = DIM == 2 && sizeof(TC) == 4 && sm && g.stash && ks.meth == 1 &&
+                          !no_rows && rows2_fit(g, ks.deg);
   int TB = 1;
   if (sm && !rows && sizeof(TC) == 4 && G <= 8 && g.stash) {
     if (ntr >= 4 && 4 * smem1 <= 100 * 1024)
@@ -1112,7 +1115,7 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
     else if (ntr >= 2 && 2 * smem1 <= 100 * 1024)
       TB = 2;
   }
-  if (rows2 && TB == 2) TB = 1;
+  const bool rows2 = rows2_fits && TB == 4;
   for (int t0 = 0; t0 < ntr; t0 += 65535 * TB) {
     const int nt = std::min(ntr - t0, 65535 * TB);
     dim3 grid((unsigned)nblk, (unsigned)((nt + TB - 1) / TB));
@@ -1180,12 +1183,10 @@ cudaError_t run_spread(const Geom& g, const KerSpec<TC>& ks, int method, int64_t
             note_launch();
             return cudaSuccess;
           };
-          // four stacked transforms: 512-thread blocks (two per SM); one: 256
-#define GBN_ROWS2(W_)                                                                       \
-  e = g.bs[0] == 16 ? (TB == 4 ? go_rows2(spread_rows2_kernel<TD, W_, 16, 4, 512>, 4, 512)       \
-                               : go_rows2(spread_rows2_kernel<TD, W_, 16, 1, 256>, 1, 256))      \
-                    : (TB == 4 ? go_rows2(spread_rows2_kernel<TD, W_, 32, 4, 512>, 4, 512)       \
-                               : go_rows2(spread_rows2_kernel<TD, W_, 32, 1, 256>, 1, 256));
+          // four stacked transforms per 512-thread block (two blocks per SM)
+#define GBN_ROWS2(W_)                                                          \
+  e = g.bs[0] == 16 ? go_rows2(spread_rows2_kernel<TD, W_, 16, 4, 512>, 4, 512) \
+                    : go_rows2(spread_rows2_kernel<TD, W_, 32, 4, 512>, 4, 512);
           switch (g.w) {
             case 4:
               GBN_ROWS2(4)

@@ -2,8 +2,8 @@
 
 spread_rows_kernel serves 3D FP32 type-1 plans with bins 16 x 16 x bz and
 kernel widths 4..8 (one template instance per width); spread_rows2_kernel
-2D plans with bins 16 x 16 (the type-1 FP32 default) or 32 x 32, one or
-four stacked transforms per block.  Both round each contribution to the
+2D plans of four or more stacked transforms with bins 16 x 16 (the type-1
+FP32 default) or 32 x 32, four transforms per block.  Both round each contribution to the
 fixed-point tile by one FFMA where the tolerance is >= 1e-5 or a
 subproblem's strengths sum to >= 512 times the largest; otherwise the 3D
 kernel uses the FP32-to-int32 conversion and the 2D kernel integer products
@@ -77,8 +77,9 @@ def test_row_spread_dense_unit_strengths():
 @pytest.mark.parametrize("kernel", [0, 1])
 @pytest.mark.parametrize("T", [None, 6])
 def test_row_spread_2d_widths_match_oracle(eps, kernel, T):
-    """2D: one transform (a block per transform) and six stacked transforms
-    (blocks of four, then a block of two)."""
+    """2D: one transform (the G-lane kernel, which serves fewer than four
+    stacked transforms) and six stacked transforms (row-owned blocks of four,
+    then a block of two)."""
     import jax_finufft_gb300 as jf
     from jax_finufft_gb300.options import Opts
     from oracle import cpu_nufft as cn
