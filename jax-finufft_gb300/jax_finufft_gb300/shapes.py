@@ -28,8 +28,61 @@ class BroadcastIndex:
         return out
 
 
+def _flat_vector_points(nufft_type, output_shape, source, points):
+    """The common case of one point set, every point array 1-D of one length
+    M: the general rules below reduce to reshapes (n_tot = 1; a source with
+    one leading axis is that many stacked transforms).  None when the inputs
+    are not of that form or disagree on the point count (the general path
+    then checks and reports them).  Same results as the general path, in a
+    few tensor operations instead of some twenty (per call that is most of
+    a small transform's host time)."""
+    if not all(isinstance(p, torch.Tensor) and p.ndim == 1 for p in points):
+        return None
+    m = points[0].shape[0]
+    if any(p.shape[0] != m for p in points[1:]):
+        return None
+    if nufft_type == 3:
+        num_dim = len(points) // 2
+        src_pts, tgt_pts = points[:num_dim], points[num_dim:]
+        n3 = tgt_pts[0].shape[0]
+        if any(p.shape[0] != n3 for p in tgt_pts[1:]):
+            return None
+        if any(p.shape[0] != m for p in src_pts):
+            return None
+        extra = (m,)
+        tail = (n3,)
+    elif nufft_type == 2:
+        num_dim = len(points)
+        extra = tuple(source.shape[source.ndim - num_dim:]) if source.ndim >= num_dim else None
+        tail = (m,)
+        if extra is None:
+            return None
+    else:
+        num_dim = len(points)
+        extra = (m,)
+        tail = tuple(output_shape) if output_shape is not None else None
+        if tail is None:
+            return None
+    lead = source.ndim - len(extra)
+    if lead == 0:
+        n_transf, expected = 1, tail
+    elif lead == 1:
+        n_transf, expected = int(source.shape[0]), (int(source.shape[0]),) + tail
+    else:
+        return None
+    if tuple(source.shape[lead:]) != extra:
+        return None
+    index = BroadcastIndex(broadcast_from=(), broadcast_to=(),
+                           expected_output_shape=expected)
+    flat = torch.reshape(source, (1, n_transf) + extra)
+    return (index, flat) + tuple(p.reshape(1, p.shape[0]) for p in points)
+
+
 def broadcast_and_flatten_inputs(nufft_type, output_shape, source, *points):
     """Port of shapes.py:27-126 (same dimension bookkeeping, torch ops)."""
+    fast = _flat_vector_points(nufft_type, output_shape, source, points)
+    if fast is not None:
+        return fast
     if nufft_type == 3:
         num_dim = len(points) // 2
         points3 = points[num_dim:]

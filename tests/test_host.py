@@ -98,6 +98,45 @@ def test_unflatten_roundtrip():
     assert tuple(out.shape) == (2, 3, 4)
 
 
+def _general_path(monkeypatch, *args):
+    monkeypatch.setattr(shapes, "_flat_vector_points", lambda *a: None)
+    try:
+        return shapes.broadcast_and_flatten_inputs(*args)
+    finally:
+        monkeypatch.undo()
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+@pytest.mark.parametrize("M", [1, 7])
+@pytest.mark.parametrize("T", [None, 1, 3])
+def test_vector_points_fast_path_matches_general_rules(monkeypatch, dim, M, T):
+    """One set of 1-D points (the common call): the shortcut's buffers, output
+    shape and unflattening equal the general broadcasting rules' for types
+    1, 2 and 3."""
+    g = torch.Generator().manual_seed(dim * 100 + M)
+    pts = [torch.randn(M, generator=g) for _ in range(dim)]
+    modes = (4, 5, 6)[:dim]
+    src1 = torch.randn(M, generator=g) if T is None else torch.randn(T, M, generator=g)
+    src2 = torch.randn(*modes, generator=g) if T is None else torch.randn(T, *modes, generator=g)
+    tgts = [torch.randn(5, generator=g) for _ in range(dim)]
+    cases = [(1, modes, src1, pts), (2, None, src2, pts), (3, None, src1, pts + tgts)]
+    for t, out_shape, src, ps in cases:
+        fast = shapes.broadcast_and_flatten_inputs(t, out_shape, src, *ps)
+        ref = _general_path(monkeypatch, t, out_shape, src, *ps)
+        assert tuple(fast[0].expected_output_shape) == tuple(ref[0].expected_output_shape)
+        for a, b in zip(fast[1:], ref[1:]):
+            assert a.shape == b.shape and torch.equal(a, b)
+        n_out = {1: modes, 2: (M,), 3: (5,)}[t]
+        res = torch.randn(*fast[1].shape[:2], *n_out, generator=g)
+        assert torch.equal(fast[0].unflatten(res), ref[0].unflatten(res))
+
+
+def test_vector_points_of_different_lengths_take_the_general_path():
+    with pytest.raises((AssertionError, RuntimeError)):
+        shapes.broadcast_and_flatten_inputs(1, (4, 4), torch.zeros(5), torch.zeros(5),
+                                            torch.zeros(6))
+
+
 # --- options (port of the reference's tests/options_test.py) ------------------
 @pytest.mark.parametrize("opts", [None, options.Opts()])
 def test_default_options(opts):
