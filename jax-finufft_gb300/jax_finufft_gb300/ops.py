@@ -25,6 +25,7 @@ import threading
 
 import numpy as np
 import torch
+import torch.autograd.forward_ad as _forward_ad
 
 from . import _fused, _native, tune
 from .options import Opts, to_native, unpack_opts
@@ -154,6 +155,28 @@ def _wants_fused(nufft_type, opts, source, points):
         if any(p.requires_grad for p in points[nd:]):
             return False
     return bool(source.requires_grad or any(p.requires_grad for p in points))
+
+
+def _no_transform_active(source, points):
+    """True when nothing needs the autograd Function around a call: no input
+    requires grad (or grad mode is off), no forward-mode dual level is open
+    and no functorch transform (vmap, grad, jvp) is active.  The Function's
+    machinery then costs more host time than a small transform's kernels;
+    with an unknown torch the Function is always used."""
+    if torch.is_grad_enabled() and (source.requires_grad
+                                    or any(p.requires_grad for p in points)):
+        return False
+    level = getattr(_forward_ad, "_current_level", None)
+    active = getattr(torch._C, "_are_functorch_transforms_active", None)
+    if level is None or level != -1 or active is None:
+        return False
+    return not active()
+
+
+def _apply(source, nufft_type, output_shape, iflag, eps, opts, fused, *points):
+    if not fused and _no_transform_active(source, points):
+        return _execute(nufft_type, source, points, output_shape, iflag, eps, opts)
+    return _Nufft.apply(source, nufft_type, output_shape, iflag, eps, opts, fused, *points)
 
 
 class _Nufft(torch.autograd.Function):
@@ -370,7 +393,7 @@ def nufft1(output_shape, source, *points, iflag=1, eps=1e-6, opts=None):
     output_shape = tuple(int(n) for n in output_shape)
     index, source, *points = broadcast_and_flatten_inputs(1, output_shape, source, *points)
     fused = _wants_fused(1, opts, source, points)
-    result = _Nufft.apply(source, 1, output_shape, iflag, eps, opts, fused, *points)
+    result = _apply(source, 1, output_shape, iflag, eps, opts, fused, *points)
     return index.unflatten(result)
 
 
@@ -383,7 +406,7 @@ def nufft2(source, *points, iflag=-1, eps=1e-6, opts=None):
         raise ValueError("Only 1-, 2-, and 3-dimensions are supported")
     index, source, *points = broadcast_and_flatten_inputs(2, None, source, *points)
     fused = _wants_fused(2, opts, source, points)
-    result = _Nufft.apply(source, 2, None, iflag, eps, opts, fused, *points)
+    result = _apply(source, 2, None, iflag, eps, opts, fused, *points)
     return index.unflatten(result)
 
 
@@ -399,5 +422,5 @@ def nufft3(source, *points, iflag=-1, eps=1e-6, opts=None):
         raise ValueError("Only 1-, 2-, and 3-dimensions are supported")
     index, source, *points = broadcast_and_flatten_inputs(3, None, source, *points)
     fused = _wants_fused(3, opts, source, points)
-    result = _Nufft.apply(source, 3, None, iflag, eps, opts, fused, *points)
+    result = _apply(source, 3, None, iflag, eps, opts, fused, *points)
     return index.unflatten(result)
