@@ -50,6 +50,22 @@ def get_frequency_array(n, modeord):
     raise ValueError(f"Unsupported modeord: {modeord}")
 
 
+_DEFAULT_OPTS = Opts()
+
+# gbn_opts structs of the options seen by _execute, by value (Opts is frozen;
+# the structs are passed read-only to the library and never modified here)
+_native_cache = {}
+
+
+def _native_opts(fwd):
+    n = _native_cache.get(fwd)
+    if n is None:
+        if len(_native_cache) > 64:
+            _native_cache.clear()
+        n = _native_cache[fwd] = to_native(fwd)
+    return n
+
+
 def _modeord(opts):
     return int(opts.modeord) if hasattr(opts, "modeord") else 0
 
@@ -64,7 +80,7 @@ def _execute(nufft_type, source, points, output_shape, iflag, eps, opts):
     ndim = len(points) // 2 if nufft_type == 3 else len(points)
     fwd = unpack_opts(opts, nufft_type, True)
     if fwd is None:
-        fwd = Opts()
+        fwd = _DEFAULT_OPTS
     n_tot, n_transf = int(source.shape[0]), int(source.shape[1])
     n_j = int(points[0].shape[1])
     if nufft_type == 1:
@@ -90,7 +106,7 @@ def _execute(nufft_type, source, points, output_shape, iflag, eps, opts):
     eps_v = float(np.float32(eps)) if single else float(eps)
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev).cuda_stream
-        native = to_native(fwd)
+        native = _native_opts(fwd)
         if getattr(fwd, "gpu_autotune", False) and nufft_type in (1, 2):
             native, _ = tune.tuned_native(nufft_type, ndim, single, nk_b, n_j, n_transf, eps_v,
                                           int(iflag), native, stream)
