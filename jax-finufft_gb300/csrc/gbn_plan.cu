@@ -414,6 +414,30 @@ struct gbn_plan_s {
   // debug timings: 4 events per executed batch (stage boundaries) and 2 per
   // setpts, recorded without host synchronisation and summed by
   // gbn_get_timings, which then resets the pool.
+  // per-call driver (gbn_run): the arguments of recent calls and, for
+  // arguments that came again, that call's setpts + execute captured as a
+  // CUDA graph, replayed by later identical calls (types 1 and 2).  All are
+  // for one (n_tot, n_j): a call of other sizes may grow the plan's buffers
+  // and drops them first.
+  struct OneshotArgs {
+    int64_t n_tot, n_j, n_k_total;
+    const void* src;
+    void* out;
+    const void* pts[3];
+  };
+  static constexpr size_t kOneshotKeep = 4;
+  std::vector<OneshotArgs> os_seen;
+  std::vector<std::pair<OneshotArgs, cudaGraphExec_t>> os_graphs;
+  bool os_nograph = false;  // a capture failed: no graphs for this plan
+  // stream the graphs are captured on (the caller's may be the legacy
+  // default stream, which cannot be captured; a graph launches on any)
+  cudaStream_t os_cap = nullptr;
+  void os_clear() {
+    for (auto& g : os_graphs) cudaGraphExecDestroy(g.second);
+    os_graphs.clear();
+    os_seen.clear();
+  }
+
   bool ev_ok = false;
   std::vector<cudaEvent_t> ev_exec, ev_setpts;
   size_t ev_exec_used = 0, ev_setpts_used = 0;
@@ -433,6 +457,8 @@ struct gbn_plan_s {
     fft_work.release(stream);
     for (auto& e : ev_exec) cudaEventDestroy(e);
     for (auto& e : ev_setpts) cudaEventDestroy(e);
+    os_clear();
+    if (os_cap) cudaStreamDestroy(os_cap);
     cudaStreamSynchronize(stream);
   }
 };
@@ -1509,29 +1535,117 @@ int run_oneshot(int type, int dim, bool single, void* stream, double eps, int if
     warn = p->warn;
   }
   const size_t dsz = cplx_size(single);
-  int ret = GBN_OK;
-  for (int64_t idx = 0; idx < n_tot && ret < 2; ++idx) {
-    const int64_t i = idx * n_j;
-    const int64_t j = idx * n_j * n_transf;
-    const int64_t k = idx * n_k_total * n_transf;
-    const TX* xs[3] = {nullptr, nullptr, nullptr};
-    const TX* ss[3] = {nullptr, nullptr, nullptr};
-    for (int d = 0; d < dim; ++d) {
-      xs[d] = pts[d] ? pts[d] + i : nullptr;
-      if (type == 3) ss[d] = tgts[d] ? tgts[d] + idx * n_k_total : nullptr;
+  // Identical calls (same plan, sizes and buffers) replay a CUDA graph of
+  // the previous one: one launch instead of a dozen, the host time of a
+  // small transform.  Buffers of a plan only grow for other sizes, so the
+  // graph's addresses stay valid while the arguments repeat.  Not while the
+  // caller's stream is being captured (the work joins that capture) or with
+  // debug timings; never for type 3 (its setpts may read the host).
+  gbn_plan_s::OneshotArgs oa{};
+  oa.n_tot = n_tot;
+  oa.n_j = n_j;
+  oa.n_k_total = n_k_total;
+  oa.src = source;
+  oa.out = output;
+  for (int d = 0; d < dim; ++d) oa.pts[d] = pts[d];
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GBN_CUDA(cudaStreamIsCapturing((cudaStream_t)stream, &cap));
+  const bool graphable = type != 3 && !p->ev_ok && !p->os_nograph &&
+                         cap == cudaStreamCaptureStatusNone;
+  auto eq = [&](const gbn_plan_s::OneshotArgs& o) {
+    return std::memcmp(&o, &oa, sizeof(oa)) == 0;
+  };
+  // other sizes than the kept calls': their graphs and records go first
+  if ((!p->os_seen.empty() &&
+       (p->os_seen.front().n_j != n_j || p->os_seen.front().n_tot != n_tot)) ||
+      (!p->os_graphs.empty() &&
+       (p->os_graphs.front().first.n_j != n_j || p->os_graphs.front().first.n_tot != n_tot)))
+    p->os_clear();
+  if (graphable) {
+    for (auto& g : p->os_graphs) {
+      if (!eq(g.first)) continue;
+      const cudaError_t e = cudaGraphLaunch(g.second, (cudaStream_t)stream);
+      if (e != cudaSuccess) {
+        delete p;
+        return fail(GBN_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e));
+      }
+      cache().give(key, p);
+      return warn ? GBN_WARN_EPS_TOO_SMALL : GBN_OK;
     }
-    ret = plan_setpts<TX>(p, n_j, xs[0], xs[1], xs[2], type == 3 ? n_k_total : 0, ss[0], ss[1],
-                          ss[2]);
-    if (ret >= 2) break;
-    const char* src = (const char*)source;
-    char* out = (char*)output;
-    if (type == 2)
-      ret = execute_ntr(p, p->own, out + (size_t)j * dsz, (void*)(src + (size_t)k * dsz),
-                        p->ntransf, 1);
-    else
-      ret = execute_ntr(p, p->own, (void*)(src + (size_t)j * dsz), out + (size_t)k * dsz,
-                        p->ntransf, 1);
   }
+  bool same = false;  // seen before, not yet a graph
+  for (const auto& o : p->os_seen) same = same || eq(o);
+  if (!same) {
+    if (p->os_seen.size() >= gbn_plan_s::kOneshotKeep) p->os_seen.erase(p->os_seen.begin());
+    p->os_seen.push_back(oa);
+  }
+  // the setpts + execute of every n_tot slice
+  auto run_all = [&]() -> int {
+    int r = GBN_OK;
+    for (int64_t idx = 0; idx < n_tot && r < 2; ++idx) {
+      const int64_t i = idx * n_j;
+      const int64_t j = idx * n_j * n_transf;
+      const int64_t k = idx * n_k_total * n_transf;
+      const TX* xs[3] = {nullptr, nullptr, nullptr};
+      const TX* ss[3] = {nullptr, nullptr, nullptr};
+      for (int d = 0; d < dim; ++d) {
+        xs[d] = pts[d] ? pts[d] + i : nullptr;
+        if (type == 3) ss[d] = tgts[d] ? tgts[d] + idx * n_k_total : nullptr;
+      }
+      r = plan_setpts<TX>(p, n_j, xs[0], xs[1], xs[2], type == 3 ? n_k_total : 0, ss[0], ss[1],
+                          ss[2]);
+      if (r >= 2) break;
+      const char* src = (const char*)source;
+      char* out = (char*)output;
+      if (type == 2)
+        r = execute_ntr(p, p->own, out + (size_t)j * dsz, (void*)(src + (size_t)k * dsz),
+                        p->ntransf, 1);
+      else
+        r = execute_ntr(p, p->own, (void*)(src + (size_t)j * dsz), out + (size_t)k * dsz,
+                        p->ntransf, 1);
+    }
+    return r;
+  };
+  int ret = GBN_OK;
+  bool done = false;
+  if (graphable && same && !p->os_cap &&
+      cudaStreamCreateWithFlags(&p->os_cap, cudaStreamNonBlocking) != cudaSuccess) {
+    p->os_cap = nullptr;
+    p->os_nograph = true;
+    cudaGetLastError();
+  }
+  if (graphable && same && p->os_cap &&
+      cudaStreamBeginCapture(p->os_cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    // the second identical call: capture it on the plan's capture stream,
+    // then launch the graph on the caller's (the captured work has not run
+    // yet); any failure on the way disables graphs for this plan and the
+    // call runs directly
+    cudaStream_t user = p->stream;
+    p->stream = p->os_cap;
+    const int r = run_all();
+    p->stream = user;
+    p->own.stream = user;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(p->os_cap, &graph);
+    const bool made = r < 2 && e == cudaSuccess && graph &&
+                      cudaGraphInstantiate(&ex, graph, 0) == cudaSuccess;
+    if (made && cudaGraphLaunch(ex, (cudaStream_t)stream) == cudaSuccess) {
+      if (p->os_graphs.size() >= gbn_plan_s::kOneshotKeep) {
+        cudaGraphExecDestroy(p->os_graphs.front().second);
+        p->os_graphs.erase(p->os_graphs.begin());
+      }
+      p->os_graphs.emplace_back(oa, ex);
+      done = true;
+    } else {
+      if (made) cudaGraphExecDestroy(ex);
+      p->os_nograph = true;
+      cudaGetLastError();
+    }
+    if (graph) cudaGraphDestroy(graph);
+  }
+  if (graphable && same && !done) cudaGetLastError();  // a refused capture's status
+  if (!done) ret = run_all();
   if (ret >= 2) {
     delete p;  // state unknown after a failure: do not cache
     return ret;
